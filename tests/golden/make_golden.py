@@ -1,0 +1,184 @@
+"""Generate the golden vectors in tests/golden/ from the reference module itself.
+
+Run in a container that has the reference checked out (default path below, or
+pass it as the first argument).  The reference is imported unmodified:
+  * Parameter_inversion/Inversion_adam.py is imported as a module with stub
+    modules for matplotlib and h5py (absent here, unused on this path);
+  * Damage_inversion/Inversion_adam.py selects a GPU at import time
+    (Inversion_adam.py:36-43), so only its definitions are extracted with `ast`
+    and executed with `device` bound to the CPU.
+
+Each fixture stores the exact inputs the reference used (constants after
+exp/clamp, the Gaussian load map, the source signal) and its outputs
+(operator values, forward histories, loss, autograd gradients), in FP32 and in
+the FP64 run of the same scheme (torch default dtype float64).
+"""
+from __future__ import annotations
+
+import ast
+import importlib.util
+import os
+import sys
+import types
+from unittest import mock
+
+import numpy as np
+import torch
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = os.path.dirname(os.path.abspath(__file__))
+sys.dont_write_bytecode = True
+
+
+def _stub_plotting():
+    for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.ticker", "mpl_toolkits",
+                 "mpl_toolkits.axes_grid1", "h5py"]:
+        sys.modules.setdefault(name, mock.MagicMock(name=name))
+
+
+def load_param_module():
+    _stub_plotting()
+    path = os.path.join(REF, "Parameter_inversion", "Inversion_adam.py")
+    spec = importlib.util.spec_from_file_location("ref_param_inversion", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_damage_defs():
+    path = os.path.join(REF, "Damage_inversion", "Inversion_adam.py")
+    tree = ast.parse(open(path).read(), filename=path)
+    keep = {"gaussian_point_load", "ricker_wavelet", "conv2d_fixed",
+            "_general_anisotropic_elastic_operator_with_force_spatially_varying",
+            "total_variation_2d", "SpatiallyVaryingAnisotropicSimulator",
+            "SpatiallyVaryingParameterInverter"}
+    body = [n for n in tree.body
+            if isinstance(n, (ast.FunctionDef, ast.ClassDef)) and n.name in keep]
+    ns = {"torch": torch, "nn": torch.nn, "F": torch.nn.functional, "np": np,
+          "optim": torch.optim, "os": os, "device": torch.device("cpu")}
+    exec(compile(ast.Module(body=body, type_ignores=[]), path, "exec"), ns)
+    return types.SimpleNamespace(**{k: ns[k] for k in keep})
+
+
+# --------------------------------------------------------------------------
+H, DT, RHO = 1e-4, 5e-9, 1610.0
+TRUE = dict(C11=160.06e9, C22=70.86e9, C12=48.04e9, C16=9.48e9, C26=16.27e9, C66=37.64e9)
+INIT = dict(C11=150e9, C22=75e9, C12=45e9, C16=11e9, C26=15e9, C66=39e9)
+SRC = dict(source_f0=4e6, source_t0=2.5e-7, source_amplitude=1e10, gaussian_param=5e6)
+
+
+def param_case(P, dtype, domain=(24, 20), nt=150, stride=5, ts=2, ss=3):
+    torch.set_default_dtype(dtype)
+    try:
+        def make(C):
+            return P.CFRPWaveSimulatorRicker(
+                domain, H, DT, nt, stride, source_component="y", rho_known=RHO,
+                source_position=(0.0, 0.0),
+                C11_init=C["C11"], C22_init=C["C22"], C12_init=C["C12"],
+                C16_init=C["C16"], C26_init=C["C26"], C66_init=C["C66"], **SRC)
+        true_sim = make(TRUE)
+        with torch.no_grad():
+            tx, ty = true_sim()
+        sim = make(INIT)
+        inv = P.CFRPParameterInverterRicker(sim, tx, ty, secondary_time_stride=ts,
+                                            secondary_space_stride=ss)
+        ux, uy = sim(save_all_steps=False)
+        loss = inv.compute_loss(ux, uy)
+        loss.backward()
+        C = sim.get_material_params()
+        names = ["log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66"]
+        return dict(
+            nx=domain[0], ny=domain[1], nt=nt, stride=stride, ts=ts, ss=ss, h=H, dt=DT,
+            rho=float(sim.rho), C=np.array([float(c) for c in C[:6]], np.float64),
+            C_true=np.array([float(c) for c in true_sim.get_material_params()[:6]]),
+            gauss=sim.gaussian_dist.detach().double().numpy(),
+            signal=sim.source_signal.detach().double().numpy()[0],
+            hist_ux=ux.detach().double().numpy(), hist_uy=uy.detach().double().numpy(),
+            target_ux=tx.double().numpy(), target_uy=ty.double().numpy(),
+            loss=float(loss), grad_log=np.array([float(getattr(sim, n).grad) for n in names]))
+    finally:
+        torch.set_default_dtype(torch.float32)
+
+
+def operator_case(P, Dm, dtype, nx=19, ny=16, nsq=17, seed=3):
+    torch.set_default_dtype(dtype)
+    try:
+        g = torch.Generator().manual_seed(seed)
+        ux = torch.randn(1, nx, ny, generator=g) * 1e-3
+        uy = torch.randn(1, nx, ny, generator=g) * 1e-3
+        fx = torch.randn(1, nx, ny, generator=g) * 1e16
+        fy = torch.randn(1, nx, ny, generator=g) * 1e16
+        Cs = [torch.tensor(v, dtype=torch.float32) for v in TRUE.values()]
+        rho = torch.tensor(RHO, dtype=torch.float32)
+        Lx, Ly = P._general_anisotropic_elastic_operator_with_force(ux, uy, *Cs, H, fx, fy, rho)
+        # The spatially varying operator adds the force transposed
+        # (Damage_inversion/Inversion_adam.py:169-174), so it only accepts square
+        # grids; its case uses its own square fields and an asymmetric force.
+        n = nsq
+        vx = torch.randn(1, n, n, generator=g) * 1e-3
+        vy = torch.randn(1, n, n, generator=g) * 1e-3
+        gx = torch.randn(1, n, n, generator=g) * 1e16
+        gy = torch.randn(1, n, n, generator=g) * 1e16
+        base = torch.tensor(list(TRUE.values()), dtype=torch.float32).view(6, 1, 1)
+        fields = (base * (1 + 0.2 * torch.rand(6, n, n, generator=g))).to(torch.float32)
+        Lxf, Lyf = Dm._general_anisotropic_elastic_operator_with_force_spatially_varying(
+            vx, vy, *[fields[t:t + 1] for t in range(6)], H, gx, gy, rho)
+        d = lambda a: a.detach().double().numpy()
+        return dict(nx=nx, ny=ny, h=H, rho=RHO, C=np.array([float(c) for c in Cs]),
+                    ux=d(ux[0]), uy=d(uy[0]), fx=d(fx[0]), fy=d(fy[0]),
+                    Lux=d(Lx[0]), Luy=d(Ly[0]), nsq=n, C_fields=d(fields), vx=d(vx[0]),
+                    vy=d(vy[0]), gx=d(gx[0]), gy=d(gy[0]), Lux_fields=d(Lxf[0]),
+                    Luy_fields=d(Lyf[0]))
+    finally:
+        torch.set_default_dtype(torch.float32)
+
+
+def damage_case(Dm, dtype, domain=(20, 20), nt=120, stride=5, ts=2, seed=7):
+    torch.set_default_dtype(dtype)
+    try:
+        base = dict(C11_init=130.74e9, C22_init=11.50e9, C12_init=10.49e9, C16_init=30.67e9,
+                    C26_init=3.75e9, C66_init=14.77e9)
+        def make():
+            return Dm.SpatiallyVaryingAnisotropicSimulator(
+                domain, H, DT, nt, stride, source_component="y", total_time=nt * DT,
+                rho_known=RHO, use_log_params=True, **base, **SRC)
+        healthy = make()
+        with torch.no_grad():
+            tx, ty = healthy()
+        sim = make()
+        g = torch.Generator().manual_seed(seed)
+        with torch.no_grad():
+            for n in ["log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66"]:
+                p = getattr(sim, n)
+                p.add_(0.08 * torch.randn(p.shape, generator=g))
+        inv = Dm.SpatiallyVaryingParameterInverter(sim, tx, ty, secondary_time_stride=ts,
+                                                   lambda_tv=0.0)
+        ux, uy = sim(save_all_steps=False)
+        loss, _, _ = inv.compute_loss(ux, uy)
+        loss.backward()
+        C = sim.get_material_params()
+        names = ["log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66"]
+        d = lambda a: a.detach().double().numpy()
+        return dict(
+            nx=domain[0], ny=domain[1], nt=nt, stride=stride, ts=ts, h=H, dt=DT,
+            rho=float(sim.rho), C_fields=np.stack([d(c[0]) for c in C[:6]]),
+            gauss=d(sim.gaussian_dist), signal=d(sim.source_signal)[0],
+            hist_ux=d(ux), hist_uy=d(uy), target_ux=d(tx), target_uy=d(ty), loss=float(loss),
+            grad_log=np.stack([d(getattr(sim, n).grad[0]) for n in names]))
+    finally:
+        torch.set_default_dtype(torch.float32)
+
+
+def main():
+    torch.manual_seed(0)
+    P = load_param_module()
+    Dm = load_damage_defs()
+    for tag, dtype in (("f32", torch.float32), ("f64", torch.float64)):
+        np.savez_compressed(os.path.join(OUT, f"operator_{tag}.npz"), **operator_case(P, Dm, dtype))
+        np.savez_compressed(os.path.join(OUT, f"param_inversion_{tag}.npz"), **param_case(P, dtype))
+        np.savez_compressed(os.path.join(OUT, f"damage_inversion_{tag}.npz"), **damage_case(Dm, dtype))
+    print("wrote fixtures to", OUT)
+
+
+if __name__ == "__main__":
+    main()
