@@ -1,0 +1,34 @@
+"""GB300-native ERNN propagation: the time-recurrent anisotropic elastic FD cell
+and its hand-written adjoint, running in libernn_gb300.so (sm_103a).
+
+Public surface:
+  CFRPWaveSimulatorRicker, SpatiallyVaryingAnisotropicSimulator
+      drop-in replacements of the reference's simulator modules;
+  ShotGatherSimulator, DegradationSimulator
+      receiver-trace and degradation-map forms;
+  ErnnPropagate / propagate, Geometry
+      the autograd Function over the C ABI;
+  elastic_operator_with_force
+      one application of the operator;
+  sources, materials, harness
+      source signals and loads, in-plane rotation and stability, benchmark
+      configurations.
+"""
+from . import _lib, materials, sources
+from .propagate import (MODE_DFIELD, MODE_FIELDS, MODE_SCALAR, RECORD_FIELDS,
+                        RECORD_RECEIVERS, ErnnPropagate, Geometry,
+                        elastic_operator_with_force, propagate)
+from .simulators import (CFRPWaveSimulatorRicker, DegradationSimulator, ShotGatherSimulator,
+                         SpatiallyVaryingAnisotropicSimulator)
+
+__all__ = [
+    "CFRPWaveSimulatorRicker", "SpatiallyVaryingAnisotropicSimulator", "ShotGatherSimulator",
+    "DegradationSimulator", "ErnnPropagate", "Geometry", "propagate",
+    "elastic_operator_with_force", "sources", "materials", "MODE_SCALAR", "MODE_DFIELD",
+    "MODE_FIELDS", "RECORD_FIELDS", "RECORD_RECEIVERS", "load_library",
+]
+
+
+def load_library():
+    """Load (building in-tree if needed) libernn_gb300.so; raises if unavailable."""
+    return _lib.load()

@@ -1,0 +1,336 @@
+// C ABI entry points of libernn_gb300.so (declared in include/ernn.h) and the
+// host-side time-loop driver: step schedule, checkpoint/recompute plan,
+// workspace layout.  Every launch goes on the caller's stream; nothing here
+// synchronises the host or allocates device memory.
+#include <cmath>
+#include <cstring>
+
+#include "ernn.h"
+#include "ernn_launch.h"
+
+namespace ernn {
+namespace {
+
+constexpr size_t kAlign = 256;
+constexpr double kPi = 3.14159265358979323846;
+inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+// Workspace plan of one problem.
+struct Plan {
+  int S, nx, ny, nt, k, nseg, nt_out, nblocks;
+  bool store_all;
+  size_t N, state_bytes;
+  // tape
+  size_t t_coef, t_A, t_B, t_store, t_total_tape, t_total_notape;
+  // adjoint scratch
+  size_t s_coef, s_LA, s_LB, s_seg, s_gacc, s_part, s_total;
+};
+
+Plan make_plan(const ErnnProblem& p) {
+  Plan pl{};
+  pl.S = p.nshots; pl.nx = p.nx; pl.ny = p.ny; pl.nt = p.nt;
+  pl.k = p.ckpt_k < p.nt ? p.ckpt_k : p.nt;
+  pl.nseg = (p.nt + pl.k - 1) / pl.k;
+  pl.store_all = (pl.nseg == 1);
+  pl.nt_out = (p.nt + p.stride - 1) / p.stride;
+  pl.N = (size_t)p.nx * p.ny;
+  pl.state_bytes = align_up((size_t)p.nshots * 2 * pl.N * sizeof(float));
+  const dim3 g = step_grid(p.nx, p.ny, p.nshots);
+  pl.nblocks = (int)(g.x * g.y * g.z);
+  size_t off = 0;
+  pl.t_coef = off; off += align_up(sizeof(Coef));
+  pl.t_A = off; off += pl.state_bytes;
+  pl.t_B = off; off += pl.state_bytes;
+  pl.t_total_notape = off;
+  pl.t_store = off;
+  if (pl.store_all) off += (size_t)p.nt * pl.state_bytes;           // u^1..u^nt
+  else off += (size_t)(pl.nseg - 1) * 2 * pl.state_bytes;          // (u^{jk}, u^{jk-1})
+  pl.t_total_tape = off;
+  off = 0;
+  pl.s_coef = off; off += align_up(sizeof(Coef));
+  pl.s_LA = off; off += pl.state_bytes;
+  pl.s_LB = off; off += pl.state_bytes;
+  pl.s_seg = off; if (!pl.store_all) off += (size_t)pl.k * pl.state_bytes;
+  pl.s_gacc = off;
+  if (p.mode == kModeDField) off += align_up((size_t)p.nshots * pl.N * sizeof(float));
+  if (p.mode == kModeFields) off += align_up((size_t)p.nshots * 6 * pl.N * sizeof(float));
+  pl.s_part = off;
+  if (p.mode == kModeScalar) off += align_up((size_t)pl.nblocks * 8 * sizeof(double));
+  pl.s_total = off;
+  return pl;
+}
+
+int validate(const ErnnProblem* p) {
+  if (p == nullptr) return ERNN_ERR_INVALID;
+  if (p->nshots < 1 || p->nshots > 65535 || p->nx < 1 || p->ny < 1 || p->nt < 1 ||
+      p->stride < 1 || p->ckpt_k < 1)
+    return ERNN_ERR_INVALID;
+  if ((int64_t)p->nx * p->ny >= ((int64_t)1 << 31) || p->nx > 2000000) return ERNN_ERR_INVALID;
+  if (p->mode < kModeScalar || p->mode > kModeFields) return ERNN_ERR_INVALID;
+  if (p->record != kRecordFields && p->record != kRecordReceivers) return ERNN_ERR_INVALID;
+  if (p->record == kRecordReceivers && p->nrec < 1) return ERNN_ERR_INVALID;
+  if (p->src_comp != 0 && p->src_comp != 1) return ERNN_ERR_INVALID;
+  if (p->src_bx < 0 || p->src_by < 0) return ERNN_ERR_INVALID;
+  if (!(p->h > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->h) || !std::isfinite(p->dt))
+    return ERNN_ERR_INVALID;
+  return ERNN_OK;
+}
+
+int validate_inputs(const ErnnProblem* p, const ErnnInputs* in) {
+  if (in == nullptr || in->C == nullptr || in->rho == nullptr || in->src_signal == nullptr)
+    return ERNN_ERR_INVALID;
+  if (p->mode == kModeDField && in->D == nullptr) return ERNN_ERR_INVALID;
+  if ((size_t)p->src_bx * p->src_by > 0 && (in->src_map == nullptr || in->src_origin == nullptr))
+    return ERNN_ERR_INVALID;
+  if (p->record == kRecordReceivers && in->rec_idx == nullptr) return ERNN_ERR_INVALID;
+  return ERNN_OK;
+}
+
+inline char* at(void* base, size_t off) { return static_cast<char*>(base) + off; }
+inline float* fat(void* base, size_t off) { return reinterpret_cast<float*>(at(base, off)); }
+
+#define ERNN_CUDA(expr)                      \
+  do {                                       \
+    if ((expr) != cudaSuccess) return ERNN_ERR_CUDA; \
+  } while (0)
+
+FwdStep base_fwd(const ErnnProblem& p, const ErnnInputs& in, const Coef* coef, int nt_out) {
+  FwdStep a;
+  std::memset(&a, 0, sizeof(a));
+  a.nx = p.nx; a.ny = p.ny; a.S = p.nshots; a.nt = p.nt;
+  a.frame = -1; a.gframe = -1; a.nt_out = nt_out;
+  a.coef = coef;
+  a.field = (p.mode == kModeFields) ? in.C : in.D;
+  a.src_signal = in.src_signal;
+  a.src_map = in.src_map;
+  a.src_origin = in.src_origin;
+  a.bx = p.src_bx; a.by = p.src_by; a.src_comp = p.src_comp;
+  a.rec_idx = in.rec_idx;
+  a.nrec = p.nrec;
+  return a;
+}
+
+}  // namespace
+}  // namespace ernn
+
+using namespace ernn;
+
+extern "C" {
+
+int ernn_abi_version(void) { return ERNN_ABI_VERSION; }
+
+const char* ernn_error_string(int code) {
+  switch (code) {
+    case ERNN_OK: return "ok";
+    case ERNN_ERR_INVALID: return "invalid argument (null pointer, size or enum out of range)";
+    case ERNN_ERR_WORKSPACE: return "workspace smaller than the size query returned";
+    case ERNN_ERR_CUDA: return "CUDA runtime call failed";
+    case ERNN_ERR_UNSTABLE: return "leapfrog stability bound violated for these constants";
+    case ERNN_ERR_TIMEOUT: return "bounded device-side wait timed out";
+    case ERNN_ERR_UNSUPPORTED: return "request not supported by this build";
+    default: return "unknown error code";
+  }
+}
+
+int ernn_validate(const ErnnProblem* p) { return validate(p); }
+
+size_t ernn_tape_bytes(const ErnnProblem* p, int with_tape) {
+  if (validate(p) != ERNN_OK) return 0;
+  const Plan pl = make_plan(*p);
+  return with_tape ? pl.t_total_tape : pl.t_total_notape;
+}
+
+size_t ernn_adjoint_scratch_bytes(const ErnnProblem* p) {
+  if (validate(p) != ERNN_OK) return 0;
+  return make_plan(*p).s_total;
+}
+
+int ernn_check_stability(const double* C, double rho, double h, double dt, double* courant) {
+  if (C == nullptr || !(rho > 0.0) || !(h > 0.0) || !(dt > 0.0)) return ERNN_ERR_INVALID;
+  // Symbol of -(h^2) A on the Fourier mode exp(i(tx*i + ty*j)):
+  //   a = 4 sin^2(tx/2), b = 4 sin^2(ty/2), d = sin(tx) sin(ty)
+  //   Mxx = C11 a + C66 b + 2 C16 d,  Myy = C66 a + C22 b + 2 C26 d,
+  //   Mxy = C16 a + C26 b + (C12 + C66) d.
+  // Leapfrog is stable when every eigenvalue of (dt^2 / (rho h^2)) M lies in [0, 4].
+  const double q = dt * dt / (rho * h * h);
+  const int n = 128;
+  double worst = 0.0;
+  bool indefinite = false;
+  for (int u = 0; u <= n; ++u) {
+    for (int v = 0; v <= n; ++v) {
+      const double tx = kPi * u / n, ty = kPi * v / n;
+      const double a = 4.0 * std::sin(tx / 2) * std::sin(tx / 2);
+      const double b = 4.0 * std::sin(ty / 2) * std::sin(ty / 2);
+      for (int sgn = -1; sgn <= 1; sgn += 2) {
+        const double d = sgn * std::sin(tx) * std::sin(ty);
+        const double mxx = C[0] * a + C[5] * b + 2 * C[3] * d;
+        const double myy = C[5] * a + C[1] * b + 2 * C[4] * d;
+        const double mxy = C[3] * a + C[4] * b + (C[2] + C[5]) * d;
+        const double tr = mxx + myy, det = mxx * myy - mxy * mxy;
+        const double disc = std::sqrt(std::fmax(tr * tr / 4 - det, 0.0));
+        const double lmax = tr / 2 + disc, lmin = tr / 2 - disc;
+        if (lmin < -1e-9 * std::fabs(lmax)) indefinite = true;
+        if (q * lmax / 4.0 > worst) worst = q * lmax / 4.0;
+      }
+    }
+  }
+  if (courant) *courant = worst;
+  return (worst > 1.0 || indefinite) ? ERNN_ERR_UNSTABLE : ERNN_OK;
+}
+
+int ernn_operator(int32_t nshots, int32_t nx, int32_t ny, int32_t mode, double h, const float* C,
+                  const float* D, const float* rho, const float* ux, const float* uy,
+                  const float* fx, const float* fy, float* Lux, float* Luy, void* stream) {
+  if (nshots < 1 || nx < 1 || ny < 1 || mode < 0 || mode > 2 || !(h > 0.0)) return ERNN_ERR_INVALID;
+  if (C == nullptr || rho == nullptr || ux == nullptr || uy == nullptr || Lux == nullptr ||
+      Luy == nullptr || (mode == kModeDField && D == nullptr))
+    return ERNN_ERR_INVALID;
+  ERNN_CUDA(launch_operator(nshots, nx, ny, mode, h, C, D, rho, ux, uy, fx, fy, Lux, Luy,
+                            (cudaStream_t)stream));
+  return ERNN_OK;
+}
+
+int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, float* out_uy,
+                 void* tape, size_t tape_bytes, int with_tape, void* stream) {
+  int rc = validate(p);
+  if (rc) return rc;
+  if ((rc = validate_inputs(p, in))) return rc;
+  if (out_ux == nullptr || out_uy == nullptr || tape == nullptr) return ERNN_ERR_INVALID;
+  const Plan pl = make_plan(*p);
+  if (tape_bytes < (with_tape ? pl.t_total_tape : pl.t_total_notape)) return ERNN_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  Coef* coef = reinterpret_cast<Coef*>(at(tape, pl.t_coef));
+  ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st));
+
+  const bool store_all = with_tape && pl.store_all;
+  float* A = fat(tape, pl.t_A);
+  float* B = fat(tape, pl.t_B);
+  auto stored = [&](int n) { return fat(tape, pl.t_store + (size_t)(n - 1) * pl.state_bytes); };
+  auto ck = [&](int j, int lev) {  // checkpoint j >= 1: lev 0 = u^{jk}, lev 1 = u^{jk-1}
+    return fat(tape, pl.t_store + ((size_t)(j - 1) * 2 + lev) * pl.state_bytes);
+  };
+  const bool receivers = (p->record == kRecordReceivers);
+  FwdStep a = base_fwd(*p, *in, coef, pl.nt_out);
+  const float* last = nullptr;
+  for (int i = 0; i < p->nt; ++i) {
+    if (store_all) {
+      a.out = stored(i + 1);
+      a.cur = i >= 1 ? stored(i) : nullptr;
+      a.prev = i >= 2 ? stored(i - 1) : nullptr;
+    } else {
+      a.out = (i % 2 == 0) ? A : B;
+      a.cur = i == 0 ? nullptr : ((i % 2 == 0) ? B : A);
+      a.prev = i <= 1 ? nullptr : a.out;
+    }
+    a.i = i;
+    a.copy0 = a.copy1 = nullptr;
+    if (with_tape && !pl.store_all) {
+      if ((i + 1) % pl.k == 0 && (i + 1) / pl.k <= pl.nseg - 1) a.copy0 = ck((i + 1) / pl.k, 0);
+      if ((i + 2) % pl.k == 0 && (i + 2) / pl.k <= pl.nseg - 1) a.copy1 = ck((i + 2) / pl.k, 1);
+    }
+    a.frame = -1;
+    a.gframe = -1;
+    if (!receivers) {
+      if (i % p->stride == 0) { a.frame = i / p->stride; a.hist_x = out_ux; a.hist_y = out_uy; }
+    } else if (i >= 1 && (i - 1) % p->stride == 0) {
+      a.gframe = (i - 1) / p->stride; a.tr_x = out_ux; a.tr_y = out_uy;
+    }
+    ERNN_CUDA(launch_fwd_step(p->mode, a, st));
+    last = a.out;
+  }
+  if (receivers && (p->nt - 1) % p->stride == 0) {
+    ERNN_CUDA(launch_gather(last, p->nx, p->ny, p->nshots, in->rec_idx, p->nrec,
+                            (p->nt - 1) / p->stride, pl.nt_out, out_ux, out_uy, st));
+  }
+  return ERNN_OK;
+}
+
+int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
+                 const float* g_uy, const void* tape_c, size_t tape_bytes, void* scratch,
+                 size_t scratch_bytes, double* grad_C, float* grad_field, void* stream) {
+  int rc = validate(p);
+  if (rc) return rc;
+  if ((rc = validate_inputs(p, in))) return rc;
+  if (g_ux == nullptr || g_uy == nullptr || tape_c == nullptr || scratch == nullptr)
+    return ERNN_ERR_INVALID;
+  if (p->mode == kModeScalar && grad_C == nullptr) return ERNN_ERR_INVALID;
+  if (p->mode != kModeScalar && grad_field == nullptr) return ERNN_ERR_INVALID;
+  const Plan pl = make_plan(*p);
+  if (tape_bytes < pl.t_total_tape || scratch_bytes < pl.s_total) return ERNN_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  void* tape = const_cast<void*>(tape_c);  // read only below
+
+  Coef* coef = reinterpret_cast<Coef*>(at(scratch, pl.s_coef));
+  ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st));
+  const size_t gcount = (size_t)p->nshots * pl.nt_out *
+                        (p->record == kRecordFields ? pl.N : (size_t)p->nrec);
+  ERNN_CUDA(launch_gscale(g_ux, g_uy, gcount, coef, st));
+  float* LA = fat(scratch, pl.s_LA);
+  float* LB = fat(scratch, pl.s_LB);
+  ERNN_CUDA(cudaMemsetAsync(LA, 0, 2 * pl.state_bytes, st));  // LA and LB are adjacent
+  float* gacc = fat(scratch, pl.s_gacc);
+  double* partials = reinterpret_cast<double*>(at(scratch, pl.s_part));
+  if (p->mode != kModeScalar) ERNN_CUDA(cudaMemsetAsync(gacc, 0, pl.s_part - pl.s_gacc, st));
+  else ERNN_CUDA(cudaMemsetAsync(partials, 0, pl.s_total - pl.s_part, st));
+
+  auto stored = [&](int n) { return fat(tape, pl.t_store + (size_t)(n - 1) * pl.state_bytes); };
+  auto ck = [&](int j, int lev) -> const float* {
+    if (j == 0) return nullptr;
+    if (lev == 1 && j * pl.k - 1 == 0) return nullptr;  // u^0 = 0 (k == 1)
+    return fat(tape, pl.t_store + ((size_t)(j - 1) * 2 + lev) * pl.state_bytes);
+  };
+  auto seg = [&](int slot) { return fat(scratch, pl.s_seg + (size_t)slot * pl.state_bytes); };
+
+  AdjStep b;
+  std::memset(&b, 0, sizeof(b));
+  b.nx = p->nx; b.ny = p->ny; b.S = p->nshots;
+  b.coef = coef;
+  b.field = (p->mode == kModeFields) ? in->C : in->D;
+  b.g_x = g_ux; b.g_y = g_uy;
+  b.nt_out = pl.nt_out; b.record = p->record; b.nrec = p->nrec; b.rec_idx = in->rec_idx;
+  b.partials = partials;
+  b.gacc = gacc;
+
+  auto adj_step = [&](int m, const float* um) -> int {
+    const int idx = p->nt - m;
+    b.m = m;
+    b.out = (idx % 2 == 0) ? LA : LB;
+    b.cur = (idx % 2 == 0) ? LB : LA;
+    b.prev = b.out;
+    b.u = (m <= p->nt - 1) ? um : nullptr;
+    b.frame = ((m - 1) % p->stride == 0) ? (m - 1) / p->stride : -1;
+    return launch_adj_step(p->mode, b, st) == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
+  };
+
+  if (pl.store_all) {
+    for (int m = p->nt; m >= 1; --m)
+      if ((rc = adj_step(m, stored(m)))) return rc;
+  } else {
+    FwdStep a = base_fwd(*p, *in, coef, pl.nt_out);
+    for (int j = pl.nseg - 1; j >= 0; --j) {
+      const int i0 = j * pl.k, i1 = (j + 1) * pl.k < p->nt ? (j + 1) * pl.k : p->nt;
+      // recompute u^{i0+1} .. u^{i1} into the segment buffer; u^{nt} is never
+      // imaged, so the last segment stops one step short
+      const int iend = i1 < p->nt ? i1 : p->nt - 1;
+      for (int i = i0; i < iend; ++i) {
+        a.i = i;
+        a.out = seg(i - i0);
+        a.cur = (i == i0) ? ck(j, 0) : seg(i - i0 - 1);
+        a.prev = (i == i0) ? ck(j, 1) : (i == i0 + 1 ? ck(j, 0) : seg(i - i0 - 2));
+        ERNN_CUDA(launch_fwd_step(p->mode, a, st));
+      }
+      for (int m = i1; m >= i0 + 1; --m)
+        if ((rc = adj_step(m, seg(m - 1 - i0)))) return rc;
+    }
+  }
+  if (p->mode == kModeScalar) {
+    ERNN_CUDA(launch_finalize_scalar(partials, pl.nblocks, coef, grad_C, st));
+  } else {
+    ERNN_CUDA(launch_finalize_fields(p->mode, gacc, p->nshots, (int)pl.N, coef, grad_field, st));
+  }
+  return ERNN_OK;
+}
+
+uint64_t ernn_launch_count(void) { return launches(); }
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// Host-side launch interface between the C ABI driver (ernn_abi.cu) and the
+// kernels (ernn_kernels.cu).  Internal to the library.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ernn_common.cuh"
+
+namespace ernn {
+
+// Per-step arguments of the forward kernel: computes u^{i+1} from u^i, u^{i-1}.
+// State buffers are laid out [shot][component][cell] with N = nx*ny cells.
+struct FwdStep {
+  int nx, ny, S, nt, i;
+  const float* cur;   // u^i (nullptr: zero state)
+  const float* prev;  // u^{i-1} (nullptr: zero state)
+  float* out;         // u^{i+1}
+  float* copy0;       // optional second destination of u^{i+1} (checkpoint), or nullptr
+  float* copy1;       // optional third destination, or nullptr
+  // dense history: frame index (>= 0 when this step records), bases of (S, nt_out, N)
+  float* hist_x;
+  float* hist_y;
+  int frame, nt_out;
+  // receiver gather of the INPUT state u^i into frame gframe (>= 0 when due)
+  const int32_t* rec_idx;
+  int nrec, gframe;
+  float* tr_x;
+  float* tr_y;
+  const Coef* coef;
+  const float* field;  // FIELDS: 6 planes of C; DFIELD: D plane
+  const float* src_signal;
+  const float* src_map;
+  const int32_t* src_origin;
+  int bx, by, src_comp;
+};
+
+// Per-step arguments of the adjoint kernel: computes lam^m from lam^{m+1},
+// lam^{m+2}, adds the adjoint source of frame `frame` and accumulates the
+// imaging condition of lam^{m+1} against u^m.
+struct AdjStep {
+  int nx, ny, S, m;
+  const float* cur;   // lam^{m+1}
+  const float* prev;  // lam^{m+2}
+  float* out;         // lam^m (may alias prev)
+  const float* u;     // u^m, nullptr when the imaging term vanishes (m == nt)
+  const Coef* coef;
+  const float* field;
+  const float* g_x;   // adjoint source bases (S, nt_out, N or nrec)
+  const float* g_y;
+  int frame, nt_out, record, nrec;
+  const int32_t* rec_idx;
+  double* partials;   // SCALAR: [block][8] FP64 running sums
+  float* gacc;        // DFIELD: [S][N]; FIELDS: [S][6][N] running sums
+};
+
+dim3 step_grid(int nx, int ny, int S);
+
+cudaError_t launch_coef(int mode, const float* C, const float* rho, double h, double dt,
+                        Coef* coef, cudaStream_t st);
+cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st);
+cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st);
+cudaError_t launch_gather(const float* state, int nx, int ny, int S, const int32_t* rec_idx,
+                          int nrec, int frame, int nt_out, float* tr_x, float* tr_y,
+                          cudaStream_t st);
+cudaError_t launch_gscale(const float* gx, const float* gy, size_t n, Coef* coef,
+                          cudaStream_t st);
+cudaError_t launch_finalize_scalar(const double* partials, int nblocks, const Coef* coef,
+                                   double* grad_C, cudaStream_t st);
+cudaError_t launch_finalize_fields(int mode, const float* gacc, int S, int N,
+                                   const Coef* coef, float* grad_field, cudaStream_t st);
+cudaError_t launch_operator(int S, int nx, int ny, int mode, double h, const float* C,
+                            const float* D, const float* rho, const float* ux, const float* uy,
+                            const float* fx, const float* fy, float* Lux, float* Luy,
+                            cudaStream_t st);
+
+uint64_t launches();
+void count_launch();
+
+}  // namespace ernn

@@ -1,0 +1,248 @@
+"""torch.autograd.Function over the CUDA library: forward time loop + hand adjoint.
+
+ErnnPropagate replaces the reference's Python time loop
+(Parameter_inversion/Inversion_adam.py:240-307,
+Damage_inversion/Inversion_adam.py:331-393) and the autograd backward through
+it (Inversion_adam.py:447).  Inputs are the physical constants (already
+clamped by the caller, as get_material_params does), so any parameterisation
+upstream keeps working with loss.backward() and torch.optim unchanged.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import torch
+
+from . import _lib
+
+MODE_SCALAR, MODE_DFIELD, MODE_FIELDS = _lib.MODE_SCALAR, _lib.MODE_DFIELD, _lib.MODE_FIELDS
+RECORD_FIELDS, RECORD_RECEIVERS = _lib.RECORD_FIELDS, _lib.RECORD_RECEIVERS
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@dataclass
+class Geometry:
+    """Static description of one propagation: grid, time axis, sources, receivers.
+
+    src_signal: (S, nt) float32 force amplitude per step and shot.
+    src_map:    (S, bx, by) float32 spatial load inside each shot's box.
+    src_origin: (S, 2) int32 box origin (x0, y0) per shot.
+    rec_idx:    (S, R) int32 flat receiver cells (i*ny + j), or None for the
+                dense history of the reference.
+    ckpt_k:     checkpoint interval in steps (>= nt keeps every state).
+    """
+    nx: int
+    ny: int
+    nt: int
+    h: float
+    dt: float
+    src_signal: torch.Tensor
+    src_map: torch.Tensor
+    src_origin: torch.Tensor
+    stride: int = 1
+    src_comp: int = 1
+    rec_idx: torch.Tensor | None = None
+    ckpt_k: int | None = None
+    _checked: bool = field(default=False, repr=False)
+
+    @property
+    def nshots(self) -> int:
+        return int(self.src_signal.shape[0])
+
+    @property
+    def nt_out(self) -> int:
+        return (self.nt + self.stride - 1) // self.stride
+
+    @property
+    def record(self) -> int:
+        return RECORD_FIELDS if self.rec_idx is None else RECORD_RECEIVERS
+
+    def problem(self, mode: int) -> _lib.ErnnProblem:
+        nrec = 0 if self.rec_idx is None else int(self.rec_idx.shape[1])
+        k = self.ckpt_k if self.ckpt_k is not None else self.nt
+        return _lib.ErnnProblem(self.nshots, self.nx, self.ny, self.nt, self.stride, mode,
+                                self.record, nrec, self.src_comp, int(self.src_map.shape[1]),
+                                int(self.src_map.shape[2]), int(max(1, k)), float(self.h),
+                                float(self.dt))
+
+    def out_shape(self):
+        if self.rec_idx is None:
+            return (self.nshots, self.nt_out, self.nx, self.ny)
+        return (self.nshots, self.nt_out, int(self.rec_idx.shape[1]))
+
+    def check(self, device) -> None:
+        """Host-side validation, once: shapes, dtypes, devices, receiver range."""
+        if self._checked:
+            return
+        S = self.nshots
+        if self.src_signal.shape != (S, self.nt):
+            raise ValueError(f"src_signal must be (S, nt) = ({S}, {self.nt})")
+        if self.src_map.dim() != 3 or self.src_map.shape[0] != S:
+            raise ValueError("src_map must be (S, bx, by)")
+        if tuple(self.src_origin.shape) != (S, 2):
+            raise ValueError("src_origin must be (S, 2)")
+        for name in ("src_signal", "src_map"):
+            t = getattr(self, name)
+            if t.dtype != torch.float32 or not t.is_contiguous() or t.device != device:
+                raise ValueError(f"{name} must be contiguous float32 on {device}")
+        if self.src_origin.dtype != torch.int32 or self.src_origin.device != device:
+            raise ValueError(f"src_origin must be int32 on {device}")
+        if self.rec_idx is not None:
+            r = self.rec_idx
+            if r.dim() != 2 or r.shape[0] != S or r.dtype != torch.int32 or r.device != device:
+                raise ValueError(f"rec_idx must be (S, R) int32 on {device}")
+            lo, hi = int(r.min()), int(r.max())
+            if lo < 0 or hi >= self.nx * self.ny:
+                raise ValueError("receiver index outside the grid")
+        rc = _lib.load().ernn_validate(ctypes.byref(self.problem(MODE_SCALAR)))
+        _lib.check("ernn_validate", rc)
+        self._checked = True
+
+
+def _inputs(geom: Geometry, C, D, rho) -> _lib.ErnnInputs:
+    return _lib.ErnnInputs(_ptr(C), _ptr(D), _ptr(rho), _ptr(geom.src_signal),
+                           _ptr(geom.src_map), _ptr(geom.src_origin), _ptr(geom.rec_idx))
+
+
+def _mode_of(C: torch.Tensor, D) -> int:
+    if D is not None:
+        return MODE_DFIELD
+    return MODE_SCALAR if C.dim() == 1 else MODE_FIELDS
+
+
+def _require_cuda(*ts):
+    for t in ts:
+        if t is not None and not t.is_cuda:
+            raise RuntimeError("the ERNN propagation runs only on a CUDA device through "
+                               "libernn_gb300.so; there is no CPU path")
+
+
+class ErnnPropagate(torch.autograd.Function):
+    """(C, D, rho) -> (out_ux, out_uy) through the fused CUDA time loop.
+
+    C:   (6,) scalar constants (SCALAR, or C0 of DFIELD) or (6, nx, ny) planes (FIELDS).
+    D:   (nx, ny) degradation map or None.
+    rho: 0-dim density.
+    Returns the dense history (S, nt_out, nx, ny) per component, or receiver
+    traces (S, nt_out, R), frame k holding u^{k*stride+1}.
+    Gradients: dL/dC (FP64 reduction, returned as float32) in SCALAR mode,
+    dL/dC(x) in FIELDS mode, dL/dD(x) in DFIELD mode (C0 gets none).
+    """
+
+    @staticmethod
+    def forward(ctx, C, D, rho, geom: Geometry, keep_tape: bool = True):
+        _require_cuda(C, D, rho)
+        dev = C.device
+        mode = _mode_of(C, D)
+        C = C.detach().to(torch.float32).contiguous()
+        D = None if D is None else D.detach().to(torch.float32).contiguous()
+        rho = rho.detach().to(torch.float32).reshape(1).contiguous()
+        if mode == MODE_FIELDS and tuple(C.shape) != (6, geom.nx, geom.ny):
+            raise ValueError("per-cell constants must be (6, nx, ny)")
+        if mode != MODE_FIELDS and tuple(C.shape) != (6,):
+            raise ValueError("scalar constants must be (6,)")
+        if D is not None and tuple(D.shape) != (geom.nx, geom.ny):
+            raise ValueError("D must be (nx, ny)")
+        geom.check(dev)
+        lib = _lib.load()
+        prob = geom.problem(mode)
+        want_grad = bool(keep_tape and (ctx.needs_input_grad[0] or ctx.needs_input_grad[1]))
+        tape_bytes = lib.ernn_tape_bytes(ctypes.byref(prob), int(want_grad))
+        with torch.cuda.device(dev):
+            tape = torch.empty(tape_bytes, dtype=torch.uint8, device=dev)
+            out_ux = torch.empty(geom.out_shape(), dtype=torch.float32, device=dev)
+            out_uy = torch.empty(geom.out_shape(), dtype=torch.float32, device=dev)
+            ins = _inputs(geom, C, D, rho)
+            rc = lib.ernn_forward(ctypes.byref(prob), ctypes.byref(ins), _ptr(out_ux),
+                                  _ptr(out_uy), _ptr(tape), ctypes.c_size_t(tape_bytes),
+                                  int(want_grad), _stream())
+            _lib.check("ernn_forward", rc)
+        ctx.geom = geom
+        ctx.mode = mode
+        ctx.tape = tape if want_grad else None
+        ctx.save_for_backward(C, D, rho)
+        return out_ux, out_uy
+
+    @staticmethod
+    def backward(ctx, g_ux, g_uy):
+        C, D, rho = ctx.saved_tensors
+        geom, mode = ctx.geom, ctx.mode
+        if ctx.tape is None:
+            return None, None, None, None, None
+        dev = C.device
+        shape = geom.out_shape()
+        g_ux = torch.zeros(shape, device=dev) if g_ux is None else g_ux.to(torch.float32).contiguous()
+        g_uy = torch.zeros(shape, device=dev) if g_uy is None else g_uy.to(torch.float32).contiguous()
+        lib = _lib.load()
+        prob = geom.problem(mode)
+        scratch_bytes = lib.ernn_adjoint_scratch_bytes(ctypes.byref(prob))
+        with torch.cuda.device(dev):
+            scratch = torch.empty(scratch_bytes, dtype=torch.uint8, device=dev)
+            grad_C64 = torch.empty(6, dtype=torch.float64, device=dev) if mode == MODE_SCALAR else None
+            if mode == MODE_FIELDS:
+                grad_field = torch.empty((6, geom.nx, geom.ny), dtype=torch.float32, device=dev)
+            elif mode == MODE_DFIELD:
+                grad_field = torch.empty((geom.nx, geom.ny), dtype=torch.float32, device=dev)
+            else:
+                grad_field = None
+            ins = _inputs(geom, C, D, rho)
+            rc = lib.ernn_adjoint(ctypes.byref(prob), ctypes.byref(ins), _ptr(g_ux), _ptr(g_uy),
+                                  _ptr(ctx.tape), ctypes.c_size_t(ctx.tape.numel()),
+                                  _ptr(scratch), ctypes.c_size_t(scratch_bytes), _ptr(grad_C64),
+                                  _ptr(grad_field), _stream())
+            _lib.check("ernn_adjoint", rc)
+        if mode == MODE_SCALAR:
+            return grad_C64.to(torch.float32), None, None, None, None
+        if mode == MODE_FIELDS:
+            return grad_field, None, None, None, None
+        return None, grad_field, None, None, None
+
+
+def propagate(C, rho, geom: Geometry, D=None):
+    """Functional form of ErnnPropagate.  The forward keeps a tape for the
+    adjoint only when grad mode is on and C or D requires a gradient."""
+    keep = torch.is_grad_enabled() and any(
+        t is not None and t.requires_grad for t in (C, D))
+    return ErnnPropagate.apply(C, D, rho, geom, keep)
+
+
+def elastic_operator_with_force(ux, uy, C11, C22, C12, C16, C26, C66, h, force_x, force_y, rho):
+    """((A u + f) / rho) for (S, nx, ny) fields on the GPU, the values of
+    _general_anisotropic_elastic_operator_with_force
+    (Parameter_inversion/Inversion_adam.py:54-106).  Constants are 0-dim
+    (scalar mode) or (1, nx, ny) planes; with planes the force is added as given
+    (the reference's spatially varying variant adds force.transpose(1, 2),
+    Damage_inversion/Inversion_adam.py:169-174 — transpose it before calling to
+    reproduce that).  Forward values only: no autograd graph is recorded."""
+    _require_cuda(ux, uy)
+    dev = ux.device
+    S, nx, ny = ux.shape
+    consts = [torch.as_tensor(c, device=dev, dtype=torch.float32) for c in
+              (C11, C22, C12, C16, C26, C66)]
+    if consts[0].dim() == 0:
+        C = torch.stack(consts).contiguous()
+        mode = MODE_SCALAR
+    else:
+        C = torch.cat([c.reshape(1, nx, ny) for c in consts]).contiguous()
+        mode = MODE_FIELDS
+    ux = ux.detach().to(torch.float32).contiguous()
+    uy = uy.detach().to(torch.float32).contiguous()
+    fx = None if force_x is None else torch.as_tensor(force_x, device=dev).to(torch.float32).expand(S, nx, ny).contiguous()
+    fy = None if force_y is None else torch.as_tensor(force_y, device=dev).to(torch.float32).expand(S, nx, ny).contiguous()
+    rho_t = torch.as_tensor(rho, device=dev, dtype=torch.float32).reshape(1).contiguous()
+    Lux = torch.empty_like(ux)
+    Luy = torch.empty_like(uy)
+    lib = _lib.load()
+    with torch.cuda.device(dev):
+        rc = lib.ernn_operator(S, nx, ny, mode, float(h), _ptr(C), None, _ptr(rho_t), _ptr(ux),
+                               _ptr(uy), _ptr(fx), _ptr(fy), _ptr(Lux), _ptr(Luy), _stream())
+    _lib.check("ernn_operator", rc)
+    return Lux, Luy

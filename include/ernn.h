@@ -1,0 +1,154 @@
+/*
+ * ernn.h — C ABI of the GB300 ERNN propagation library (libernn_gb300.so).
+ *
+ * The library advances the 2D anisotropic elastic displacement field of the
+ * Elastodynamics-Encoded RNN with a fused sm_103a stencil kernel per step and
+ * returns the exact discrete gradient through a hand-written reverse-time
+ * adjoint with checkpoint recomputation.
+ *
+ * Conventions shared by every entry point:
+ *   - Grid (nx, ny), row-major with y contiguous: cell (i, j) is at i*ny + j,
+ *     the layout of the reference's (1, nx, ny) tensors.
+ *   - The constants are ordered C11, C22, C12, C16, C26, C66 (x-y plane of the
+ *     reference; the x-z names C11, C33, C13, C15, C35, C55 map one to one).
+ *   - Every pointer argument is DEVICE memory unless its comment says host.
+ *     The caller allocates everything; the library allocates nothing.
+ *   - `stream` is a cudaStream_t passed as void*; all work is enqueued on it,
+ *     nothing synchronises the host.
+ *   - Return value: ERNN_OK (0) or a positive error code; ernn_error_string()
+ *     describes it.  Nothing aborts or traps.
+ *
+ * The reference exposes this path as Python functions and an nn.Module; each
+ * entry point below names the reference code it stands in for (paths inside
+ * the reference project).
+ */
+#ifndef ERNN_H_
+#define ERNN_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ERNN_ABI_VERSION 1
+
+enum {
+  ERNN_OK = 0,
+  ERNN_ERR_INVALID = 1,     /* bad argument: null pointer, size or enum */
+  ERNN_ERR_WORKSPACE = 2,   /* workspace smaller than the query returned */
+  ERNN_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  ERNN_ERR_UNSTABLE = 4,    /* leapfrog stability bound violated */
+  ERNN_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  ERNN_ERR_UNSUPPORTED = 6  /* valid request this build cannot serve */
+};
+
+enum {
+  ERNN_MODE_SCALAR = 0, /* six scalar constants */
+  ERNN_MODE_DFIELD = 1, /* C_ij(x) = (1 - D(x)) C0_ij: scalar C0 and a degradation map D */
+  ERNN_MODE_FIELDS = 2  /* six per-cell constant planes */
+};
+
+enum {
+  ERNN_RECORD_FIELDS = 0,   /* dense history (S, nt_out, nx, ny) per component */
+  ERNN_RECORD_RECEIVERS = 1 /* receiver traces (S, nt_out, nrec) per component */
+};
+
+/* One propagation problem.  Plain data; identical layout in C, C++, ctypes. */
+typedef struct ErnnProblem {
+  int32_t nshots;   /* independent shots sharing the medium (batched) */
+  int32_t nx, ny;   /* grid */
+  int32_t nt;       /* time steps */
+  int32_t stride;   /* frame k records u^{k*stride+1} (step i records when i % stride == 0) */
+  int32_t mode;     /* ERNN_MODE_* */
+  int32_t record;   /* ERNN_RECORD_* */
+  int32_t nrec;     /* receivers per shot (ERNN_RECORD_RECEIVERS) */
+  int32_t src_comp; /* 0: force along x, 1: force along y */
+  int32_t src_bx, src_by; /* source map box size in cells */
+  int32_t ckpt_k;   /* checkpoint interval in steps; >= nt keeps every state */
+  double h;         /* grid spacing [m] */
+  double dt;        /* time step [s] */
+} ErnnProblem;
+
+/* Inputs shared by the forward and the adjoint (all device pointers). */
+typedef struct ErnnInputs {
+  const float* C;            /* SCALAR, DFIELD: 6 floats; FIELDS: 6 planes of nx*ny */
+  const float* D;            /* DFIELD: nx*ny; otherwise NULL */
+  const float* rho;          /* 1 float, density [kg/m^3] */
+  const float* src_signal;   /* nshots*nt: force amplitude of step i */
+  const float* src_map;      /* nshots*src_bx*src_by: spatial load inside the box */
+  const int32_t* src_origin; /* nshots*2: (x0, y0) of each shot's box; may lie partly outside */
+  const int32_t* rec_idx;    /* nshots*nrec flat cell indices; NULL unless RECEIVERS */
+} ErnnInputs;
+
+/* ABI version of the loaded library (ERNN_ABI_VERSION). */
+int ernn_abi_version(void);
+
+/* Static description of an error code. */
+const char* ernn_error_string(int code);
+
+/* Validate a problem on the host; ERNN_OK or ERNN_ERR_INVALID. */
+int ernn_validate(const ErnnProblem* p);
+
+/* Bytes of the tape: state the forward writes and the adjoint reads
+ * (checkpoints or, when ckpt_k >= nt, every state).  With with_tape == 0 the
+ * forward only needs the two-level state and no tape. (host call) */
+size_t ernn_tape_bytes(const ErnnProblem* p, int with_tape);
+
+/* Bytes of scratch the adjoint needs besides the tape (recompute segment,
+ * gradient accumulators, FP64 partial sums). (host call) */
+size_t ernn_adjoint_scratch_bytes(const ErnnProblem* p);
+
+/* Leapfrog stability of the scheme for scalar constants (host call, host
+ * pointers): *courant receives max over wavenumbers of the largest
+ * eigenvalue of -(dt^2/rho) A(k) divided by 4 (the scheme is stable for
+ * values <= 1).  Returns ERNN_ERR_UNSTABLE when it exceeds 1.
+ * No counterpart in the reference, which does not check stability. */
+int ernn_check_stability(const double* C6_host, double rho, double h, double dt, double* courant);
+
+/* One application of the operator, ((A u + f) / rho) for nshots fields.
+ * Stands in for _general_anisotropic_elastic_operator_with_force
+ * (Parameter_inversion/Inversion_adam.py:54-106) and, with mode FIELDS, its
+ * spatially varying variant (Damage_inversion/Inversion_adam.py:100-176; that
+ * one adds force.transpose(1, 2), so pass the transposed force to reproduce
+ * it).  ux, uy, fx, fy, Lux, Luy: (nshots, nx, ny); fx, fy may be NULL. */
+int ernn_operator(int32_t nshots, int32_t nx, int32_t ny, int32_t mode, double h,
+                  const float* C, const float* D, const float* rho, const float* ux,
+                  const float* uy, const float* fx, const float* fy, float* Lux, float* Luy,
+                  void* stream);
+
+/* Forward time loop.  Stands in for CFRPWaveSimulatorRicker.forward
+ * (Parameter_inversion/Inversion_adam.py:240-307) and
+ * SpatiallyVaryingAnisotropicSimulator.forward
+ * (Damage_inversion/Inversion_adam.py:331-393), batched over shots.
+ * out_ux, out_uy: (nshots, nt_out, nx, ny) for RECORD_FIELDS or
+ * (nshots, nt_out, nrec) for RECORD_RECEIVERS, nt_out = ceil(nt / stride).
+ * tape: ernn_tape_bytes(p, with_tape) bytes; keep it unchanged until
+ * ernn_adjoint when with_tape != 0. */
+int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, float* out_uy,
+                 void* tape, size_t tape_bytes, int with_tape, void* stream);
+
+/* Reverse-time adjoint: the gradient that loss.backward() produces through
+ * the forward loop (Parameter_inversion/Inversion_adam.py:447,
+ * Damage_inversion/Inversion_adam.py:511).
+ * g_ux, g_uy: dL/d(out_ux, out_uy), same shapes as the forward outputs.
+ * tape: the tape of the matching ernn_forward(with_tape = 1) call.
+ * scratch: ernn_adjoint_scratch_bytes(p) bytes.
+ * grad_C: SCALAR: 6 doubles dL/dC (FP64 reduction over cells, steps, shots);
+ *         other modes: may be NULL.
+ * grad_field: FIELDS: 6 planes dL/dC_ij(x) (float); DFIELD: nx*ny dL/dD(x);
+ *             SCALAR: may be NULL. */
+int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
+                 const float* g_uy, const void* tape, size_t tape_bytes, void* scratch,
+                 size_t scratch_bytes, double* grad_C, float* grad_field, void* stream);
+
+/* Number of kernels this library has launched since it was loaded. (host call)
+ * Diagnostic; no counterpart in the reference. */
+uint64_t ernn_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ERNN_H_ */

@@ -1,0 +1,143 @@
+"""The C-ABI library loads, exports every entry point of include/ernn.h, and its
+host-only calls behave (no GPU needed: nothing here launches a kernel)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+import ernn_gb300 as E
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "ernn.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ernn_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = E.load_library()
+    names = declared_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+    # and the Python binding declares a signature for each of them
+    assert set(names) <= set(E._lib.SIGNATURES)
+
+
+def test_struct_layout_matches_header():
+    # ErnnProblem: 12 int32 then 2 doubles = 64 bytes; ErnnInputs: 7 pointers
+    assert ctypes.sizeof(E._lib.ErnnProblem) == 64
+    assert ctypes.sizeof(E._lib.ErnnInputs) == 7 * ctypes.sizeof(ctypes.c_void_p)
+
+
+def test_version_and_error_strings():
+    lib = E.load_library()
+    assert lib.ernn_abi_version() == 1
+    for code in range(0, 7):
+        assert lib.ernn_error_string(code)
+    assert b"unknown" in lib.ernn_error_string(99)
+
+
+def _problem(**kw):
+    base = dict(nshots=2, nx=64, ny=48, nt=100, stride=5, mode=0, record=1, nrec=8, src_comp=1,
+                src_bx=9, src_by=9, ckpt_k=10, h=1e-4, dt=5e-9)
+    base.update(kw)
+    return E._lib.ErnnProblem(*[base[f] for f, _ in E._lib.ErnnProblem._fields_])
+
+
+def test_validation_rejects_bad_problems():
+    lib = E.load_library()
+    assert lib.ernn_validate(ctypes.byref(_problem())) == 0
+    bad = [dict(nx=0), dict(nt=0), dict(stride=0), dict(mode=3), dict(record=2),
+           dict(nrec=0), dict(src_comp=2), dict(h=0.0), dict(dt=-1.0), dict(ckpt_k=0),
+           dict(nshots=0), dict(nx=70000, ny=70000)]
+    for kw in bad:
+        assert lib.ernn_validate(ctypes.byref(_problem(**kw))) == 1, kw
+    assert lib.ernn_validate(None) == 1
+
+
+def test_workspace_sizes_follow_checkpoint_plan():
+    lib = E.load_library()
+    state = 2 * 2 * 64 * 48 * 4  # shots * comps * cells * float
+    align = lambda v: (v + 255) // 256 * 256
+    # segmented: 10 segments -> 9 checkpoints of two states
+    p = _problem(ckpt_k=10)
+    t = lib.ernn_tape_bytes(ctypes.byref(p), 1)
+    assert t == 256 + 2 * align(state) + 9 * 2 * align(state)
+    assert lib.ernn_tape_bytes(ctypes.byref(p), 0) == 256 + 2 * align(state)
+    # store-all when k >= nt
+    p = _problem(ckpt_k=100)
+    assert lib.ernn_tape_bytes(ctypes.byref(p), 1) == 256 + 2 * align(state) + 100 * align(state)
+    s_seg = lib.ernn_adjoint_scratch_bytes(ctypes.byref(_problem(ckpt_k=10)))
+    s_all = lib.ernn_adjoint_scratch_bytes(ctypes.byref(_problem(ckpt_k=100)))
+    assert s_seg - s_all == 10 * align(state)
+    assert lib.ernn_tape_bytes(ctypes.byref(_problem(nx=0)), 1) == 0
+
+
+def test_stability_check():
+    c = E.materials.orthotropic_xz(130e9, 12e9, 6e9, 5.5e9)
+    v = E.materials.check_stability(c, 1560.0, 1e-4, 5e-9)
+    assert 0.1 < v < 1.0
+    # the stability number scales with dt^2
+    v2 = E.materials.check_stability(c, 1560.0, 1e-4, 10e-9)
+    assert abs(v2 / v - 4.0) < 1e-9
+    with pytest.raises(ValueError):
+        E.materials.check_stability(c, 1560.0, 1e-4, 20e-9)
+    # 1D limit: C11 only, q = v^2 dt^2 / h^2 -> number = q * 4 / 4
+    one = np.array([1.0, 0, 0, 0, 0, 0])
+    assert abs(E.materials.check_stability(one, 1.0, 1.0, 0.5) - 0.25) < 1e-12
+
+
+def test_rotation_properties():
+    c = E.materials.orthotropic_xz(130e9, 12e9, 6e9, 5.5e9)
+    assert np.allclose(E.materials.rotate(c, 0), c)
+    r90 = E.materials.rotate(c, 90)
+    assert np.allclose(r90[[0, 1, 2, 5]], c[[1, 0, 2, 5]], rtol=1e-12, atol=1e-3)
+    r30 = E.materials.rotate(c, 30)
+    assert np.all(np.abs(r30) > 1e9)          # all six non-zero
+    # rotation invariants of the 2D stiffness: C_iijj = C11 + C22 + 2 C12, C_ijij = C11 + C22 + 2 C66
+    inv1 = lambda v: v[0] + v[1] + 2 * v[2]
+    inv2 = lambda v: v[0] + v[1] + 2 * v[5]
+    assert abs(inv1(r30) - inv1(c)) < 1e-3 * inv1(c)
+    assert abs(inv2(r30) - inv2(c)) < 1e-3 * inv2(c)
+    assert np.allclose(E.materials.rotate(E.materials.rotate(c, 30), -30), c, rtol=1e-12, atol=1e-2)
+
+
+def test_sources():
+    t = np.arange(2000) * 5e-9
+    b = E.sources.tone_burst(t, 1e6, 5)
+    assert b[0] == 0 and np.all(b[t > 5e-6] == 0) and np.abs(b).max() > 0.9
+    r = E.sources.ricker_wavelet(t, 1e6, 1e-6, 2.0)
+    assert abs(r[200] - 2.0) < 1e-12  # peak at t0
+    dense = torch.zeros(2, 20, 16)
+    dense[0, 3:6, 4:9] = 1.0
+    dense[1, 10:12, 0:3] = 2.0
+    m, o = E.sources.crop_box(dense)
+    assert m.shape == (2, 3, 5)
+    assert o.tolist() == [[3, 4], [10, 0]]
+    assert float(m[1].sum()) == 12.0
+
+
+def test_geometry_validation_on_host():
+    geom = E.Geometry(nx=8, ny=8, nt=4, h=1e-4, dt=5e-9, src_signal=torch.zeros(1, 4),
+                      src_map=torch.zeros(1, 2, 2), src_origin=torch.zeros(1, 2, dtype=torch.int32),
+                      rec_idx=torch.tensor([[0, 64]], dtype=torch.int32))
+    with pytest.raises(ValueError):
+        geom.check(torch.device("cpu"))   # receiver 64 is outside the 8x8 grid
+    geom = E.Geometry(nx=8, ny=8, nt=5, h=1e-4, dt=5e-9, src_signal=torch.zeros(1, 4),
+                      src_map=torch.zeros(1, 2, 2), src_origin=torch.zeros(1, 2, dtype=torch.int32))
+    with pytest.raises(ValueError):
+        geom.check(torch.device("cpu"))   # signal length != nt
+
+
+def test_product_path_refuses_cpu_tensors():
+    geom = E.Geometry(nx=8, ny=8, nt=4, h=1e-4, dt=5e-9, src_signal=torch.zeros(1, 4),
+                      src_map=torch.zeros(1, 2, 2), src_origin=torch.zeros(1, 2, dtype=torch.int32))
+    with pytest.raises(RuntimeError, match="CUDA"):
+        E.propagate(torch.ones(6), torch.tensor(1.0), geom)

@@ -1,0 +1,235 @@
+"""CUDA path vs the oracle and vs the reference's golden vectors (GPU only).
+
+Tolerances (stated by the benchmark spec): forward relative L2 error
+<= 1e-4 against the FP64 run of the same scheme, gradient relative error
+<= 1e-4.  The FP32 CUDA path typically lands near 1e-6.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import ernn_gb300 as E
+from cases import C_ROT30, random_case, rel
+from conftest import GOLDEN
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+FWD_TOL = 1e-4
+GRAD_TOL = 1e-4
+DEV = "cuda:0"
+
+
+def to_geometry(case: O.Case, ckpt_k=None) -> E.Geometry:
+    t = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a)).to(dt).to(DEV).contiguous()
+    return E.Geometry(nx=case.nx, ny=case.ny, nt=case.nt, h=case.h, dt=case.dt,
+                      src_signal=t(case.src_signal), src_map=t(case.src_map),
+                      src_origin=t(case.src_origin, torch.int32), stride=case.stride,
+                      src_comp=case.src_comp,
+                      rec_idx=None if case.rec_idx is None else t(case.rec_idx, torch.int32),
+                      ckpt_k=ckpt_k)
+
+
+def run_gpu(case: O.Case, wx, wy, ckpt_k=None):
+    """Forward + hand adjoint of L = sum(wx*out_x) + sum(wy*out_y) on the GPU."""
+    geom = to_geometry(case, ckpt_k)
+    C = torch.tensor(case.C, dtype=torch.float32, device=DEV, requires_grad=case.mode != O.MODE_DFIELD)
+    D = None
+    if case.mode == O.MODE_DFIELD:
+        D = torch.tensor(case.D, dtype=torch.float32, device=DEV, requires_grad=True)
+    rho = torch.tensor(case.rho, dtype=torch.float32, device=DEV)
+    ox, oy = E.propagate(C, rho, geom, D=D)
+    L = (ox.double() * torch.as_tensor(wx, device=DEV)).sum() + \
+        (oy.double() * torch.as_tensor(wy, device=DEV)).sum()
+    L.backward()
+    g = D.grad if D is not None else C.grad
+    return ox.detach().cpu().numpy(), oy.detach().cpu().numpy(), g.detach().cpu().numpy()
+
+
+def run_oracle(case: O.Case, wx, wy):
+    ox, oy, st = O.forward(case, "f64", keep_states=True)
+    gC, gD = O.adjoint(case, st, wx, wy, "f64")
+    return ox, oy, (gD if case.mode == O.MODE_DFIELD else gC)
+
+
+def weights(case, seed=11):
+    rng = np.random.default_rng(seed)
+    shape = case.out_shape()
+    return rng.standard_normal(shape), rng.standard_normal(shape)
+
+
+CASES = {
+    "scalar_fields": dict(),
+    "scalar_receivers_multishot": dict(record=O.RECORD_RECEIVERS, S=3, nrec=9),
+    "dfield_fields": dict(mode=O.MODE_DFIELD, nx=41, ny=37),
+    "fields_receivers": dict(mode=O.MODE_FIELDS, record=O.RECORD_RECEIVERS, S=2),
+    "odd_small": dict(nx=7, ny=5, nt=40, stride=1, box=3),
+    "x_force_stride_gt_nt": dict(src_comp=0, stride=200, nt=60),
+    "duplicate_receivers": dict(record=O.RECORD_RECEIVERS, nrec=5, dup_receiver=True),
+    "wide_multi_tile": dict(nx=70, ny=97, nt=80, S=2, stride=4),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_forward_and_gradient_vs_fp64_oracle(name):
+    case = random_case(**CASES[name])
+    wx, wy = weights(case)
+    gx, gy, gg = run_gpu(case, wx, wy)
+    rx, ry, rg = run_oracle(case, wx, wy)
+    assert rel(gx, rx) <= FWD_TOL and rel(gy, ry) <= FWD_TOL, (rel(gx, rx), rel(gy, ry))
+    assert rel(gg, rg) <= GRAD_TOL, rel(gg, rg)
+
+
+@pytest.mark.parametrize("k", [1, 2, 7, 50, 119, 120, 1000])
+def test_checkpoint_interval_does_not_change_results(k):
+    case = random_case(nt=120, S=2, record=O.RECORD_RECEIVERS)
+    wx, wy = weights(case)
+    ref = run_gpu(case, wx, wy, ckpt_k=None)
+    got = run_gpu(case, wx, wy, ckpt_k=k)
+    # recomputation replays the identical kernels: bit-identical results
+    for a, b in zip(ref, got):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("mode", [O.MODE_FIELDS, O.MODE_DFIELD])
+def test_checkpointed_percell_modes(mode):
+    case = random_case(mode=mode, nt=90, record=O.RECORD_RECEIVERS, S=2)
+    wx, wy = weights(case)
+    got = run_gpu(case, wx, wy, ckpt_k=13)
+    ref = run_oracle(case, wx, wy)
+    assert rel(got[2], ref[2]) <= GRAD_TOL
+
+
+def test_operator_vs_reference_golden():
+    for tag in ("f32", "f64"):
+        g = np.load(os.path.join(GOLDEN, f"operator_{tag}.npz"))
+        t = lambda a: torch.tensor(a, dtype=torch.float32, device=DEV)
+        C = [t(v) for v in g["C"]]
+        Lx, Ly = E.elastic_operator_with_force(t(g["ux"])[None], t(g["uy"])[None], *C, float(g["h"]),
+                                               t(g["fx"])[None], t(g["fy"])[None], float(g["rho"]))
+        assert rel(Lx.cpu().numpy()[0], g["Lux"]) < 1e-5
+        assert rel(Ly.cpu().numpy()[0], g["Luy"]) < 1e-5
+        n = int(g["nsq"])
+        Cf = [t(g["C_fields"][i])[None] for i in range(6)]
+        # the spatially varying reference adds the transposed force
+        Lx, Ly = E.elastic_operator_with_force(t(g["vx"])[None], t(g["vy"])[None], *Cf, float(g["h"]),
+                                               t(g["gx"].T)[None], t(g["gy"].T)[None], float(g["rho"]))
+        assert rel(Lx.cpu().numpy()[0], g["Lux_fields"]) < 1e-5
+        assert rel(Ly.cpu().numpy()[0], g["Luy_fields"]) < 1e-5
+
+
+def _reference_loss(pred_ux, pred_uy, tx, ty, ts, ss, wx=1.0):
+    """compute_loss of Parameter_inversion/Inversion_adam.py:358-391 (wx=5, ss=1:
+    Damage_inversion/Inversion_adam.py:441-450)."""
+    px = pred_ux[:, ::ts, ::ss, ::ss]
+    py = pred_uy[:, ::ts, ::ss, ::ss]
+    return wx * torch.mean((px - tx[:, ::ts, ::ss, ::ss]) ** 2) + torch.mean((py - ty[:, ::ts, ::ss, ::ss]) ** 2)
+
+
+@pytest.mark.parametrize("ckpt_k", [None, 16])
+def test_dropin_param_simulator_vs_reference_golden(ckpt_k):
+    g = np.load(os.path.join(GOLDEN, "param_inversion_f64.npz"))
+    init = dict(C11_init=150e9, C22_init=75e9, C12_init=45e9, C16_init=11e9, C26_init=15e9,
+                C66_init=39e9)
+    sim = E.CFRPWaveSimulatorRicker((int(g["nx"]), int(g["ny"])), float(g["h"]), float(g["dt"]),
+                                    int(g["nt"]), int(g["stride"]), source_component="y",
+                                    source_f0=4e6, source_t0=2.5e-7, source_amplitude=1e10,
+                                    rho_known=float(g["rho"]), gaussian_param=5e6, ckpt_k=ckpt_k,
+                                    **init).to(DEV)
+    ux, uy = sim(save_all_steps=False)
+    assert ux.shape == g["hist_ux"].shape
+    assert rel(ux.detach().cpu().numpy(), g["hist_ux"]) <= FWD_TOL
+    assert rel(uy.detach().cpu().numpy(), g["hist_uy"]) <= FWD_TOL
+    tx = torch.tensor(g["target_ux"], dtype=torch.float32, device=DEV)
+    ty = torch.tensor(g["target_uy"], dtype=torch.float32, device=DEV)
+    loss = _reference_loss(ux, uy, tx, ty, int(g["ts"]), int(g["ss"]))
+    assert abs(loss.item() - float(g["loss"])) <= 1e-4 * abs(float(g["loss"]))
+    loss.backward()
+    got = np.array([float(getattr(sim, n).grad) for n in
+                    ("log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66")])
+    assert rel(got, g["grad_log"]) <= GRAD_TOL, (got, g["grad_log"])
+
+
+def test_dropin_save_all_steps_matches_every_frame():
+    sim = E.CFRPWaveSimulatorRicker((24, 20), 1e-4, 5e-9, 60, 5, source_f0=4e6, source_t0=2.5e-7,
+                                    source_amplitude=1e10).to(DEV)
+    with torch.no_grad():
+        a, _ = sim(save_all_steps=False)
+        b, _ = sim(save_all_steps=True)
+    assert b.shape[1] == 60 and a.shape[1] == 12
+    assert torch.equal(a, b[:, ::5])
+
+
+def test_dropin_damage_simulator_vs_reference_golden():
+    g = np.load(os.path.join(GOLDEN, "damage_inversion_f64.npz"))
+    n = int(g["nx"])
+    sim = E.SpatiallyVaryingAnisotropicSimulator((n, n), float(g["h"]), float(g["dt"]), int(g["nt"]),
+                                                 int(g["stride"]), source_f0=4e6, source_t0=2.5e-7,
+                                                 source_amplitude=1e10, total_time=int(g["nt"]) * float(g["dt"]),
+                                                 rho_known=float(g["rho"]), gaussian_param=5e6).to(DEV)
+    with torch.no_grad():
+        for t, name in enumerate(("log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66")):
+            getattr(sim, name).copy_(torch.log(torch.tensor(g["C_fields"][t], dtype=torch.float64))[None].float())
+    ux, uy = sim(save_all_steps=False)
+    assert rel(ux.detach().cpu().numpy(), g["hist_ux"]) <= FWD_TOL
+    assert rel(uy.detach().cpu().numpy(), g["hist_uy"]) <= FWD_TOL
+    tx = torch.tensor(g["target_ux"], dtype=torch.float32, device=DEV)
+    ty = torch.tensor(g["target_uy"], dtype=torch.float32, device=DEV)
+    loss = _reference_loss(ux, uy, tx, ty, int(g["ts"]), 1, wx=5.0)
+    loss.backward()
+    got = np.stack([getattr(sim, n).grad[0].cpu().numpy() for n in
+                    ("log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66")])
+    assert rel(got, g["grad_log"]) <= GRAD_TOL
+
+
+def test_damage_simulator_rejects_non_square_like_reference():
+    sim = E.SpatiallyVaryingAnisotropicSimulator((12, 10), 1e-4, 5e-9, 10, 5).to(DEV)
+    with pytest.raises(RuntimeError):
+        sim()
+
+
+def test_gradient_vs_central_differences_fp32():
+    """Config-2-style check: central differences with h = 1e-3 relative on each
+    constant, FP32 forward on the GPU; agreement is limited by FP32 noise of
+    the loss difference and the O(h^2) truncation (see the FP64 oracle test
+    for the tight bound)."""
+    case = random_case(nx=48, ny=40, nt=150, record=O.RECORD_RECEIVERS, nrec=12)
+    geom = to_geometry(case, ckpt_k=25)
+    rho = torch.tensor(case.rho, device=DEV)
+    obs = [o + 0.05 * o.std() * torch.randn_like(o) for o in
+           E.propagate(torch.tensor(case.C * 1.02, dtype=torch.float32, device=DEV), rho, geom)]
+
+    def loss(Cv):
+        ox, oy = E.propagate(Cv, rho, geom)
+        return ((ox.double() - obs[0].double()) ** 2).mean() + ((oy.double() - obs[1].double()) ** 2).mean()
+
+    C = torch.tensor(case.C, dtype=torch.float32, device=DEV, requires_grad=True)
+    loss(C).backward()
+    g = C.grad.double().cpu().numpy()
+    scale = np.abs(g).max()
+    with torch.no_grad():
+        for t in range(6):
+            e = torch.zeros(6, dtype=torch.float64)
+            e[t] = case.C[t] * 1e-3
+            Cp = (torch.tensor(case.C) + e).float().to(DEV)
+            Cm = (torch.tensor(case.C) - e).float().to(DEV)
+            de = float((Cp - Cm)[t]) / 2.0
+            fd = (loss(Cp).item() - loss(Cm).item()) / (2 * de)
+            assert abs(fd - g[t]) <= 2e-3 * scale, (t, fd, g[t])
+
+
+def test_cpu_tensors_raise_instead_of_falling_back():
+    case = random_case(nx=8, ny=8, nt=5)
+    geom = to_geometry(case)
+    with pytest.raises(RuntimeError):
+        E.propagate(torch.tensor(case.C, dtype=torch.float32), torch.tensor(1560.0), geom)
+
+
+def test_launch_counter_counts_kernels():
+    lib = E.load_library()
+    n0 = lib.ernn_launch_count()
+    case = random_case(nx=16, ny=16, nt=10)
+    wx, wy = weights(case)
+    run_gpu(case, wx, wy)
+    assert lib.ernn_launch_count() - n0 >= 20
