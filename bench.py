@@ -1,0 +1,436 @@
+#!/usr/bin/env python
+"""Benchmark of the ERNN hot path: one inversion iteration of the rot256 workload.
+
+A step = forward time loop (256x256, 2000 steps, 30-degree rotated orthotropic
+constants, one top-centre 1 MHz tone-burst source, 64 top-edge receivers,
+checkpoint every 100 steps) -> FP64 trace misfit -> hand-written adjoint
+(gradient of the six constants) -> Adam step on normalised constants.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ernn|reference]
+
+The ernn arm prints one JSON line: value = Gcell-steps/s of forward+adjoint
+(cell-steps = shots x nx x ny x nt per iteration, summed over ranks), with
+e2e (host traces in, loss and gradient out), roofline of the dominant
+kernel, clocks sampled during the timed region and the CPU baseline (the
+PyTorch restatement of the reference path on the host cores, bounded sample).
+The reference arm (--impl reference) times that restatement on the host
+cores (all threads) and, as an extra key, on the GPU with autograd.
+Under torchrun every rank runs an independent replica (the path shards over
+independent inversions; there is no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+L2_BYTES = 129 * 1024 * 1024
+FLUSH_BYTES = 256 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ernn", "reference"], default="ernn")
+    ap.add_argument("--workload", default="rot256")
+    ap.add_argument("--cpu-sample-steps", type=int, default=100,
+                    help="time steps of the bounded CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nt", type=int, default=None, help="override the workload's step count")
+    ap.add_argument("--ckpt", type=int, default=None, help="override the checkpoint interval")
+    ap.add_argument("--plain", action="store_true",
+                    help="only run warmup + steps iterations (no timing, no JSON): a profiling target")
+    return ap.parse_args()
+
+
+def make_workload(args):
+    from ernn_gb300 import harness as Hn
+    w = Hn.WORKLOADS[args.workload]()
+    if args.nt is not None:
+        w.nt = args.nt
+    if args.ckpt is not None:
+        w.ckpt_k = args.ckpt
+    return w
+
+
+# --------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg is not None:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if self.pg is None:
+            return v
+        dev = torch.device("cuda", self.local) if torch.cuda.is_available() else torch.device("cpu")
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg is not None:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+# --------------------------------------------------------------------------
+def cpu_sample(workload, nt_sample, iters=2):
+    """The reference path (PyTorch restatement, autograd) on the host cores:
+    forward (receiver traces) -> misfit -> backward -> Adam, truncated to
+    nt_sample steps of the same grid.  Returns (Gcell-steps/s, threads, sample)."""
+    import ernn_gb300.harness as Hn
+    from oracle import torch_ref
+
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    w = Hn.WORKLOADS[workload]()
+    dev = torch.device("cpu")
+    sig = torch.tensor(Hn.sources.hann_burst_signal(nt_sample, Hn.DT, w.f0, 5, w.amplitude),
+                       dtype=torch.float32)[None].repeat(w.nshots, 1)
+    pos = [Hn.sources.cell_position(i, j, w.nx, w.ny, Hn.H) for (i, j) in w.src_cells]
+    load = Hn.sources.point_load_maps(w.nx, w.ny, Hn.H, pos, w.gaussian_param, device=dev)
+    rec = torch.tensor([[i * w.ny + j for (i, j) in w.rec_cells]] * w.nshots, dtype=torch.int32)
+    rho = torch.tensor(Hn.RHO)
+    theta = torch.nn.Parameter(torch.tensor(Hn.initial_guess(w) / Hn.scales(w.C_true), dtype=torch.float32))
+    sc = torch.tensor(Hn.scales(w.C_true), dtype=torch.float32)
+    opt = torch.optim.Adam([theta], lr=1e-2)
+    with torch.no_grad():
+        Ct = [torch.tensor(float(c)) for c in w.C_true]
+        ox, oy = torch_ref.propagate(Ct, rho, w.nx, w.ny, nt_sample, Hn.H, Hn.DT, sig, load, 1, rec)
+    times = []
+    for _ in range(iters):
+        t0 = time.perf_counter()
+        opt.zero_grad()
+        C = theta * sc
+        px, py = torch_ref.propagate([C[i] for i in range(6)], rho, w.nx, w.ny, nt_sample, Hn.H,
+                                     Hn.DT, sig, load, 1, rec)
+        loss = ((px.double() - ox.double()) ** 2).mean() + ((py.double() - oy.double()) ** 2).mean()
+        loss.backward()
+        opt.step()
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    cells = w.nshots * w.nx * w.ny * nt_sample
+    return cells / t / 1e9, threads, f"{workload} grid, {nt_sample} of {w.nt} steps, {w.nshots} shot(s), best of {iters}"
+
+
+# --------------------------------------------------------------------------
+def run_ernn(args, dist):
+    import ernn_gb300 as E
+    from ernn_gb300 import harness as Hn
+
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    lib = E.load_library()
+    w = make_workload(args)
+    inv = Hn.Inversion(w, dev)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    for _ in range(max(args.warmup, 0)):
+        inv.step()
+    torch.cuda.synchronize()
+    if args.plain:
+        for _ in range(args.steps):
+            inv.step()
+        torch.cuda.synchronize()
+        return None
+
+    # ---- main timed region: device-resident inputs
+    clocks = Clocks(dev.index)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    n0 = lib.ernn_launch_count()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()                       # L2 flush between timed iterations
+        ev[k][0].record()
+        inv.step()
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = (lib.ernn_launch_count() - n0) // max(args.steps, 1)
+    clk = clocks.stop()
+    dist.barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    ms = dist.max(ms)
+    value = dist.world * w.cell_steps / (ms * 1e-3) / 1e9
+
+    # ---- e2e through the public API: pinned host traces in, loss + gradient out
+    obs_h = [o.detach().cpu().pin_memory() for o in inv.obs]
+    obs_d = [torch.empty_like(o) for o in inv.obs]
+    out_h = torch.empty(7, dtype=torch.float64).pin_memory()
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        e2e_ev[k][0].record()
+        for hsrc, ddst in zip(obs_h, obs_d):
+            ddst.copy_(hsrc, non_blocking=True)
+        loss = inv.step(obs_d)
+        res = torch.cat([loss.detach().reshape(1), inv.params.theta.grad.double()])
+        out_h.copy_(res, non_blocking=True)
+        e2e_ev[k][1].record()
+    torch.cuda.synchronize()
+    e2e_ms = dist.max(sum(a.elapsed_time(b) for a, b in e2e_ev) / args.steps)
+    h2d = sum(o.numel() * o.element_size() for o in obs_h)
+    d2h = out_h.numel() * out_h.element_size()
+
+    # ---- forward-only throughput (no tape)
+    geom_f = inv.geom
+    C = inv.params().detach()
+    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    with torch.no_grad():
+        for k in range(args.steps):
+            flush.zero_()
+            fev[k][0].record()
+            E.propagate(C, inv.rho, geom_f)
+            fev[k][1].record()
+    torch.cuda.synchronize()
+    fwd_ms = dist.max(sum(a.elapsed_time(b) for a, b in fev) / args.steps)
+
+    # ---- dominant kernel: per-launch device time from library events
+    E._lib.profile(True)
+    inv.step()
+    torch.cuda.synchronize()
+    prof = E._lib.profile_read()
+    E._lib.profile(False)
+    cls = max(("forward", "adjoint"), key=lambda c: prof[c][0])
+    tot_ms, nlaunch = prof[cls]
+    per_launch_ms = tot_ms / max(nlaunch, 1)
+    N = w.nshots * w.nx * w.ny
+    alg_bytes = {"forward": 24, "adjoint": 32}[cls] * N     # see DESIGN: bytes per cell-step
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    kernel_name = {"forward": "fwd_step_kernel", "adjoint": "adj_step_kernel"}[cls]
+    traffic = profiled_traffic(kernel_name, args.workload)
+
+    rec = {
+        "metric": "Gcell-steps/s fwd+adj (hand adjoint, one Adam iteration)",
+        "value": round(value, 4),
+        "unit": "Gcell-steps/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded tone-burst shots; observations = same forward at true constants + 0.5% noise)",
+        "config": {"workload": f"{w.name}: {w.nx}x{w.ny} grid, {w.nt} steps, {w.nshots} shot(s), "
+                               f"{len(w.rec_cells)} receivers, {'D-field' if w.D_true is not None else 'scalar constants'}, "
+                               f"ckpt every {inv.geom.ckpt_k} steps",
+                   "cell_steps_per_iter": w.cell_steps,
+                   "l2": "flushed between timed iterations (256 MiB write)",
+                   "parallelism": f"replicas x{dist.world}"},
+        "e2e": {"value": round(dist.world * w.cell_steps / (e2e_ms * 1e-3) / 1e9, 4),
+                "unit": "Gcell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(e2e_ms, 4)},
+        "forward_only": {"value": round(dist.world * w.cell_steps / (fwd_ms * 1e-3) / 1e9, 4),
+                         "unit": "Gcell-steps/s", "ms": round(fwd_ms, 4)},
+        "ms_per_iter": round(ms, 4),
+        "wall_ms_per_step": round(wall * 1e3 / args.steps, 4),
+        "gpu_launches": int(launches * args.steps),
+        "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": round(achieved, 2),
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
+                     "launch_us": round(per_launch_ms * 1e3, 3), "launches_per_iter": nlaunch,
+                     "note": "working set is L2-resident at this size; bytes are algorithmic"},
+        "clocks": clk,
+        "loss": float(inv.step().item()),
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        v, thr, sample = cpu_sample(args.workload, args.cpu_sample_steps)
+        rec["cpu_baseline"] = {"value": round(v, 6), "unit": "Gcell-steps/s", "cores": thr,
+                               "kind": "port", "sample": sample + " (PyTorch restatement of the reference path, autograd)"}
+    return rec
+
+
+def run_reference(args, dist):
+    """The reference path restated op for op in PyTorch (oracle/torch_ref.py),
+    on the host cores with all threads; bounded sample per step."""
+    if dist.rank != 0:
+        return None
+    import ernn_gb300.harness as Hn
+    w = Hn.WORKLOADS[args.workload]()
+    nts = args.cpu_sample_steps
+    for _ in range(max(args.warmup, 0)):
+        cpu_sample(args.workload, min(nts, 20), iters=1)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, thr, sample = cpu_sample(args.workload, nts, iters=1)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = statistics.median(vals)
+    rec = {
+        "impl": "reference",
+        "metric": "Gcell-steps/s fwd+adj (hand adjoint, one Adam iteration)",
+        "value": round(value, 6), "unit": "Gcell-steps/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(wall * 1e3 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{w.name}: {w.nx}x{w.ny} grid, {w.nt} steps (sampled {nts}), "
+                               f"{w.nshots} shot(s), {len(w.rec_cells)} receivers"},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gcell-steps/s", "cores": thr,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 6), "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    if torch.cuda.is_available():
+        rec["gpu_autograd"] = gpu_autograd(args, w)
+    return rec
+
+
+def gpu_autograd(args, w, iters=3):
+    """The same restated reference path on the GPU with autograd (the reference's
+    plain form on the same device), full workload."""
+    import ernn_gb300.harness as Hn
+    from oracle import torch_ref
+    dev = torch.device("cuda", 0)
+    sig = torch.tensor(Hn.sources.hann_burst_signal(w.nt, Hn.DT, w.f0, 5, w.amplitude),
+                       dtype=torch.float32, device=dev)[None].repeat(w.nshots, 1)
+    pos = [Hn.sources.cell_position(i, j, w.nx, w.ny, Hn.H) for (i, j) in w.src_cells]
+    load = Hn.sources.point_load_maps(w.nx, w.ny, Hn.H, pos, w.gaussian_param, device=dev)
+    rec = torch.tensor([[i * w.ny + j for (i, j) in w.rec_cells]] * w.nshots, dtype=torch.int32, device=dev)
+    rho = torch.tensor(Hn.RHO, device=dev)
+    with torch.no_grad():
+        Ct = [torch.tensor(float(c), device=dev) for c in w.C_true]
+        ox, oy = torch_ref.propagate(Ct, rho, w.nx, w.ny, w.nt, Hn.H, Hn.DT, sig, load, 1, rec)
+    theta = torch.nn.Parameter(torch.tensor(Hn.initial_guess(w) / Hn.scales(w.C_true), dtype=torch.float32, device=dev))
+    sc = torch.tensor(Hn.scales(w.C_true), dtype=torch.float32, device=dev)
+    opt = torch.optim.Adam([theta], lr=1e-2)
+
+    def it():
+        opt.zero_grad()
+        C = theta * sc
+        px, py = torch_ref.propagate([C[i] for i in range(6)], rho, w.nx, w.ny, w.nt, Hn.H, Hn.DT,
+                                     sig, load, 1, rec)
+        loss = ((px.double() - ox.double()) ** 2).mean() + ((py.double() - oy.double()) ** 2).mean()
+        loss.backward()
+        opt.step()
+    it()
+    torch.cuda.synchronize()
+    t = []
+    for _ in range(iters):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        it()
+        b.record()
+        torch.cuda.synchronize()
+        t.append(a.elapsed_time(b))
+    ms = statistics.median(t)
+    return {"ms_per_iter": round(ms, 3), "value": round(w.cell_steps / (ms * 1e-3) / 1e9, 5),
+            "unit": "Gcell-steps/s", "peak_mem_gb": round(torch.cuda.max_memory_allocated(dev) / 1e9, 2)}
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        rec = run_reference(args, dist) if args.impl == "reference" else run_ernn(args, dist)
+        if rec is not None and dist.rank == 0:
+            print(json.dumps(rec), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

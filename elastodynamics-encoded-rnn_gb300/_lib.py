@@ -46,14 +46,29 @@ SIGNATURES = {
     "ernn_adjoint_scratch_bytes": (ctypes.c_size_t, [ctypes.POINTER(ErnnProblem)]),
     "ernn_check_stability": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, _P]),
-    "ernn_operator": (ctypes.c_int, [ctypes.c_int32] * 4 + [ctypes.c_double] + [_P] * 11),
+    "ernn_operator": (ctypes.c_int, [ctypes.c_int32] * 4 + [ctypes.c_double] + [_P] * 10),
     "ernn_forward": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
                                     _P, _P, _P, ctypes.c_size_t, ctypes.c_int, _P]),
     "ernn_adjoint": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
                                     _P, _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, _P,
                                     _P]),
     "ernn_launch_count": (ctypes.c_uint64, []),
+    "ernn_profile_enable": (ctypes.c_int, [ctypes.c_int]),
+    "ernn_profile_read": (ctypes.c_int, [_P, _P]),
 }
+
+
+def profile(enable: bool) -> None:
+    """Start (True) or stop (False) the library's event timing of its own launches."""
+    call("ernn_profile_enable", int(enable))
+
+
+def profile_read():
+    """{class: (total_ms, launches)} for classes 'forward', 'adjoint', 'other'."""
+    ms = (ctypes.c_double * 3)()
+    n = (ctypes.c_uint64 * 3)()
+    call("ernn_profile_read", ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(n, ctypes.c_void_p))
+    return {name: (ms[i], int(n[i])) for i, name in enumerate(("forward", "adjoint", "other"))}
 
 _LIB = None
 

@@ -333,4 +333,14 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
 
 uint64_t ernn_launch_count(void) { return launches(); }
 
+int ernn_profile_enable(int enable) {
+  profile_enable(enable != 0);
+  return ERNN_OK;
+}
+
+int ernn_profile_read(double* ms3, uint64_t* launches3) {
+  if (ms3 == nullptr || launches3 == nullptr) return ERNN_ERR_INVALID;
+  return profile_read(ms3, launches3) == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
+}
+
 }  // extern "C"

@@ -9,6 +9,8 @@
 // The notation (sxx, syy, sxy, k11 ... kq12, q, kappa) is defined in
 // ernn_common.cuh.
 #include <atomic>
+#include <utility>
+#include <vector>
 
 #include "ernn_launch.h"
 
@@ -17,6 +19,62 @@ namespace ernn {
 static std::atomic<uint64_t> g_launches{0};
 uint64_t launches() { return g_launches.load(std::memory_order_relaxed); }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// Diagnostic timing: CUDA events recorded on the launch stream around every
+// launch of a kernel class while enabled.  Host-side, single-threaded use.
+namespace {
+struct Profiler {
+  bool on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool[kProfClasses];
+  size_t used[kProfClasses] = {0, 0, 0};
+};
+Profiler g_prof;
+}  // namespace
+
+void profile_enable(bool on) {
+  g_prof.on = on;
+  for (int c = 0; c < kProfClasses; ++c) g_prof.used[c] = 0;
+}
+
+cudaError_t profile_read(double* ms, uint64_t* count) {
+  for (int c = 0; c < kProfClasses; ++c) {
+    double total = 0.0;
+    for (size_t i = 0; i < g_prof.used[c]; ++i) {
+      float t = 0.f;
+      cudaError_t e = cudaEventSynchronize(g_prof.pool[c][i].second);
+      if (e != cudaSuccess) return e;
+      e = cudaEventElapsedTime(&t, g_prof.pool[c][i].first, g_prof.pool[c][i].second);
+      if (e != cudaSuccess) return e;
+      total += t;
+    }
+    if (ms) ms[c] = total;
+    if (count) count[c] = g_prof.used[c];
+  }
+  return cudaSuccess;
+}
+
+// Launch `fn` (which enqueues one kernel on st), counting it and, while the
+// profiler is on, bracketing it with events of class `cls`.
+template <class Fn>
+static cudaError_t tracked(int cls, cudaStream_t st, Fn&& fn) {
+  if (g_prof.on) {
+    auto& pool = g_prof.pool[cls];
+    if (g_prof.used[cls] == pool.size()) {
+      cudaEvent_t a, b;
+      if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+        return cudaGetLastError();
+      pool.emplace_back(a, b);
+    }
+    auto& ev = pool[g_prof.used[cls]++];
+    cudaEventRecord(ev.first, st);
+    fn();
+    cudaEventRecord(ev.second, st);
+  } else {
+    fn();
+  }
+  count_launch();
+  return cudaGetLastError();
+}
 
 dim3 step_grid(int nx, int ny, int S) {
   return dim3((unsigned)((ny + TY - 1) / TY), (unsigned)((nx + TX - 1) / TX), (unsigned)S);
@@ -533,64 +591,62 @@ static int small_grid(size_t n, int threads) {
 
 cudaError_t launch_coef(int mode, const float* C, const float* rho, double h, double dt,
                         Coef* coef, cudaStream_t st) {
-  coef_kernel<<<1, 32, 0, st>>>(mode, C, rho, h, dt, coef);
-  count_launch();
-  return cudaGetLastError();
+  return tracked(kProfOther, st, [&] { coef_kernel<<<1, 32, 0, st>>>(mode, C, rho, h, dt, coef); });
 }
 
 cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st) {
   const dim3 grid = step_grid(a.nx, a.ny, a.S), block(TY, NTHR / TY);
-  switch (mode) {
-    case kModeScalar: fwd_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
-    case kModeDField: fwd_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
-    default: fwd_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
-  }
-  count_launch();
-  return cudaGetLastError();
+  return tracked(kProfForward, st, [&] {
+    switch (mode) {
+      case kModeScalar: fwd_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
+      case kModeDField: fwd_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
+      default: fwd_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
+    }
+  });
 }
 
 cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st) {
   const dim3 grid = step_grid(a.nx, a.ny, a.S), block(TY, NTHR / TY);
-  switch (mode) {
-    case kModeScalar: adj_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
-    case kModeDField: adj_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
-    default: adj_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
-  }
-  count_launch();
-  return cudaGetLastError();
+  return tracked(kProfAdjoint, st, [&] {
+    switch (mode) {
+      case kModeScalar: adj_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
+      case kModeDField: adj_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
+      default: adj_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
+    }
+  });
 }
 
 cudaError_t launch_gather(const float* state, int nx, int ny, int S, const int32_t* rec_idx,
                           int nrec, int frame, int nt_out, float* tr_x, float* tr_y,
                           cudaStream_t st) {
-  gather_kernel<<<small_grid((size_t)S * nrec, 256), 256, 0, st>>>(
-      state, nx * ny, S, rec_idx, nrec, frame, nt_out, tr_x, tr_y);
-  count_launch();
-  return cudaGetLastError();
+  return tracked(kProfOther, st, [&] {
+    gather_kernel<<<small_grid((size_t)S * nrec, 256), 256, 0, st>>>(
+        state, nx * ny, S, rec_idx, nrec, frame, nt_out, tr_x, tr_y);
+  });
 }
 
 cudaError_t launch_gscale(const float* gx, const float* gy, size_t n, Coef* coef,
                           cudaStream_t st) {
-  gmax_kernel<<<small_grid(n, 256), 256, 0, st>>>(gx, gy, n, coef);
-  count_launch();
-  gscale_kernel<<<1, 32, 0, st>>>(coef);
-  count_launch();
-  return cudaGetLastError();
+  cudaError_t e = tracked(kProfOther, st, [&] {
+    gmax_kernel<<<small_grid(n, 256), 256, 0, st>>>(gx, gy, n, coef);
+  });
+  if (e != cudaSuccess) return e;
+  return tracked(kProfOther, st, [&] { gscale_kernel<<<1, 32, 0, st>>>(coef); });
 }
 
 cudaError_t launch_finalize_scalar(const double* partials, int nblocks, const Coef* coef,
                                    double* grad_C, cudaStream_t st) {
-  finalize_scalar_kernel<<<1, 256, 0, st>>>(partials, nblocks, coef, grad_C);
-  count_launch();
-  return cudaGetLastError();
+  return tracked(kProfOther, st, [&] {
+    finalize_scalar_kernel<<<1, 256, 0, st>>>(partials, nblocks, coef, grad_C);
+  });
 }
 
 cudaError_t launch_finalize_fields(int mode, const float* gacc, int S, int N, const Coef* coef,
                                    float* grad_field, cudaStream_t st) {
-  finalize_fields_kernel<<<small_grid((size_t)N, 256), 256, 0, st>>>(mode, gacc, S, N, coef,
-                                                                     grad_field);
-  count_launch();
-  return cudaGetLastError();
+  return tracked(kProfOther, st, [&] {
+    finalize_fields_kernel<<<small_grid((size_t)N, 256), 256, 0, st>>>(mode, gacc, S, N, coef,
+                                                                       grad_field);
+  });
 }
 
 cudaError_t launch_operator(int S, int nx, int ny, int mode, double h, const float* C,
@@ -598,10 +654,10 @@ cudaError_t launch_operator(int S, int nx, int ny, int mode, double h, const flo
                             const float* fx, const float* fy, float* Lux, float* Luy,
                             cudaStream_t st) {
   const float w1 = (float)(1.0 / (h * h));
-  operator_kernel<<<small_grid((size_t)S * nx * ny, 256), 256, 0, st>>>(
-      S, nx, ny, mode, w1, C, D, rho, ux, uy, fx, fy, Lux, Luy);
-  count_launch();
-  return cudaGetLastError();
+  return tracked(kProfOther, st, [&] {
+    operator_kernel<<<small_grid((size_t)S * nx * ny, 256), 256, 0, st>>>(
+        S, nx, ny, mode, w1, C, D, rho, ux, uy, fx, fy, Lux, Luy);
+  });
 }
 
 }  // namespace ernn

@@ -78,4 +78,12 @@ cudaError_t launch_operator(int S, int nx, int ny, int mode, double h, const flo
 uint64_t launches();
 void count_launch();
 
+// kernel classes of the diagnostic profiler
+constexpr int kProfForward = 0;
+constexpr int kProfAdjoint = 1;
+constexpr int kProfOther = 2;
+constexpr int kProfClasses = 3;
+void profile_enable(bool on);
+cudaError_t profile_read(double* ms, uint64_t* count);
+
 }  // namespace ernn

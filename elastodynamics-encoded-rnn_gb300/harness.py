@@ -1,0 +1,198 @@
+"""Benchmark configurations and the inversion iteration built on the CUDA path.
+
+Workloads (synthetic inputs; no dataset is involved):
+  plate128   128x128, 1000 steps, orthotropic, 1 source, 32 top-edge receivers
+  rot256     256x256, 2000 steps, orthotropic rotated 30 deg, 1 source,
+             64 top-edge receivers, checkpoint every 100 steps
+  shots1024  1024x1024, 4000 steps, rotated 30 deg, 16 top-edge sources,
+             256 receivers per shot
+  damage512  512x512, 3000 steps, C = (1 - D) C0, 8 top sources, 128
+             receivers on the top and bottom edges
+dx = dz = 0.1 mm, dt = 5 ns, rho = 1560 kg/m^3, 5-cycle Hann 1 MHz tone-burst
+vertical force (Gaussian point load of the reference's source model, a = 5e6
+m^-2) on the top edge (y = ny - 1).  Observations: the same forward at the
+true constants plus Gaussian noise of 0.5 % of the trace RMS.
+One inversion iteration = forward (receiver traces) -> FP64 misfit ->
+hand adjoint -> Adam step on normalised constants.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import materials, sources
+from .propagate import Geometry, propagate
+
+H, DT, RHO = 1e-4, 5e-9, 1560.0
+C_ORTHO = materials.orthotropic_xz(130e9, 12e9, 6e9, 5.5e9)  # C11, C33, C13, C55 (GPa), C15 = C35 = 0
+
+
+@dataclass
+class Workload:
+    name: str
+    nx: int
+    ny: int
+    nt: int
+    C_true: np.ndarray
+    src_cells: list            # [(i, j)] per shot
+    rec_cells: list            # [(i, j)] shared by every shot
+    ckpt_k: int | None = None
+    stride: int = 1
+    f0: float = 1e6
+    amplitude: float = 1e10
+    gaussian_param: float = 5e6
+    D_true: np.ndarray | None = None
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nshots(self):
+        return len(self.src_cells)
+
+    @property
+    def cell_steps(self):
+        return self.nshots * self.nx * self.ny * self.nt
+
+
+def _top(n, nx, ny, margin=2):
+    return [(i, ny - 1) for i in sources.top_edge_positions(n, nx, margin)]
+
+
+def plate128():
+    return Workload("plate128", 128, 128, 1000, C_ORTHO.copy(), [(64, 127)], _top(32, 128, 128))
+
+
+def rot256(ckpt_k=100):
+    C = materials.rotate(C_ORTHO, 30.0)
+    return Workload("rot256", 256, 256, 2000, C, [(128, 255)], _top(64, 256, 256), ckpt_k=ckpt_k)
+
+
+def shots1024(ckpt_k=None, nt=4000):
+    C = materials.rotate(C_ORTHO, 30.0)
+    src = _top(16, 1024, 1024, margin=32)
+    return Workload("shots1024", 1024, 1024, nt, C, src, _top(256, 1024, 1024), ckpt_k=ckpt_k)
+
+
+def damage_map(nx, ny, seed=0, n=3):
+    """True degradation D in [0, 0.6]: three Gaussian ellipses with seeded
+    centres, axes sigma in [1, 4] mm and peak depths in [0.2, 0.6] of the depth."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(nx) * H
+    y = np.arange(ny) * H
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    D = np.zeros((nx, ny))
+    for _ in range(n):
+        cx = rng.uniform(0.2, 0.8) * x[-1]
+        depth = rng.uniform(0.2, 0.6) * y[-1]
+        cy = y[-1] - depth                      # depth measured from the top edge
+        sx, sy = rng.uniform(1e-3, 4e-3, size=2)
+        peak = rng.uniform(0.3, 0.6)
+        D = np.maximum(D, peak * np.exp(-0.5 * (((X - cx) / sx) ** 2 + ((Y - cy) / sy) ** 2)))
+    return np.clip(D, 0.0, 0.6)
+
+
+def damage512(ckpt_k=None, nt=3000):
+    rec = _top(64, 512, 512) + [(i, 0) for i in sources.top_edge_positions(64, 512, 2)]
+    return Workload("damage512", 512, 512, nt, C_ORTHO.copy(), _top(8, 512, 512, margin=16), rec,
+                    ckpt_k=ckpt_k, D_true=damage_map(512, 512))
+
+
+WORKLOADS = {"plate128": plate128, "rot256": rot256, "shots1024": shots1024,
+             "damage512": damage512}
+
+
+def geometry(w: Workload, device, nt=None) -> Geometry:
+    nt = w.nt if nt is None else nt
+    sig = sources.hann_burst_signal(nt, DT, w.f0, 5, w.amplitude).astype(np.float32)
+    S = w.nshots
+    pos = [sources.cell_position(i, j, w.nx, w.ny, H) for (i, j) in w.src_cells]
+    # the load of each shot only matters where it is non-zero: build it on a
+    # window around the source cell and crop
+    dense = sources.point_load_maps(w.nx, w.ny, H, pos, w.gaussian_param, device=device)
+    smap, origin = sources.crop_box(dense)
+    rec = torch.tensor([[i * w.ny + j for (i, j) in w.rec_cells]] * S, dtype=torch.int32, device=device)
+    return Geometry(nx=w.nx, ny=w.ny, nt=nt, h=H, dt=DT,
+                    src_signal=torch.tensor(np.repeat(sig[None], S, 0), device=device),
+                    src_map=smap, src_origin=origin, stride=w.stride, src_comp=1, rec_idx=rec,
+                    ckpt_k=w.ckpt_k)
+
+
+def observed(w: Workload, geom: Geometry, device, noise=0.005, seed=0):
+    """Traces at the true constants plus seeded Gaussian noise of `noise` x RMS
+    (0.5 % ~ add_noise_snr at 46 dB, Parameter_inversion/Inversion_adam.py:109-129)."""
+    rho = torch.tensor(RHO, device=device)
+    C = torch.tensor(w.C_true, dtype=torch.float32, device=device)
+    with torch.no_grad():
+        if w.D_true is not None:
+            ox, oy = propagate(C, rho, geom, D=torch.tensor(w.D_true, dtype=torch.float32, device=device))
+        else:
+            ox, oy = propagate(C, rho, geom)
+    g = torch.Generator(device=device).manual_seed(seed)
+    out = []
+    for o in (ox, oy):
+        rms = o.double().pow(2).mean().sqrt().float()
+        out.append(o + noise * rms * torch.randn(o.shape, generator=g, device=device))
+    return out
+
+
+def trace_misfit(pred_x, pred_y, obs_x, obs_y):
+    """MSE(ux) + MSE(uy) (the loss of Parameter_inversion/Inversion_adam.py:389-391),
+    summed in FP64."""
+    return ((pred_x.double() - obs_x.double()) ** 2).mean() + \
+           ((pred_y.double() - obs_y.double()) ** 2).mean()
+
+
+class NormalisedConstants(torch.nn.Module):
+    """C_t = s_t * theta_t with theta trained by Adam; s_t is a fixed per-constant
+    scale (the constant's magnitude, or 5 % of C11 for constants that are zero)."""
+
+    def __init__(self, C_init, C_scale):
+        super().__init__()
+        self.register_buffer("scale", torch.tensor(np.asarray(C_scale, np.float32)))
+        self.theta = torch.nn.Parameter(torch.tensor(np.asarray(C_init) / np.asarray(C_scale),
+                                                     dtype=torch.float32))
+
+    def forward(self):
+        return self.theta * self.scale
+
+
+def initial_guess(w: Workload, seed=0, spread=0.2):
+    """Each constant perturbed uniformly by +-spread (seeded)."""
+    rng = np.random.default_rng(seed)
+    return w.C_true * rng.uniform(1 - spread, 1 + spread, size=6)
+
+
+def scales(C_true):
+    C = np.abs(np.asarray(C_true, np.float64))
+    return np.where(C > 0, C, 0.05 * C.max())
+
+
+class Inversion:
+    """One inversion iteration of the scalar-constant workloads."""
+
+    def __init__(self, w: Workload, device, lr=1e-2, seed=0, nt=None):
+        self.w = w
+        self.device = device
+        self.geom = geometry(w, device, nt)
+        self.obs = observed(w, self.geom, device, seed=seed)
+        self.rho = torch.tensor(RHO, device=device)
+        self.params = NormalisedConstants(initial_guess(w, seed), scales(w.C_true)).to(device)
+        self.opt = torch.optim.Adam(self.params.parameters(), lr=lr)
+
+    def step(self, obs=None):
+        obs = self.obs if obs is None else obs
+        self.opt.zero_grad(set_to_none=True)
+        ux, uy = propagate(self.params(), self.rho, self.geom)
+        loss = trace_misfit(ux, uy, obs[0], obs[1])
+        loss.backward()
+        self.opt.step()
+        return loss
+
+    def constants(self):
+        return self.params().detach().double().cpu().numpy()
+
+    def relative_errors(self):
+        C, T = self.constants(), self.w.C_true
+        sc = scales(T)
+        return np.abs(C - T) / sc

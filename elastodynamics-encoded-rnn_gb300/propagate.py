@@ -107,6 +107,31 @@ class Geometry:
         self._checked = True
 
 
+def choose_ckpt_k(geom: Geometry, mode: int, device, budget_fraction: float = 0.4) -> int:
+    """Checkpoint interval for a problem: keep every state when the tape fits in
+    `budget_fraction` of the free device memory (no recomputation), otherwise the
+    largest interval whose checkpoints plus recompute segment fit, starting from
+    the memory-optimal sqrt(2 nt)."""
+    lib = _lib.load()
+    free, _ = torch.cuda.mem_get_info(device)
+    budget = budget_fraction * free
+    nt = geom.nt
+
+    def need(k):
+        p = geom.problem(mode)
+        p.ckpt_k = k
+        return lib.ernn_tape_bytes(ctypes.byref(p), 1) + lib.ernn_adjoint_scratch_bytes(ctypes.byref(p))
+
+    if need(nt) <= budget:
+        return nt
+    k = max(1, int(round((2 * nt) ** 0.5)))
+    best = k
+    while k < nt and need(k) <= budget:
+        best = k
+        k *= 2
+    return best
+
+
 def _inputs(geom: Geometry, C, D, rho) -> _lib.ErnnInputs:
     return _lib.ErnnInputs(_ptr(C), _ptr(D), _ptr(rho), _ptr(geom.src_signal),
                            _ptr(geom.src_map), _ptr(geom.src_origin), _ptr(geom.rec_idx))
@@ -153,6 +178,8 @@ class ErnnPropagate(torch.autograd.Function):
             raise ValueError("D must be (nx, ny)")
         geom.check(dev)
         lib = _lib.load()
+        if geom.ckpt_k is None:
+            geom.ckpt_k = choose_ckpt_k(geom, mode, dev)
         prob = geom.problem(mode)
         want_grad = bool(keep_tape and (ctx.needs_input_grad[0] or ctx.needs_input_grad[1]))
         tape_bytes = lib.ernn_tape_bytes(ctypes.byref(prob), int(want_grad))

@@ -147,6 +147,17 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
  * Diagnostic; no counterpart in the reference. */
 uint64_t ernn_launch_count(void);
 
+/* Diagnostic kernel timing (no counterpart in the reference): while enabled,
+ * every launch of the library is bracketed by CUDA events on its stream.
+ * enable != 0 starts a new measurement (totals reset). (host call) */
+int ernn_profile_enable(int enable);
+
+/* Totals since ernn_profile_enable(1), per kernel class
+ * [0: forward step, 1: adjoint step, 2: everything else]: device time in
+ * milliseconds (ms3[3], host) and launch counts (launches3[3], host).
+ * Waits for the recorded events. (host call) */
+int ernn_profile_read(double* ms3, uint64_t* launches3);
+
 #ifdef __cplusplus
 }
 #endif
