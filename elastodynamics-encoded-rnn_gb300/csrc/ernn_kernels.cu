@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   const float* prev = a.prev + (size_t)s * 2 * N;
   float* out = a.out + (size_t)s * 2 * N;
   const int gj = y0 + tx;
-  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // this thread's cells, one step
   float nvx[RPT], nvy[RPT];
 #pragma unroll
   for (int k = 0; k < RPT; ++k) {
@@ -372,8 +372,8 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
         const float g4 = l1x * su_.yy_y + l1y * (su_.yy_x + 0.5f * su_.xy_y);
         const float g5 = l1x * su_.yy_x + l1y * su_.xx_y;
         if (MODE == kModeScalar) {
-          acc[0] += (double)g0; acc[1] += (double)g1; acc[2] += (double)g2;
-          acc[3] += (double)g3; acc[4] += (double)g4; acc[5] += (double)g5;
+          acc[0] += g0; acc[1] += g1; acc[2] += g2;
+          acc[3] += g3; acc[4] += g4; acc[5] += g5;
         } else {
           float* ga = a.gacc + (size_t)s * 6 * N + o;
           ga[0] += g0; ga[N] += g1; ga[2 * N] += g2;
@@ -423,12 +423,13 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   }
 
   if (MODE == kModeScalar && um != nullptr) {
-    // FP64 block reduction of the six imaging sums.
+    // Imaging sums: FP32 over one warp's 128 cells (the FP64 pipe of this part
+    // is far narrower than FP32), FP64 across warps, tiles and steps.
 #pragma unroll
     for (int t = 0; t < 6; ++t) {
-      double v = acc[t];
+      float v = acc[t];
       for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-      if (tx == 0) red[ty][t] = v;
+      if (tx == 0) red[ty][t] = (double)v;
     }
     __syncthreads();
     if (tid < 6) {
