@@ -15,6 +15,7 @@ Public surface:
       configurations.
 """
 from . import _lib, materials, sources
+from ._lib import PATH_AUTO, PATH_RESIDENT, PATH_STEP
 from .propagate import (MODE_DFIELD, MODE_FIELDS, MODE_SCALAR, RECORD_FIELDS,
                         RECORD_RECEIVERS, ErnnPropagate, Geometry,
                         elastic_operator_with_force, propagate)
@@ -25,7 +26,8 @@ __all__ = [
     "CFRPWaveSimulatorRicker", "SpatiallyVaryingAnisotropicSimulator", "ShotGatherSimulator",
     "DegradationSimulator", "ErnnPropagate", "Geometry", "propagate",
     "elastic_operator_with_force", "sources", "materials", "MODE_SCALAR", "MODE_DFIELD",
-    "MODE_FIELDS", "RECORD_FIELDS", "RECORD_RECEIVERS", "load_library",
+    "MODE_FIELDS", "RECORD_FIELDS", "RECORD_RECEIVERS", "PATH_AUTO", "PATH_STEP",
+    "PATH_RESIDENT", "load_library",
 ]
 
 

@@ -7,6 +7,7 @@
 
 #include "ernn.h"
 #include "ernn_launch.h"
+#include "ernn_resident.h"
 
 namespace ernn {
 namespace {
@@ -17,7 +18,7 @@ inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 // Workspace plan of one problem.
 struct Plan {
-  int S, nx, ny, nt, k, nseg, nt_out, nblocks;
+  int S, nx, ny, nt, k, nseg, nt_out, nblocks, npart;
   bool store_all;
   size_t N, state_bytes;
   // tape
@@ -50,12 +51,15 @@ Plan make_plan(const ErnnProblem& p) {
   pl.s_coef = off; off += align_up(sizeof(Coef));
   pl.s_LA = off; off += pl.state_bytes;
   pl.s_LB = off; off += pl.state_bytes;
-  pl.s_seg = off; if (!pl.store_all) off += (size_t)pl.k * pl.state_bytes;
+  // two recompute segments: the cluster-resident path recomputes segment j-1
+  // while the adjoint consumes segment j
+  pl.s_seg = off; if (!pl.store_all) off += (size_t)2 * pl.k * pl.state_bytes;
   pl.s_gacc = off;
   if (p.mode == kModeDField) off += align_up((size_t)p.nshots * pl.N * sizeof(float));
   if (p.mode == kModeFields) off += align_up((size_t)p.nshots * 6 * pl.N * sizeof(float));
   pl.s_part = off;
-  if (p.mode == kModeScalar) off += align_up((size_t)pl.nblocks * 8 * sizeof(double));
+  pl.npart = pl.nblocks > p.nshots * 16 ? pl.nblocks : p.nshots * 16;
+  if (p.mode == kModeScalar) off += align_up((size_t)pl.npart * 8 * sizeof(double));
   pl.s_total = off;
   return pl;
 }
@@ -71,6 +75,8 @@ int validate(const ErnnProblem* p) {
   if (p->record == kRecordReceivers && p->nrec < 1) return ERNN_ERR_INVALID;
   if (p->src_comp != 0 && p->src_comp != 1) return ERNN_ERR_INVALID;
   if (p->src_bx < 0 || p->src_by < 0) return ERNN_ERR_INVALID;
+  if (p->path < ERNN_PATH_AUTO || p->path > ERNN_PATH_RESIDENT || p->reserved != 0)
+    return ERNN_ERR_INVALID;
   if (!(p->h > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->h) || !std::isfinite(p->dt))
     return ERNN_ERR_INVALID;
   return ERNN_OK;
@@ -108,6 +114,102 @@ FwdStep base_fwd(const ErnnProblem& p, const ErnnInputs& in, const Coef* coef, i
   a.rec_idx = in.rec_idx;
   a.nrec = p.nrec;
   return a;
+}
+
+// Cluster-resident configuration: CL CTAs of R rows each.  Returns false when
+// the problem does not fit the path (mode, alignment, receivers, memory).
+bool pick_resident(const ErnnProblem& p, const ErnnInputs& in, Coef* coef, ResCommon& rc) {
+  if (p.mode != kModeScalar || p.ny % 4 != 0) return false;
+  if (p.record == kRecordReceivers && p.nrec > kResMaxRec) return false;
+  rc.nx = p.nx; rc.ny = p.ny; rc.S = p.nshots; rc.nt = p.nt; rc.stride = p.stride;
+  rc.nt_out = (p.nt + p.stride - 1) / p.stride;
+  rc.coef = coef;
+  rc.src_signal = in.src_signal; rc.src_map = in.src_map; rc.src_origin = in.src_origin;
+  rc.bx = p.src_bx; rc.by = p.src_by; rc.src_comp = p.src_comp;
+  rc.rec_idx = (p.record == kRecordReceivers) ? in.rec_idx : nullptr;
+  rc.nrec = (p.record == kRecordReceivers) ? p.nrec : 0;
+  rc.err = &coef->err;
+  for (int CL = 16; CL >= 1; CL /= 2) {
+    if (CL > p.nx) continue;
+    rc.CL = CL;
+    rc.R = (p.nx + CL - 1) / CL;
+    if ((CL - 1) * rc.R >= p.nx) continue;
+    if (resident_feasible(rc, p.record == kRecordFields)) return true;
+  }
+  return false;
+}
+
+int resident_forward(const ErnnProblem& p, const Plan& pl, ResCommon& rc, float* out_ux,
+                     float* out_uy, void* tape, int with_tape, cudaStream_t st) {
+  ResFwd f;
+  std::memset(&f, 0, sizeof(f));
+  f.i0 = 0; f.i1 = p.nt;
+  f.state_stride = pl.state_bytes / sizeof(float);
+  if (with_tape && pl.store_all) f.states = fat(tape, pl.t_store);
+  if (with_tape && !pl.store_all) {
+    f.ckpt = fat(tape, pl.t_store);
+    f.ck_k = pl.k;
+    f.ck_nseg = pl.nseg;
+  }
+  const bool dense = (p.record == kRecordFields);
+  if (dense) { f.hist_x = out_ux; f.hist_y = out_uy; }
+  else { f.tr_x = out_ux; f.tr_y = out_uy; }
+  ResAdj a;
+  std::memset(&a, 0, sizeof(a));
+  ERNN_CUDA(launch_resident(rc, f, a, true, false, dense, st));
+  return ERNN_OK;
+}
+
+int resident_adjoint(const ErnnProblem& p, const Plan& pl, ResCommon& rc, const float* g_ux,
+                     const float* g_uy, void* tape, void* scratch, double* partials,
+                     cudaStream_t st) {
+  const size_t ss = pl.state_bytes / sizeof(float);
+  const bool dense = (p.record == kRecordFields);
+  ResAdj a;
+  std::memset(&a, 0, sizeof(a));
+  a.state_stride = ss;
+  a.lam_save = fat(scratch, pl.s_LA);
+  a.save_stride = ss;  // LB follows LA
+  a.g_x = g_ux; a.g_y = g_uy;
+  a.partials = partials;
+  ResFwd f;
+  std::memset(&f, 0, sizeof(f));
+  f.state_stride = ss;
+  if (pl.store_all) {
+    a.m_hi = p.nt; a.m_lo = 0;
+    a.u_states = fat(tape, pl.t_store);
+    a.u_base = 1;
+    a.first = 1;
+    ERNN_CUDA(launch_resident(rc, f, a, false, true, dense, st));
+    return ERNN_OK;
+  }
+  auto seg = [&](int j) { return fat(scratch, pl.s_seg + (size_t)(j & 1) * pl.k * pl.state_bytes); };
+  auto ck = [&](int j, int lev) -> const float* {
+    if (j == 0) return nullptr;
+    if (lev == 1 && j * pl.k - 1 == 0) return nullptr;  // u^0 = 0 (k == 1)
+    return fat(tape, pl.t_store + ((size_t)(j - 1) * 2 + lev) * pl.state_bytes);
+  };
+  auto set_recompute = [&](int j) {  // steps of segment j; u^nt is never imaged
+    f.i0 = j * pl.k;
+    f.i1 = (j + 1) * pl.k < p.nt - 1 ? (j + 1) * pl.k : p.nt - 1;
+    f.init_cur = ck(j, 0);
+    f.init_prev = ck(j, 1);
+    f.states = seg(j);
+  };
+  const int last = pl.nseg - 1;
+  set_recompute(last);
+  if (f.i1 > f.i0) ERNN_CUDA(launch_resident(rc, f, a, true, false, dense, st));
+  for (int j = last; j >= 0; --j) {
+    a.m_hi = (j + 1) * pl.k < p.nt ? (j + 1) * pl.k : p.nt;
+    a.m_lo = j * pl.k;
+    a.u_states = seg(j);
+    a.u_base = j * pl.k + 1;
+    a.first = (j == last) ? 1 : 0;
+    const bool overlap = j >= 1;
+    if (overlap) set_recompute(j - 1);
+    ERNN_CUDA(launch_resident(rc, f, a, overlap, true, dense, st));
+  }
+  return ERNN_OK;
 }
 
 }  // namespace
@@ -202,6 +304,13 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
   Coef* coef = reinterpret_cast<Coef*>(at(tape, pl.t_coef));
   ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st));
 
+  if (p->path != ERNN_PATH_STEP) {
+    ResCommon res;
+    if (pick_resident(*p, *in, coef, res))
+      return resident_forward(*p, pl, res, out_ux, out_uy, tape, with_tape, st);
+    if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;
+  }
+
   const bool store_all = with_tape && pl.store_all;
   float* A = fat(tape, pl.t_A);
   float* B = fat(tape, pl.t_B);
@@ -272,6 +381,16 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   double* partials = reinterpret_cast<double*>(at(scratch, pl.s_part));
   if (p->mode != kModeScalar) ERNN_CUDA(cudaMemsetAsync(gacc, 0, pl.s_part - pl.s_gacc, st));
   else ERNN_CUDA(cudaMemsetAsync(partials, 0, pl.s_total - pl.s_part, st));
+
+  if (p->path != ERNN_PATH_STEP) {
+    ResCommon res;
+    if (pick_resident(*p, *in, coef, res)) {
+      if ((rc = resident_adjoint(*p, pl, res, g_ux, g_uy, tape, scratch, partials, st))) return rc;
+      ERNN_CUDA(launch_finalize_scalar(partials, p->nshots * res.CL, coef, grad_C, st));
+      return ERNN_OK;
+    }
+    if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;
+  }
 
   auto stored = [&](int n) { return fat(tape, pl.t_store + (size_t)(n - 1) * pl.state_bytes); };
   auto ck = [&](int j, int lev) -> const float* {

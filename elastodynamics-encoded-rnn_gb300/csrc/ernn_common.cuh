@@ -36,7 +36,7 @@ struct Coef {
   double qd;         // q in double
   double inv_gscale; // 1 / gscale in double
   uint32_t gmax_bits; // max |g| (non-negative float bits, atomicMax-able)
-  uint32_t pad1;
+  int err;            // device-side error word (ERNN_ERR_TIMEOUT from a bounded wait)
   double pad2;
 };
 

@@ -9,6 +9,7 @@
 // The notation (sxx, syy, sxy, k11 ... kq12, q, kappa) is defined in
 // ernn_common.cuh.
 #include <atomic>
+#include <functional>
 #include <utility>
 #include <vector>
 
@@ -80,6 +81,10 @@ dim3 step_grid(int nx, int ny, int S) {
   return dim3((unsigned)((ny + TY - 1) / TY), (unsigned)((nx + TX - 1) / TX), (unsigned)S);
 }
 
+cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>& fn) {
+  return tracked(cls, st, fn);
+}
+
 // --------------------------------------------------------------------------
 // Coefficients.  The constants arrive as float32 device scalars (the
 // reference's clamped exp(log C) tensors); C12 + C66 is formed in float32 as
@@ -109,7 +114,7 @@ __global__ void coef_kernel(int mode, const float* __restrict__ C, const float* 
   c.qd = q;
   c.inv_gscale = 1.0;
   c.gmax_bits = 0u;
-  c.pad1 = 0u;
+  c.err = 0;
   c.pad2 = 0.0;
   *out = c;
 }
@@ -209,7 +214,8 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
 
   const Coef* K = a.coef;
   const float amp = a.src_signal[(size_t)s * a.nt + a.i] * K->kappa;
-  const int ox = a.src_origin[2 * s], oy = a.src_origin[2 * s + 1];
+  const bool has_src = a.bx > 0 && a.by > 0;
+  const int ox = has_src ? a.src_origin[2 * s] : 0, oy = has_src ? a.src_origin[2 * s + 1] : 0;
   KS ks;
   if (MODE != kModeFields) ks = load_ks(K);
   const float q = K->q;
@@ -240,7 +246,7 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
     float vx = (2.f * st.cx - px) + lx;
     float vy = (2.f * st.cy - py) + ly;
     const int sa = gi - ox, sb = gj - oy;
-    if (sa >= 0 && sa < a.bx && sb >= 0 && sb < a.by) {
+    if (has_src && sa >= 0 && sa < a.bx && sb >= 0 && sb < a.by) {
       const float f = amp * a.src_map[((size_t)s * a.bx + sa) * a.by + sb];
       if (a.src_comp == 0) vx += f; else vy += f;
     }

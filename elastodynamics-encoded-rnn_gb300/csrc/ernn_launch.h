@@ -4,6 +4,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <cuda_runtime.h>
 
 #include "ernn_common.cuh"
@@ -84,6 +85,8 @@ constexpr int kProfAdjoint = 1;
 constexpr int kProfOther = 2;
 constexpr int kProfClasses = 3;
 void profile_enable(bool on);
+// Enqueue one kernel through `fn`, counting it and timing it while profiling.
+cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>& fn);
 cudaError_t profile_read(double* ms, uint64_t* count);
 
 }  // namespace ernn

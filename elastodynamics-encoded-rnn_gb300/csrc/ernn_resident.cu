@@ -1,0 +1,573 @@
+// Cluster-resident time loop (sm_103a): one thread-block cluster of CL CTAs
+// per shot keeps the shot's whole wavefield in distributed shared memory for
+// every step of a launch.
+//
+// Partition: CTA c of the cluster owns grid rows [c R, c R + R) (x), all ny
+// columns.  Its shared memory holds two levels of the field (ping-pong) with
+// one halo row above and below:  buf[level][comp][R + 2][ny].
+// One step: every thread computes a 4 x 2 block of cells from the current
+// level, writes the new values into the other level (which holds the level
+// before, read by the same thread first), and pushes its CTA's first and last
+// row into the halo rows of the neighbouring CTAs through DSMEM stores.  One
+// cluster barrier (release/acquire) per step publishes the pushes; no step
+// touches global memory except for outputs (traces, history, checkpoints,
+// stored states).
+//
+// The adjoint role streams u^m (the forward state the imaging condition needs,
+// with halo rows) from global memory with TMA bulk copies into a
+// double-buffered tile, completed on an mbarrier: the copy of u^{m-1} is in
+// flight while step m computes.
+//
+// A launch runs up to two roles per shot, selected by blockIdx.z: a forward
+// role (steps i0..i1-1) and an adjoint role (m = m_hi .. m_lo+1), so the
+// recomputation of checkpoint segment j-1 overlaps the adjoint of segment j.
+//
+// Scalar constants only (the per-cell modes use the per-step kernels).
+#include <cooperative_groups.h>
+
+#include "ernn_launch.h"
+#include "ernn_resident.h"
+
+namespace cg = cooperative_groups;
+
+namespace ernn {
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// 1D bulk copy global -> shared (this CTA), completing `bytes` on `bar`.
+// dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: gives up after ~2^31 cycles (about a second), records the
+// timeout in *err and returns so that every barrier of the kernel is still
+// matched.
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
+  if (mbar_try_wait(bar, parity)) return;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > (1ll << 31)) {
+      atomicExch(err, 5 /* ERNN_ERR_TIMEOUT */);
+      return;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- layout
+struct Tile {
+  int R, ny, rows;      // rows: valid rows of this CTA (<= R)
+  int plane;            // floats per component plane: (R + 2) * ny
+  __device__ __forceinline__ float* comp(float* level, int c) const { return level + (size_t)c * plane; }
+  // halo-coordinate row s (0 .. R+1), column j
+  __device__ __forceinline__ int at(int s, int j) const { return s * ny + j; }
+};
+
+// load one smem row window [j-1, j, j+1, j+2] of one component (zero outside 0..ny-1)
+__device__ __forceinline__ void load_row(const float* __restrict__ p, int j, int ny, float w[4]) {
+  const float2 m = *reinterpret_cast<const float2*>(p + j);
+  w[0] = (j >= 1) ? p[j - 1] : 0.f;
+  w[1] = m.x;
+  w[2] = m.y;
+  w[3] = (j + 2 < ny) ? p[j + 2] : 0.f;
+}
+
+struct Pair {
+  float cx[2], cy[2];
+  float xx_x[2], yy_x[2], xy_x[2], xx_y[2], yy_y[2], xy_y[2];
+};
+
+// stencil sums of the two cells (j, j+1) of a row from its three row windows
+__device__ __forceinline__ void pair_stencils(const float ux[3][4], const float uy[3][4], Pair& s) {
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int k = q + 1;
+    s.cx[q] = ux[1][k];
+    s.cy[q] = uy[1][k];
+    s.xx_x[q] = (ux[0][k] + ux[2][k]) - 2.f * ux[1][k];
+    s.yy_x[q] = (ux[1][k - 1] + ux[1][k + 1]) - 2.f * ux[1][k];
+    s.xy_x[q] = (ux[2][k + 1] + ux[0][k - 1]) - (ux[2][k - 1] + ux[0][k + 1]);
+    s.xx_y[q] = (uy[0][k] + uy[2][k]) - 2.f * uy[1][k];
+    s.yy_y[q] = (uy[1][k - 1] + uy[1][k + 1]) - 2.f * uy[1][k];
+    s.xy_y[q] = (uy[2][k + 1] + uy[0][k - 1]) - (uy[2][k - 1] + uy[0][k + 1]);
+  }
+}
+
+struct KSr {
+  float k11, k22, kq12, k16, k26, k66, k16h, k26h;
+};
+
+__device__ __forceinline__ void lq(const KSr& k, const Pair& s, int q, float& lx, float& ly) {
+  lx = k.k11 * s.xx_x[q] + k.k66 * s.yy_x[q] + k.kq12 * s.xy_y[q] + k.k16h * s.xy_x[q] +
+       k.k16 * s.xx_y[q] + k.k26 * s.yy_y[q];
+  ly = k.k66 * s.xx_y[q] + k.k22 * s.yy_y[q] + k.kq12 * s.xy_x[q] + k.k16 * s.xx_x[q] +
+       k.k26 * s.yy_x[q] + k.k26h * s.xy_y[q];
+}
+
+__device__ __forceinline__ void shift_windows(float ux[3][4], float uy[3][4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    ux[0][k] = ux[1][k]; ux[1][k] = ux[2][k];
+    uy[0][k] = uy[1][k]; uy[1][k] = uy[2][k];
+  }
+}
+
+// ---------------------------------------------------------------- kernel
+template <bool DENSE>
+__global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommon c, const ResFwd f,
+                                                                   const ResAdj a, int fwd_z) {
+  extern __shared__ __align__(128) float smem[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int CL = c.CL;
+  const int shot = blockIdx.y;
+  const bool is_fwd = ((int)blockIdx.z == fwd_z);
+  const int tid = threadIdx.x;
+  const int nx = c.nx, ny = c.ny, R = c.R;
+  const size_t N = (size_t)nx * ny;
+  const int r0 = rank * R;
+  const int rows = min(R, nx - r0);  // >= 1 by construction on the host
+  Tile T{R, ny, rows, (R + 2) * ny};
+  const int level_floats = 2 * T.plane;
+
+  float* L0 = smem;
+  float* L1 = smem + level_floats;
+  float* U0 = smem + 2 * level_floats;  // adjoint role: u^m tiles
+  float* U1 = smem + 3 * level_floats;
+  int* rec_list = reinterpret_cast<int*>(smem + (is_fwd ? 2 : 4) * level_floats);  // [kResMaxRec][2]
+  int* rec_count = rec_list + 2 * kResMaxRec;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(rec_count + 4);  // 8-byte aligned (see host)
+
+  const KSr ks{c.coef->k11, c.coef->k22, c.coef->kq12, c.coef->k16,
+               c.coef->k26, c.coef->k66, c.coef->k16h, c.coef->k26h};
+  const float kappa = c.coef->kappa;
+  const size_t shot_off = (size_t)shot * 2 * N;
+
+  // -------- initial state: zero everything this role uses, then load
+  const int nlev = is_fwd ? 2 : 4;
+  for (int e = tid; e < nlev * level_floats; e += kResThreads) smem[e] = 0.f;
+  if (tid == 0) *rec_count = 0;
+  __syncthreads();
+  // receivers owned by this CTA
+  if (c.nrec > 0) {
+    for (int r = tid; r < c.nrec; r += kResThreads) {
+      const int32_t idx = c.rec_idx[(size_t)shot * c.nrec + r];
+      if (idx < 0 || (size_t)idx >= N) continue;
+      const int gi = idx / ny;
+      if (gi >= r0 && gi < r0 + rows) {
+        const int slot = atomicAdd(rec_count, 1);
+        if (slot < kResMaxRec) {
+          rec_list[2 * slot] = (gi - r0 + 1) * ny + (idx - gi * ny);  // halo-coordinate offset
+          rec_list[2 * slot + 1] = r;
+        }
+      }
+    }
+  }
+  const float* init_cur = is_fwd ? f.init_cur : (a.first ? nullptr : a.lam_save);
+  const float* init_prev = is_fwd ? f.init_prev : (a.first ? nullptr : a.lam_save + a.save_stride);
+  // current level with halo rows, previous level own rows
+  for (int e = tid; e < 2 * (rows + 2) * ny; e += kResThreads) {
+    const int comp = e / ((rows + 2) * ny);
+    const int rem = e - comp * (rows + 2) * ny;
+    const int s = rem / ny, j = rem - s * ny;
+    const int gi = r0 + s - 1;
+    if (gi < 0 || gi >= nx) continue;
+    const size_t g = shot_off + (size_t)comp * N + (size_t)gi * ny + j;
+    if (init_cur) T.comp(L0, comp)[T.at(s, j)] = init_cur[g];
+    if (init_prev && s >= 1 && s <= rows) T.comp(L1, comp)[T.at(s, j)] = init_prev[g];
+  }
+  if (!is_fwd && tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+  }
+  fence_proxy_async();
+  __syncthreads();
+  cluster.sync();  // every CTA initialised before any DSMEM push
+
+  const int nloc = min(*rec_count, kResMaxRec);
+  const int ncp = ny / 2;                      // column pairs
+  const int ngr = (rows + 3) / 4;              // row groups of 4
+  const int nitems = ncp * ngr;
+  float* up_nb = (rank > 0) ? cluster.map_shared_rank(smem, rank - 1) : nullptr;
+  float* dn_nb = (rank < CL - 1) ? cluster.map_shared_rank(smem, rank + 1) : nullptr;
+
+  if (is_fwd) {
+    // ================================================================ forward role
+    const bool has_src = c.bx > 0 && c.by > 0;
+    const int ox = has_src ? c.src_origin[2 * shot] : 0, oy = has_src ? c.src_origin[2 * shot + 1] : 0;
+    for (int i = f.i0; i < f.i1; ++i) {
+      const bool odd = ((i - f.i0) & 1) != 0;
+      float* cur = odd ? L1 : L0;
+      float* nxt = odd ? L0 : L1;
+      const int nxt_off = (int)(nxt - smem);
+      const float amp = c.src_signal[(size_t)shot * c.nt + i] * kappa;
+      float* st_out = f.states ? f.states + (size_t)(i - f.i0) * f.state_stride + shot_off : nullptr;
+      float* ck0 = nullptr;
+      float* ck1 = nullptr;
+      if (f.ckpt != nullptr) {
+        if ((i + 1) % f.ck_k == 0 && (i + 1) / f.ck_k <= f.ck_nseg - 1)
+          ck0 = f.ckpt + ((size_t)((i + 1) / f.ck_k - 1) * 2 + 0) * f.state_stride + shot_off;
+        if ((i + 2) % f.ck_k == 0 && (i + 2) / f.ck_k <= f.ck_nseg - 1)
+          ck1 = f.ckpt + ((size_t)((i + 2) / f.ck_k - 1) * 2 + 1) * f.state_stride + shot_off;
+      }
+      const bool rec_step = (i % c.stride) == 0;
+      const int frame = i / c.stride;
+      for (int it = tid; it < nitems; it += kResThreads) {
+        const int p = it % ncp, g = it / ncp;
+        const int j = 2 * p;
+        const int lr0 = 4 * g;
+        float wx[3][4], wy[3][4];
+        load_row(T.comp(cur, 0) + T.at(lr0, 0), j, ny, wx[0]);
+        load_row(T.comp(cur, 1) + T.at(lr0, 0), j, ny, wy[0]);
+        load_row(T.comp(cur, 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
+        load_row(T.comp(cur, 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
+#pragma unroll
+        for (int q4 = 0; q4 < 4; ++q4) {
+          const int lr = lr0 + q4;  // local row
+          if (lr >= rows) break;
+          const int s = lr + 1;
+          load_row(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
+          load_row(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
+          Pair st;
+          pair_stencils(wx, wy, st);
+          float2* px = reinterpret_cast<float2*>(T.comp(nxt, 0) + T.at(s, j));
+          float2* py = reinterpret_cast<float2*>(T.comp(nxt, 1) + T.at(s, j));
+          const float2 prevx = *px, prevy = *py;
+          float vx[2], vy[2];
+          const int gi = r0 + lr;
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            float lx, ly;
+            lq(ks, st, q, lx, ly);
+            const float pxv = q ? prevx.y : prevx.x, pyv = q ? prevy.y : prevy.x;
+            vx[q] = (2.f * st.cx[q] - pxv) + lx;
+            vy[q] = (2.f * st.cy[q] - pyv) + ly;
+            const int sa = gi - ox, sb = j + q - oy;
+            if (has_src && sa >= 0 && sa < c.bx && sb >= 0 && sb < c.by) {
+              const float fz = amp * c.src_map[((size_t)shot * c.bx + sa) * c.by + sb];
+              if (c.src_comp == 0) vx[q] += fz; else vy[q] += fz;
+            }
+          }
+          const float2 nvx = make_float2(vx[0], vx[1]), nvy = make_float2(vy[0], vy[1]);
+          *px = nvx;
+          *py = nvy;
+          if (lr == 0 && up_nb) {
+            const int o = nxt_off + T.at(R + 1, j);
+            *reinterpret_cast<float2*>(up_nb + o) = nvx;
+            *reinterpret_cast<float2*>(up_nb + o + T.plane) = nvy;
+          }
+          if (lr == rows - 1 && dn_nb) {
+            const int o = nxt_off + T.at(0, j);
+            *reinterpret_cast<float2*>(dn_nb + o) = nvx;
+            *reinterpret_cast<float2*>(dn_nb + o + T.plane) = nvy;
+          }
+          const size_t go = (size_t)gi * ny + j;
+          if (st_out) {
+            *reinterpret_cast<float2*>(st_out + go) = nvx;
+            *reinterpret_cast<float2*>(st_out + N + go) = nvy;
+          }
+          if (ck0) {
+            *reinterpret_cast<float2*>(ck0 + go) = nvx;
+            *reinterpret_cast<float2*>(ck0 + N + go) = nvy;
+          }
+          if (ck1) {
+            *reinterpret_cast<float2*>(ck1 + go) = nvx;
+            *reinterpret_cast<float2*>(ck1 + N + go) = nvy;
+          }
+          if (DENSE && rec_step && f.hist_x) {
+            const size_t ho = ((size_t)shot * c.nt_out + frame) * N + go;
+            *reinterpret_cast<float2*>(f.hist_x + ho) = nvx;
+            *reinterpret_cast<float2*>(f.hist_y + ho) = nvy;
+          }
+          shift_windows(wx, wy);
+        }
+      }
+      cluster.sync();
+      if (!DENSE && rec_step && f.tr_x) {
+        for (int e = tid; e < nloc; e += kResThreads) {
+          const int off = rec_list[2 * e], r = rec_list[2 * e + 1];
+          const size_t o = ((size_t)shot * c.nt_out + frame) * c.nrec + r;
+          f.tr_x[o] = T.comp(nxt, 0)[off];
+          f.tr_y[o] = T.comp(nxt, 1)[off];
+        }
+      }
+    }
+    return;
+  }
+
+  // ================================================================== adjoint role
+  const float gs = c.coef->gscale;
+  const int r_lo = max(r0 - 1, 0), r_hi = min(r0 + rows + 1, nx);
+  const int dst_row = r_lo - (r0 - 1);
+  const uint32_t copy_bytes = (uint32_t)((r_hi - r_lo) * ny * sizeof(float));
+  uint32_t phase[2] = {0u, 0u};
+  auto prefetch = [&](int m) {  // u^m -> U[m & 1]
+    if (tid == 0) {
+      float* dst = (m & 1) ? U1 : U0;
+      const float* src = a.u_states + (size_t)(m - a.u_base) * a.state_stride + shot_off;
+      fence_proxy_async();
+      mbar_arrive_expect_tx(&mbar[m & 1], 2 * copy_bytes);
+      bulk_g2s(dst + T.at(dst_row, 0), src + (size_t)r_lo * ny, copy_bytes, &mbar[m & 1]);
+      bulk_g2s(dst + T.plane + T.at(dst_row, 0), src + N + (size_t)r_lo * ny, copy_bytes,
+               &mbar[m & 1]);
+    }
+  };
+  const int m_top_img = min(a.m_hi, c.nt - 1);  // highest m with an imaging term
+  if (m_top_img >= a.m_lo + 1) prefetch(m_top_img);
+
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  double acc64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  int since_flush = 0;
+  int last_level = 0;
+  for (int m = a.m_hi; m >= a.m_lo + 1; --m) {
+    const bool odd = ((a.m_hi - m) & 1) != 0;
+    float* cur = odd ? L1 : L0;  // lam^{m+1}
+    float* nxt = odd ? L0 : L1;  // lam^{m+2}, becomes lam^m
+    last_level = odd ? 0 : 1;
+    const int nxt_off = (int)(nxt - smem);
+    const bool img = (m <= c.nt - 1);
+    if (img && m - 1 >= a.m_lo + 1) prefetch(m - 1);
+    const bool src_step = ((m - 1) % c.stride) == 0;
+    const int frame = (m - 1) / c.stride;
+    if (!DENSE && src_step) {
+      // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: subtract g from the own
+      // copy of lam^{m+2}, which only the owning thread reads this step
+      for (int e = tid; e < nloc; e += kResThreads) {
+        const int off = rec_list[2 * e], r = rec_list[2 * e + 1];
+        const size_t go = ((size_t)shot * c.nt_out + frame) * c.nrec + r;
+        atomicAdd(&T.comp(nxt, 0)[off], -gs * a.g_x[go]);
+        atomicAdd(&T.comp(nxt, 1)[off], -gs * a.g_y[go]);
+      }
+      __syncthreads();
+    }
+    float* U = (m & 1) ? U1 : U0;
+    if (img) {
+      mbar_wait_bounded(&mbar[m & 1], phase[m & 1], c.err);
+      phase[m & 1] ^= 1u;
+    }
+    for (int it = tid; it < nitems; it += kResThreads) {
+      const int p = it % ncp, g = it / ncp;
+      const int j = 2 * p;
+      const int lr0 = 4 * g;
+      float wx[3][4], wy[3][4], vx_[3][4], vy_[3][4];
+      load_row(T.comp(cur, 0) + T.at(lr0, 0), j, ny, wx[0]);
+      load_row(T.comp(cur, 1) + T.at(lr0, 0), j, ny, wy[0]);
+      load_row(T.comp(cur, 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
+      load_row(T.comp(cur, 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
+      if (img) {
+        load_row(T.comp(U, 0) + T.at(lr0, 0), j, ny, vx_[0]);
+        load_row(T.comp(U, 1) + T.at(lr0, 0), j, ny, vy_[0]);
+        load_row(T.comp(U, 0) + T.at(lr0 + 1, 0), j, ny, vx_[1]);
+        load_row(T.comp(U, 1) + T.at(lr0 + 1, 0), j, ny, vy_[1]);
+      }
+#pragma unroll
+      for (int q4 = 0; q4 < 4; ++q4) {
+        const int lr = lr0 + q4;
+        if (lr >= rows) break;
+        const int s = lr + 1;
+        load_row(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
+        load_row(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
+        Pair st;
+        pair_stencils(wx, wy, st);
+        float2* px = reinterpret_cast<float2*>(T.comp(nxt, 0) + T.at(s, j));
+        float2* py = reinterpret_cast<float2*>(T.comp(nxt, 1) + T.at(s, j));
+        const float2 prevx = *px, prevy = *py;
+        const int gi = r0 + lr;
+        float vx[2], vy[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          float lx, ly;
+          lq(ks, st, q, lx, ly);
+          const float pxv = q ? prevx.y : prevx.x, pyv = q ? prevy.y : prevy.x;
+          vx[q] = (2.f * st.cx[q] - pxv) + lx;
+          vy[q] = (2.f * st.cy[q] - pyv) + ly;
+        }
+        if (DENSE && src_step) {
+          const size_t go = ((size_t)shot * c.nt_out + frame) * N + (size_t)gi * ny + j;
+          const float2 gx = *reinterpret_cast<const float2*>(a.g_x + go);
+          const float2 gy = *reinterpret_cast<const float2*>(a.g_y + go);
+          vx[0] += gs * gx.x; vx[1] += gs * gx.y;
+          vy[0] += gs * gy.x; vy[1] += gs * gy.y;
+        }
+        const float2 nvx = make_float2(vx[0], vx[1]), nvy = make_float2(vy[0], vy[1]);
+        *px = nvx;
+        *py = nvy;
+        if (lr == 0 && up_nb) {
+          const int o = nxt_off + T.at(R + 1, j);
+          *reinterpret_cast<float2*>(up_nb + o) = nvx;
+          *reinterpret_cast<float2*>(up_nb + o + T.plane) = nvy;
+        }
+        if (lr == rows - 1 && dn_nb) {
+          const int o = nxt_off + T.at(0, j);
+          *reinterpret_cast<float2*>(dn_nb + o) = nvx;
+          *reinterpret_cast<float2*>(dn_nb + o + T.plane) = nvy;
+        }
+        if (img) {
+          load_row(T.comp(U, 0) + T.at(s + 1, 0), j, ny, vx_[2]);
+          load_row(T.comp(U, 1) + T.at(s + 1, 0), j, ny, vy_[2]);
+          Pair su;
+          pair_stencils(vx_, vy_, su);
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const float l1x = st.cx[q], l1y = st.cy[q];  // lam^{m+1} at the cell
+            acc[0] += l1x * su.xx_x[q];
+            acc[1] += l1y * su.yy_y[q];
+            acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
+            acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
+            acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
+            acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
+          }
+          shift_windows(vx_, vy_);
+        }
+        shift_windows(wx, wy);
+      }
+    }
+    // FP32 over at most 16 steps of this thread's cells, FP64 from there on
+    if (++since_flush == 16) {
+#pragma unroll
+      for (int t = 0; t < 6; ++t) { acc64[t] += (double)acc[t]; acc[t] = 0.f; }
+      since_flush = 0;
+    }
+    cluster.sync();
+  }
+#pragma unroll
+  for (int t = 0; t < 6; ++t) acc64[t] += (double)acc[t];
+
+  // lam^{m_lo+1} (last written level) and lam^{m_lo+2} -> lam_save
+  if (a.m_hi >= a.m_lo + 1) {
+    float* last = last_level ? L1 : L0;
+    float* before = last_level ? L0 : L1;
+    for (int e = tid; e < 2 * rows * ny; e += kResThreads) {
+      const int comp = e / (rows * ny);
+      const int rem = e - comp * rows * ny;
+      const int lr = rem / ny, j = rem - lr * ny;
+      const size_t g = shot_off + (size_t)comp * N + (size_t)(r0 + lr) * ny + j;
+      a.lam_save[g] = T.comp(last, comp)[T.at(lr + 1, j)];
+      a.lam_save[a.save_stride + g] = T.comp(before, comp)[T.at(lr + 1, j)];
+    }
+  }
+  // FP64 block reduction of the imaging sums, once per launch
+  __shared__ double red[kResThreads / 32][6];
+  const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    double v = acc64[t];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][t] = v;
+  }
+  __syncthreads();
+  if (tid < 6) {
+    double v = 0.0;
+    for (int w = 0; w < kResThreads / 32; ++w) v += red[w][tid];
+    a.partials[((size_t)shot * CL + rank) * 8 + tid] += v;
+  }
+}
+
+// ---------------------------------------------------------------- host side
+size_t resident_smem_bytes(const ResCommon& c, bool with_adjoint) {
+  const size_t level = 2 * (size_t)(c.R + 2) * c.ny * sizeof(float);
+  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 2 * sizeof(uint64_t) + 16;
+  return (with_adjoint ? 4 : 2) * level + tail;
+}
+
+static cudaError_t configure(const void* fn, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+}
+
+bool resident_feasible(const ResCommon& c, bool dense) {
+  if (c.CL < 1 || c.CL > 16 || c.ny % 4 != 0 || c.nrec > kResMaxRec) return false;
+  if ((c.CL - 1) * c.R >= c.nx) return false;  // every CTA owns >= 1 row
+  const size_t smem = resident_smem_bytes(c, true);
+  if (smem > 227 * 1024) return false;
+  const void* fn = dense ? (const void*)resident_kernel<true> : (const void*)resident_kernel<false>;
+  if (configure(fn, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c.CL, 1, 2);
+  cfg.blockDim = dim3(kResThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = c.CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return clusters >= 1;
+}
+
+cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResAdj& a, bool run_fwd,
+                            bool run_adj, bool dense, cudaStream_t st) {
+  if (!run_fwd && !run_adj) return cudaSuccess;
+  const size_t smem = resident_smem_bytes(c, run_adj);
+  const void* fn = dense ? (const void*)resident_kernel<true> : (const void*)resident_kernel<false>;
+  cudaError_t e = configure(fn, resident_smem_bytes(c, true));
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c.CL, c.S, (run_fwd && run_adj) ? 2 : 1);
+  cfg.blockDim = dim3(kResThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = c.CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  // blockIdx.z == fwd_z runs the forward role
+  const int fwd_z = run_fwd ? (run_adj ? 1 : 0) : -1;
+  const int cls = run_adj ? kProfAdjoint : kProfForward;
+  return tracked_launch(cls, st, [&] {
+    if (dense) cudaLaunchKernelEx(&cfg, resident_kernel<true>, c, f, a, fwd_z);
+    else cudaLaunchKernelEx(&cfg, resident_kernel<false>, c, f, a, fwd_z);
+  });
+}
+
+}  // namespace ernn

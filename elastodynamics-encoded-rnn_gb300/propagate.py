@@ -38,6 +38,8 @@ class Geometry:
     rec_idx:    (S, R) int32 flat receiver cells (i*ny + j), or None for the
                 dense history of the reference.
     ckpt_k:     checkpoint interval in steps (>= nt keeps every state).
+    path:       PATH_AUTO (cluster-resident when the problem fits, else one
+                kernel per step), PATH_STEP or PATH_RESIDENT.
     """
     nx: int
     ny: int
@@ -51,6 +53,7 @@ class Geometry:
     src_comp: int = 1
     rec_idx: torch.Tensor | None = None
     ckpt_k: int | None = None
+    path: int = _lib.PATH_AUTO
     _checked: bool = field(default=False, repr=False)
 
     @property
@@ -70,8 +73,8 @@ class Geometry:
         k = self.ckpt_k if self.ckpt_k is not None else self.nt
         return _lib.ErnnProblem(self.nshots, self.nx, self.ny, self.nt, self.stride, mode,
                                 self.record, nrec, self.src_comp, int(self.src_map.shape[1]),
-                                int(self.src_map.shape[2]), int(max(1, k)), float(self.h),
-                                float(self.dt))
+                                int(self.src_map.shape[2]), int(max(1, k)), int(self.path), 0,
+                                float(self.h), float(self.dt))
 
     def out_shape(self):
         if self.rec_idx is None:

@@ -55,6 +55,14 @@ enum {
   ERNN_RECORD_RECEIVERS = 1 /* receiver traces (S, nt_out, nrec) per component */
 };
 
+enum {
+  ERNN_PATH_AUTO = 0,     /* cluster-resident when the problem fits, else per-step */
+  ERNN_PATH_STEP = 1,     /* one fused kernel launch per time step (any size, any mode) */
+  ERNN_PATH_RESIDENT = 2  /* one thread-block cluster per shot holds the state in
+                             distributed shared memory for all steps (scalar constants,
+                             ny % 4 == 0, state small enough); ERNN_ERR_UNSUPPORTED otherwise */
+};
+
 /* One propagation problem.  Plain data; identical layout in C, C++, ctypes. */
 typedef struct ErnnProblem {
   int32_t nshots;   /* independent shots sharing the medium (batched) */
@@ -67,6 +75,8 @@ typedef struct ErnnProblem {
   int32_t src_comp; /* 0: force along x, 1: force along y */
   int32_t src_bx, src_by; /* source map box size in cells */
   int32_t ckpt_k;   /* checkpoint interval in steps; >= nt keeps every state */
+  int32_t path;     /* ERNN_PATH_*: which kernels run the time loop */
+  int32_t reserved; /* must be 0 */
   double h;         /* grid spacing [m] */
   double dt;        /* time step [s] */
 } ErnnProblem;

@@ -31,8 +31,8 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_struct_layout_matches_header():
-    # ErnnProblem: 12 int32 then 2 doubles = 64 bytes; ErnnInputs: 7 pointers
-    assert ctypes.sizeof(E._lib.ErnnProblem) == 64
+    # ErnnProblem: 14 int32 then 2 doubles = 72 bytes; ErnnInputs: 7 pointers
+    assert ctypes.sizeof(E._lib.ErnnProblem) == 72
     assert ctypes.sizeof(E._lib.ErnnInputs) == 7 * ctypes.sizeof(ctypes.c_void_p)
 
 
@@ -46,7 +46,7 @@ def test_version_and_error_strings():
 
 def _problem(**kw):
     base = dict(nshots=2, nx=64, ny=48, nt=100, stride=5, mode=0, record=1, nrec=8, src_comp=1,
-                src_bx=9, src_by=9, ckpt_k=10, h=1e-4, dt=5e-9)
+                src_bx=9, src_by=9, ckpt_k=10, path=0, reserved=0, h=1e-4, dt=5e-9)
     base.update(kw)
     return E._lib.ErnnProblem(*[base[f] for f, _ in E._lib.ErnnProblem._fields_])
 
@@ -56,7 +56,7 @@ def test_validation_rejects_bad_problems():
     assert lib.ernn_validate(ctypes.byref(_problem())) == 0
     bad = [dict(nx=0), dict(nt=0), dict(stride=0), dict(mode=3), dict(record=2),
            dict(nrec=0), dict(src_comp=2), dict(h=0.0), dict(dt=-1.0), dict(ckpt_k=0),
-           dict(nshots=0), dict(nx=70000, ny=70000)]
+           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=3), dict(reserved=1)]
     for kw in bad:
         assert lib.ernn_validate(ctypes.byref(_problem(**kw))) == 1, kw
     assert lib.ernn_validate(None) == 1
@@ -76,7 +76,8 @@ def test_workspace_sizes_follow_checkpoint_plan():
     assert lib.ernn_tape_bytes(ctypes.byref(p), 1) == 256 + 2 * align(state) + 100 * align(state)
     s_seg = lib.ernn_adjoint_scratch_bytes(ctypes.byref(_problem(ckpt_k=10)))
     s_all = lib.ernn_adjoint_scratch_bytes(ctypes.byref(_problem(ckpt_k=100)))
-    assert s_seg - s_all == 10 * align(state)
+    # two recompute segments (the resident path overlaps recompute and adjoint)
+    assert s_seg - s_all == 2 * 10 * align(state)
     assert lib.ernn_tape_bytes(ctypes.byref(_problem(nx=0)), 1) == 0
 
 

@@ -21,19 +21,19 @@ GRAD_TOL = 1e-4
 DEV = "cuda:0"
 
 
-def to_geometry(case: O.Case, ckpt_k=None) -> E.Geometry:
+def to_geometry(case: O.Case, ckpt_k=None, path=E.PATH_AUTO) -> E.Geometry:
     t = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a)).to(dt).to(DEV).contiguous()
     return E.Geometry(nx=case.nx, ny=case.ny, nt=case.nt, h=case.h, dt=case.dt,
                       src_signal=t(case.src_signal), src_map=t(case.src_map),
                       src_origin=t(case.src_origin, torch.int32), stride=case.stride,
                       src_comp=case.src_comp,
                       rec_idx=None if case.rec_idx is None else t(case.rec_idx, torch.int32),
-                      ckpt_k=ckpt_k)
+                      ckpt_k=ckpt_k, path=path)
 
 
-def run_gpu(case: O.Case, wx, wy, ckpt_k=None):
+def run_gpu(case: O.Case, wx, wy, ckpt_k=None, path=E.PATH_AUTO):
     """Forward + hand adjoint of L = sum(wx*out_x) + sum(wy*out_y) on the GPU."""
-    geom = to_geometry(case, ckpt_k)
+    geom = to_geometry(case, ckpt_k, path)
     C = torch.tensor(case.C, dtype=torch.float32, device=DEV, requires_grad=case.mode != O.MODE_DFIELD)
     D = None
     if case.mode == O.MODE_DFIELD:
@@ -75,21 +75,60 @@ CASES = {
 def test_forward_and_gradient_vs_fp64_oracle(name):
     case = random_case(**CASES[name])
     wx, wy = weights(case)
-    gx, gy, gg = run_gpu(case, wx, wy)
+    gx, gy, gg = run_gpu(case, wx, wy, path=E.PATH_STEP)
     rx, ry, rg = run_oracle(case, wx, wy)
     assert rel(gx, rx) <= FWD_TOL and rel(gy, ry) <= FWD_TOL, (rel(gx, rx), rel(gy, ry))
     assert rel(gg, rg) <= GRAD_TOL, rel(gg, rg)
 
 
-@pytest.mark.parametrize("k", [1, 2, 7, 50, 119, 120, 1000])
-def test_checkpoint_interval_does_not_change_results(k):
-    case = random_case(nt=120, S=2, record=O.RECORD_RECEIVERS)
+# scalar-constant cases with ny % 4 == 0, served by the cluster-resident path
+RESIDENT_CASES = {
+    "dense_odd_nx": dict(nx=33, ny=28),
+    "receivers_multishot": dict(nx=45, ny=36, record=O.RECORD_RECEIVERS, S=3, nrec=9),
+    "x_force_stride1": dict(nx=24, ny=20, nt=70, stride=1, src_comp=0),
+    "duplicate_receivers": dict(nx=40, ny=32, record=O.RECORD_RECEIVERS, nrec=6, dup_receiver=True),
+    "tall_thin": dict(nx=150, ny=8, nt=90, stride=5),
+    "one_row_per_cta": dict(nx=17, ny=12, nt=50),
+    "wide": dict(nx=64, ny=256, nt=60, S=2, record=O.RECORD_RECEIVERS, nrec=20),
+}
+
+
+@pytest.mark.parametrize("name", list(RESIDENT_CASES))
+def test_resident_path_vs_fp64_oracle(name):
+    case = random_case(**RESIDENT_CASES[name])
     wx, wy = weights(case)
-    ref = run_gpu(case, wx, wy, ckpt_k=None)
-    got = run_gpu(case, wx, wy, ckpt_k=k)
+    gx, gy, gg = run_gpu(case, wx, wy, path=E.PATH_RESIDENT)
+    rx, ry, rg = run_oracle(case, wx, wy)
+    assert rel(gx, rx) <= FWD_TOL and rel(gy, ry) <= FWD_TOL, (rel(gx, rx), rel(gy, ry))
+    assert rel(gg, rg) <= GRAD_TOL, rel(gg, rg)
+
+
+@pytest.mark.parametrize("path", [E.PATH_STEP, E.PATH_RESIDENT])
+@pytest.mark.parametrize("k", [1, 2, 7, 50, 119, 120, 1000])
+def test_checkpoint_interval_does_not_change_results(k, path):
+    case = random_case(nt=120, S=2, ny=32, record=O.RECORD_RECEIVERS)
+    wx, wy = weights(case)
+    ref = run_gpu(case, wx, wy, ckpt_k=None, path=path)
+    got = run_gpu(case, wx, wy, ckpt_k=k, path=path)
     # recomputation replays the identical kernels: bit-identical results
     for a, b in zip(ref, got):
         assert np.array_equal(a, b)
+
+
+def test_resident_and_step_paths_agree():
+    case = random_case(nx=64, ny=64, nt=150, S=2, record=O.RECORD_RECEIVERS, nrec=16)
+    wx, wy = weights(case)
+    a = run_gpu(case, wx, wy, ckpt_k=30, path=E.PATH_STEP)
+    b = run_gpu(case, wx, wy, ckpt_k=30, path=E.PATH_RESIDENT)
+    for x, y in zip(a, b):
+        assert rel(x, y) <= 1e-5
+
+
+def test_resident_path_rejects_unsupported_problem():
+    case = random_case(nx=20, ny=18, nt=10, mode=O.MODE_DFIELD)  # per-cell mode, ny % 4 != 0
+    wx, wy = weights(case)
+    with pytest.raises(E._lib.ErnnError):
+        run_gpu(case, wx, wy, path=E.PATH_RESIDENT)
 
 
 @pytest.mark.parametrize("mode", [O.MODE_FIELDS, O.MODE_DFIELD])
