@@ -291,13 +291,14 @@ def run_ernn(args, dist):
     prof = E._lib.profile_read()
     E._lib.profile(False)
     cls = max(("forward", "adjoint"), key=lambda c: prof[c][0])
-    tot_ms, nlaunch = prof[cls]
+    tot_ms, nlaunch, tot_bytes = prof[cls]
     per_launch_ms = tot_ms / max(nlaunch, 1)
-    N = w.nshots * w.nx * w.ny
-    alg_bytes = {"forward": 24, "adjoint": 32}[cls] * N     # see DESIGN: bytes per cell-step
+    alg_bytes = tot_bytes / max(nlaunch, 1)        # algorithmic bytes per launch (library-counted)
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    kernel_name = {"forward": "fwd_step_kernel", "adjoint": "adj_step_kernel"}[cls]
+    resident = nlaunch < w.nt                        # one launch per pass, not per step
+    kernel_name = ("resident_kernel" if resident else
+                   {"forward": "fwd_step_kernel", "adjoint": "adj_step_kernel"}[cls])
     traffic = profiled_traffic(kernel_name, args.workload)
 
     rec = {
@@ -327,7 +328,7 @@ def run_ernn(args, dist):
         "ms_per_iter": round(ms, 4),
         "wall_ms_per_step": round(wall * 1e3 / args.steps, 4),
         "gpu_launches": int(launches * args.steps),
-        "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": round(achieved, 2),
+        "roofline": {"bound": "hbm", "kernel": kernel_name, "class": cls, "achieved": round(achieved, 2),
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": traffic, "alg_bytes_per_launch": alg_bytes,

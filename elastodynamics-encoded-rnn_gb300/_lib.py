@@ -56,7 +56,7 @@ SIGNATURES = {
                                     _P]),
     "ernn_launch_count": (ctypes.c_uint64, []),
     "ernn_profile_enable": (ctypes.c_int, [ctypes.c_int]),
-    "ernn_profile_read": (ctypes.c_int, [_P, _P]),
+    "ernn_profile_read": (ctypes.c_int, [_P, _P, _P]),
 }
 
 
@@ -66,11 +66,14 @@ def profile(enable: bool) -> None:
 
 
 def profile_read():
-    """{class: (total_ms, launches)} for classes 'forward', 'adjoint', 'other'."""
+    """{class: (total_ms, launches, algorithmic_bytes)} for classes 'forward',
+    'adjoint', 'other'."""
     ms = (ctypes.c_double * 3)()
     n = (ctypes.c_uint64 * 3)()
-    call("ernn_profile_read", ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(n, ctypes.c_void_p))
-    return {name: (ms[i], int(n[i])) for i, name in enumerate(("forward", "adjoint", "other"))}
+    b = (ctypes.c_double * 3)()
+    call("ernn_profile_read", ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(n, ctypes.c_void_p),
+         ctypes.cast(b, ctypes.c_void_p))
+    return {name: (ms[i], int(n[i]), b[i]) for i, name in enumerate(("forward", "adjoint", "other"))}
 
 _LIB = None
 

@@ -457,9 +457,9 @@ int ernn_profile_enable(int enable) {
   return ERNN_OK;
 }
 
-int ernn_profile_read(double* ms3, uint64_t* launches3) {
+int ernn_profile_read(double* ms3, uint64_t* launches3, double* alg_bytes3) {
   if (ms3 == nullptr || launches3 == nullptr) return ERNN_ERR_INVALID;
-  return profile_read(ms3, launches3) == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
+  return profile_read(ms3, launches3, alg_bytes3) == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -28,16 +28,20 @@ struct Profiler {
   bool on = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool[kProfClasses];
   size_t used[kProfClasses] = {0, 0, 0};
+  double alg_bytes[kProfClasses] = {0.0, 0.0, 0.0};
 };
 Profiler g_prof;
 }  // namespace
 
 void profile_enable(bool on) {
   g_prof.on = on;
-  for (int c = 0; c < kProfClasses; ++c) g_prof.used[c] = 0;
+  for (int c = 0; c < kProfClasses; ++c) {
+    g_prof.used[c] = 0;
+    g_prof.alg_bytes[c] = 0.0;
+  }
 }
 
-cudaError_t profile_read(double* ms, uint64_t* count) {
+cudaError_t profile_read(double* ms, uint64_t* count, double* alg_bytes) {
   for (int c = 0; c < kProfClasses; ++c) {
     double total = 0.0;
     for (size_t i = 0; i < g_prof.used[c]; ++i) {
@@ -50,6 +54,7 @@ cudaError_t profile_read(double* ms, uint64_t* count) {
     }
     if (ms) ms[c] = total;
     if (count) count[c] = g_prof.used[c];
+    if (alg_bytes) alg_bytes[c] = g_prof.alg_bytes[c];
   }
   return cudaSuccess;
 }
@@ -57,8 +62,9 @@ cudaError_t profile_read(double* ms, uint64_t* count) {
 // Launch `fn` (which enqueues one kernel on st), counting it and, while the
 // profiler is on, bracketing it with events of class `cls`.
 template <class Fn>
-static cudaError_t tracked(int cls, cudaStream_t st, Fn&& fn) {
+static cudaError_t tracked(int cls, cudaStream_t st, Fn&& fn, double alg_bytes = 0.0) {
   if (g_prof.on) {
+    g_prof.alg_bytes[cls] += alg_bytes;
     auto& pool = g_prof.pool[cls];
     if (g_prof.used[cls] == pool.size()) {
       cudaEvent_t a, b;
@@ -81,8 +87,9 @@ dim3 step_grid(int nx, int ny, int S) {
   return dim3((unsigned)((ny + TY - 1) / TY), (unsigned)((nx + TX - 1) / TX), (unsigned)S);
 }
 
-cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>& fn) {
-  return tracked(cls, st, fn);
+cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>& fn,
+                           double alg_bytes) {
+  return tracked(cls, st, fn, alg_bytes);
 }
 
 // --------------------------------------------------------------------------
@@ -603,24 +610,26 @@ cudaError_t launch_coef(int mode, const float* C, const float* rho, double h, do
 
 cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st) {
   const dim3 grid = step_grid(a.nx, a.ny, a.S), block(TY, NTHR / TY);
+  const double cells = (double)a.S * a.nx * a.ny;
   return tracked(kProfForward, st, [&] {
     switch (mode) {
       case kModeScalar: fwd_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
       case kModeDField: fwd_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
       default: fwd_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
     }
-  });
+  }, cells * alg_bytes_forward(mode));
 }
 
 cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st) {
   const dim3 grid = step_grid(a.nx, a.ny, a.S), block(TY, NTHR / TY);
+  const double cells = (double)a.S * a.nx * a.ny;
   return tracked(kProfAdjoint, st, [&] {
     switch (mode) {
       case kModeScalar: adj_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
       case kModeDField: adj_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
       default: adj_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
     }
-  });
+  }, cells * alg_bytes_adjoint(mode));
 }
 
 cudaError_t launch_gather(const float* state, int nx, int ny, int S, const int32_t* rec_idx,

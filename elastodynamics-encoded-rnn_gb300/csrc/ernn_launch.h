@@ -85,8 +85,23 @@ constexpr int kProfAdjoint = 1;
 constexpr int kProfOther = 2;
 constexpr int kProfClasses = 3;
 void profile_enable(bool on);
-// Enqueue one kernel through `fn`, counting it and timing it while profiling.
-cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>& fn);
-cudaError_t profile_read(double* ms, uint64_t* count);
+cudaError_t profile_read(double* ms, uint64_t* count, double* alg_bytes);
+// Enqueue one kernel through `fn`, counting it and, while profiling, timing it
+// and adding its algorithmic DRAM bytes to its class.
+cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>& fn,
+                           double alg_bytes = 0.0);
+
+// Algorithmic bytes per cell-step (the minimum DRAM traffic of a step whose
+// state does not fit on chip):
+//   forward: read u^n and u^{n-1}, write u^{n+1}: 3 x 8 B, plus 4 B of D or
+//            24 B of constant planes in the per-cell modes;
+//   adjoint: read lam^{m+1}, lam^{m+2}, u^m, write lam^m: 4 x 8 B, plus the
+//            per-cell inputs and the read-modify-write of per-cell gradients.
+inline double alg_bytes_forward(int mode) {
+  return 24.0 + (mode == kModeDField ? 4.0 : mode == kModeFields ? 24.0 : 0.0);
+}
+inline double alg_bytes_adjoint(int mode) {
+  return 32.0 + (mode == kModeDField ? 4.0 + 8.0 : mode == kModeFields ? 24.0 + 48.0 : 0.0);
+}
 
 }  // namespace ernn

@@ -170,7 +170,9 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   float* L1 = smem + level_floats;
   float* U0 = smem + 2 * level_floats;  // adjoint role: u^m tiles
   float* U1 = smem + 3 * level_floats;
-  int* rec_list = reinterpret_cast<int*>(smem + (is_fwd ? 2 : 4) * level_floats);  // [kResMaxRec][2]
+  float* F = smem + 2 * level_floats;   // forward role: source load of the own rows [R][ny]
+  const int extra = is_fwd ? R * ny : 2 * level_floats;
+  int* rec_list = reinterpret_cast<int*>(smem + 2 * level_floats + extra);  // [kResMaxRec][2]
   int* rec_count = rec_list + 2 * kResMaxRec;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(rec_count + 4);  // 8-byte aligned (see host)
 
@@ -180,10 +182,20 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   const size_t shot_off = (size_t)shot * 2 * N;
 
   // -------- initial state: zero everything this role uses, then load
-  const int nlev = is_fwd ? 2 : 4;
-  for (int e = tid; e < nlev * level_floats; e += kResThreads) smem[e] = 0.f;
+  for (int e = tid; e < 2 * level_floats + extra; e += kResThreads) smem[e] = 0.f;
   if (tid == 0) *rec_count = 0;
   __syncthreads();
+  if (is_fwd && c.bx > 0 && c.by > 0) {
+    // the shot's load restricted to the own rows, kept in shared memory so the
+    // update adds amp * F without touching global memory
+    const int ox = c.src_origin[2 * shot], oy = c.src_origin[2 * shot + 1];
+    for (int e = tid; e < c.bx * c.by; e += kResThreads) {
+      const int sa = e / c.by, sb = e - sa * c.by;
+      const int gi = ox + sa, gj = oy + sb;
+      if (gi >= r0 && gi < r0 + rows && gj >= 0 && gj < ny)
+        F[(gi - r0) * ny + gj] = c.src_map[(size_t)shot * c.bx * c.by + e];
+    }
+  }
   // receivers owned by this CTA
   if (c.nrec > 0) {
     for (int r = tid; r < c.nrec; r += kResThreads) {
@@ -230,14 +242,15 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
 
   if (is_fwd) {
     // ================================================================ forward role
-    const bool has_src = c.bx > 0 && c.by > 0;
-    const int ox = has_src ? c.src_origin[2 * shot] : 0, oy = has_src ? c.src_origin[2 * shot + 1] : 0;
+    const float* sig = c.src_signal + (size_t)shot * c.nt;
+    float amp_next = (f.i0 < f.i1) ? sig[f.i0] : 0.f;
     for (int i = f.i0; i < f.i1; ++i) {
       const bool odd = ((i - f.i0) & 1) != 0;
       float* cur = odd ? L1 : L0;
       float* nxt = odd ? L0 : L1;
       const int nxt_off = (int)(nxt - smem);
-      const float amp = c.src_signal[(size_t)shot * c.nt + i] * kappa;
+      const float amp = amp_next * kappa;
+      amp_next = (i + 1 < f.i1) ? sig[i + 1] : 0.f;  // in flight during this step
       float* st_out = f.states ? f.states + (size_t)(i - f.i0) * f.state_stride + shot_off : nullptr;
       float* ck0 = nullptr;
       float* ck1 = nullptr;
@@ -272,6 +285,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
           const float2 prevx = *px, prevy = *py;
           float vx[2], vy[2];
           const int gi = r0 + lr;
+          const float2 fl = *reinterpret_cast<const float2*>(F + lr * ny + j);
 #pragma unroll
           for (int q = 0; q < 2; ++q) {
             float lx, ly;
@@ -279,11 +293,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
             const float pxv = q ? prevx.y : prevx.x, pyv = q ? prevy.y : prevy.x;
             vx[q] = (2.f * st.cx[q] - pxv) + lx;
             vy[q] = (2.f * st.cy[q] - pyv) + ly;
-            const int sa = gi - ox, sb = j + q - oy;
-            if (has_src && sa >= 0 && sa < c.bx && sb >= 0 && sb < c.by) {
-              const float fz = amp * c.src_map[((size_t)shot * c.bx + sa) * c.by + sb];
-              if (c.src_comp == 0) vx[q] += fz; else vy[q] += fz;
-            }
+            const float fz = amp * (q ? fl.y : fl.x);
+            if (c.src_comp == 0) vx[q] += fz; else vy[q] += fz;
           }
           const float2 nvx = make_float2(vx[0], vx[1]), nvy = make_float2(vy[0], vy[1]);
           *px = nvx;
@@ -352,6 +363,24 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   const int m_top_img = min(a.m_hi, c.nt - 1);  // highest m with an imaging term
   if (m_top_img >= a.m_lo + 1) prefetch(m_top_img);
 
+  // residuals of the receivers this thread injects (entries tid, tid + kResThreads),
+  // loaded one recording step ahead
+  float gnx[2] = {0.f, 0.f}, gny[2] = {0.f, 0.f};
+  int next_src = a.m_hi - ((a.m_hi - 1) % c.stride);  // highest m <= m_hi with a frame
+  auto load_g = [&](int m) {
+    const int frame = (m - 1) / c.stride;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int e = tid + h * kResThreads;
+      if (e < nloc) {
+        const size_t go = ((size_t)shot * c.nt_out + frame) * c.nrec + rec_list[2 * e + 1];
+        gnx[h] = a.g_x[go];
+        gny[h] = a.g_y[go];
+      }
+    }
+  };
+  if (!DENSE && next_src >= a.m_lo + 1) load_g(next_src);
+
   float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   double acc64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   int since_flush = 0;
@@ -369,12 +398,17 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     if (!DENSE && src_step) {
       // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: subtract g from the own
       // copy of lam^{m+2}, which only the owning thread reads this step
-      for (int e = tid; e < nloc; e += kResThreads) {
-        const int off = rec_list[2 * e], r = rec_list[2 * e + 1];
-        const size_t go = ((size_t)shot * c.nt_out + frame) * c.nrec + r;
-        atomicAdd(&T.comp(nxt, 0)[off], -gs * a.g_x[go]);
-        atomicAdd(&T.comp(nxt, 1)[off], -gs * a.g_y[go]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int e = tid + h * kResThreads;
+        if (e < nloc) {
+          const int off = rec_list[2 * e];
+          atomicAdd(&T.comp(nxt, 0)[off], -gs * gnx[h]);
+          atomicAdd(&T.comp(nxt, 1)[off], -gs * gny[h]);
+        }
       }
+      next_src = m - c.stride;
+      if (next_src >= a.m_lo + 1) load_g(next_src);
       __syncthreads();
     }
     float* U = (m & 1) ? U1 : U0;
@@ -504,7 +538,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
 size_t resident_smem_bytes(const ResCommon& c, bool with_adjoint) {
   const size_t level = 2 * (size_t)(c.R + 2) * c.ny * sizeof(float);
   const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 2 * sizeof(uint64_t) + 16;
-  return (with_adjoint ? 4 : 2) * level + tail;
+  const size_t fwd = 2 * level + (size_t)c.R * c.ny * sizeof(float);
+  return (with_adjoint ? 4 * level : fwd) + tail;
 }
 
 static cudaError_t configure(const void* fn, size_t smem) {
@@ -564,10 +599,13 @@ cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResAdj& a
   // blockIdx.z == fwd_z runs the forward role
   const int fwd_z = run_fwd ? (run_adj ? 1 : 0) : -1;
   const int cls = run_adj ? kProfAdjoint : kProfForward;
+  const double cells = (double)c.S * c.nx * c.ny;
+  const double bytes = cells * ((run_fwd ? alg_bytes_forward(kModeScalar) * (f.i1 - f.i0) : 0.0) +
+                                (run_adj ? alg_bytes_adjoint(kModeScalar) * (a.m_hi - a.m_lo) : 0.0));
   return tracked_launch(cls, st, [&] {
     if (dense) cudaLaunchKernelEx(&cfg, resident_kernel<true>, c, f, a, fwd_z);
     else cudaLaunchKernelEx(&cfg, resident_kernel<false>, c, f, a, fwd_z);
-  });
+  }, bytes);
 }
 
 }  // namespace ernn

@@ -163,10 +163,11 @@ uint64_t ernn_launch_count(void);
 int ernn_profile_enable(int enable);
 
 /* Totals since ernn_profile_enable(1), per kernel class
- * [0: forward step, 1: adjoint step, 2: everything else]: device time in
- * milliseconds (ms3[3], host) and launch counts (launches3[3], host).
- * Waits for the recorded events. (host call) */
-int ernn_profile_read(double* ms3, uint64_t* launches3);
+ * [0: forward time loop, 1: adjoint time loop, 2: everything else]: device
+ * time in milliseconds (ms3[3], host), launch counts (launches3[3], host) and
+ * the algorithmic DRAM bytes of the work those launches did (alg_bytes3[3],
+ * host, may be NULL).  Waits for the recorded events. (host call) */
+int ernn_profile_read(double* ms3, uint64_t* launches3, double* alg_bytes3);
 
 #ifdef __cplusplus
 }

@@ -110,9 +110,14 @@ def test_checkpoint_interval_does_not_change_results(k, path):
     wx, wy = weights(case)
     ref = run_gpu(case, wx, wy, ckpt_k=None, path=path)
     got = run_gpu(case, wx, wy, ckpt_k=k, path=path)
-    # recomputation replays the identical kernels: bit-identical results
-    for a, b in zip(ref, got):
-        assert np.array_equal(a, b)
+    # recomputation replays the identical kernels: bit-identical forward outputs
+    assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
+    if path == E.PATH_STEP:
+        assert np.array_equal(ref[2], got[2])
+    else:
+        # the resident path flushes its FP32 partial sums to FP64 at segment
+        # boundaries, so the grouping (not the terms) depends on k
+        assert rel(got[2], ref[2]) <= 1e-6
 
 
 def test_resident_and_step_paths_agree():
@@ -267,8 +272,11 @@ def test_cpu_tensors_raise_instead_of_falling_back():
 
 def test_launch_counter_counts_kernels():
     lib = E.load_library()
-    n0 = lib.ernn_launch_count()
     case = random_case(nx=16, ny=16, nt=10)
     wx, wy = weights(case)
-    run_gpu(case, wx, wy)
+    n0 = lib.ernn_launch_count()
+    run_gpu(case, wx, wy, path=E.PATH_STEP)        # one launch per step and pass
     assert lib.ernn_launch_count() - n0 >= 20
+    n0 = lib.ernn_launch_count()
+    run_gpu(case, wx, wy, path=E.PATH_RESIDENT)    # one launch per pass
+    assert 3 <= lib.ernn_launch_count() - n0 < 20
