@@ -90,6 +90,20 @@ __device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity
   }
 }
 
+// 1D bulk copy shared (this CTA) -> global in the current bulk group.
+__device__ __forceinline__ void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"(smem_u32(ssrc)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// wait until the committed bulk stores have finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// wait until the committed bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // ---------------------------------------------------------------- layout
 struct Tile {
   int R, ny, rows;      // rows: valid rows of this CTA (<= R)
@@ -99,24 +113,27 @@ struct Tile {
   __device__ __forceinline__ int at(int s, int j) const { return s * ny + j; }
 };
 
-// load one smem row window [j-1, j, j+1, j+2] of one component (zero outside 0..ny-1)
-__device__ __forceinline__ void load_row(const float* __restrict__ p, int j, int ny, float w[4]) {
-  const float2 m = *reinterpret_cast<const float2*>(p + j);
+// Row window [j-1 .. j+4] of one component (zero outside 0..ny-1); j % 4 == 0.
+__device__ __forceinline__ void load_row6(const float* __restrict__ p, int j, int ny, float w[6]) {
+  const float4 m = *reinterpret_cast<const float4*>(p + j);
   w[0] = (j >= 1) ? p[j - 1] : 0.f;
   w[1] = m.x;
   w[2] = m.y;
-  w[3] = (j + 2 < ny) ? p[j + 2] : 0.f;
+  w[3] = m.z;
+  w[4] = m.w;
+  w[5] = (j + 4 < ny) ? p[j + 4] : 0.f;
 }
 
-struct Pair {
-  float cx[2], cy[2];
-  float xx_x[2], yy_x[2], xy_x[2], xx_y[2], yy_y[2], xy_y[2];
+// Stencil sums of the four cells (j .. j+3) of a row from its three row
+// windows (rows above, at, below).
+struct Quad {
+  float cx[4], cy[4];
+  float xx_x[4], yy_x[4], xy_x[4], xx_y[4], yy_y[4], xy_y[4];
 };
 
-// stencil sums of the two cells (j, j+1) of a row from its three row windows
-__device__ __forceinline__ void pair_stencils(const float ux[3][4], const float uy[3][4], Pair& s) {
+__device__ __forceinline__ void quad_stencils(const float ux[3][6], const float uy[3][6], Quad& s) {
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
+  for (int q = 0; q < 4; ++q) {
     const int k = q + 1;
     s.cx[q] = ux[1][k];
     s.cy[q] = uy[1][k];
@@ -133,18 +150,167 @@ struct KSr {
   float k11, k22, kq12, k16, k26, k66, k16h, k26h;
 };
 
-__device__ __forceinline__ void lq(const KSr& k, const Pair& s, int q, float& lx, float& ly) {
+__device__ __forceinline__ void lq(const KSr& k, const Quad& s, int q, float& lx, float& ly) {
   lx = k.k11 * s.xx_x[q] + k.k66 * s.yy_x[q] + k.kq12 * s.xy_y[q] + k.k16h * s.xy_x[q] +
        k.k16 * s.xx_y[q] + k.k26 * s.yy_y[q];
   ly = k.k66 * s.xx_y[q] + k.k22 * s.yy_y[q] + k.kq12 * s.xy_x[q] + k.k16 * s.xx_x[q] +
        k.k26 * s.yy_x[q] + k.k26h * s.xy_y[q];
 }
 
-__device__ __forceinline__ void shift_windows(float ux[3][4], float uy[3][4]) {
+__device__ __forceinline__ void shift6(float u[3][6]) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    ux[0][k] = ux[1][k]; ux[1][k] = ux[2][k];
-    uy[0][k] = uy[1][k]; uy[1][k] = uy[2][k];
+  for (int k = 0; k < 6; ++k) { u[0][k] = u[1][k]; u[1][k] = u[2][k]; }
+}
+
+__device__ __forceinline__ float4 f4(const float v[4]) { return make_float4(v[0], v[1], v[2], v[3]); }
+__device__ __forceinline__ float at4(const float4& v, int q) {
+  return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w;
+}
+
+// Per-step context of one CTA.
+struct StepCtx {
+  const float* cur;   // level read with its halo (u^n or lam^{m+1})
+  float* nxt;         // level holding the previous value, overwritten by the new one
+  int nxt_off;        // nxt - smem (for DSMEM pushes)
+  float* up_nb;       // smem of CTA rank-1 (generic address) or nullptr
+  float* dn_nb;       // smem of CTA rank+1 or nullptr
+  int rows, R, ny;
+};
+
+// Forward: one 4-row x 4-column item starting at local row lr0, column j.
+template <bool FULL>
+__device__ __forceinline__ void fwd_item(const Tile& T, const KSr& ks, const StepCtx& x,
+                                         const float* __restrict__ F, float amp, int src_comp,
+                                         int lr0, int j) {
+  const int ny = x.ny;
+  float wx[3][6], wy[3][6];
+  load_row6(T.comp(const_cast<float*>(x.cur), 0) + T.at(lr0, 0), j, ny, wx[0]);
+  load_row6(T.comp(const_cast<float*>(x.cur), 1) + T.at(lr0, 0), j, ny, wy[0]);
+  load_row6(T.comp(const_cast<float*>(x.cur), 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
+  load_row6(T.comp(const_cast<float*>(x.cur), 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
+#pragma unroll
+  for (int q4 = 0; q4 < 4; ++q4) {
+    const int lr = lr0 + q4;
+    if (!FULL && lr >= x.rows) break;
+    const int s = lr + 1;
+    load_row6(T.comp(const_cast<float*>(x.cur), 0) + T.at(s + 1, 0), j, ny, wx[2]);
+    load_row6(T.comp(const_cast<float*>(x.cur), 1) + T.at(s + 1, 0), j, ny, wy[2]);
+    Quad st;
+    quad_stencils(wx, wy, st);
+    float4* px = reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j));
+    float4* py = reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j));
+    const float4 pvx = *px, pvy = *py;
+    const float4 fl = *reinterpret_cast<const float4*>(F + lr * ny + j);
+    float vx[4], vy[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float lx, ly;
+      lq(ks, st, q, lx, ly);
+      vx[q] = (2.f * st.cx[q] - at4(pvx, q)) + lx;
+      vy[q] = (2.f * st.cy[q] - at4(pvy, q)) + ly;
+      const float fz = amp * at4(fl, q);
+      if (src_comp == 0) vx[q] += fz; else vy[q] += fz;
+    }
+    const float4 nvx = f4(vx), nvy = f4(vy);
+    *px = nvx;
+    *py = nvy;
+    if (lr == 0 && x.up_nb) {
+      const int o = x.nxt_off + T.at(x.R + 1, j);
+      *reinterpret_cast<float4*>(x.up_nb + o) = nvx;
+      *reinterpret_cast<float4*>(x.up_nb + o + T.plane) = nvy;
+    }
+    if (lr == x.rows - 1 && x.dn_nb) {
+      const int o = x.nxt_off + T.at(0, j);
+      *reinterpret_cast<float4*>(x.dn_nb + o) = nvx;
+      *reinterpret_cast<float4*>(x.dn_nb + o + T.plane) = nvy;
+    }
+    shift6(wx);
+    shift6(wy);
+  }
+}
+
+// Adjoint: one 4 x 4 item; lam^m into nxt and the imaging sums of
+// lam^{m+1} against u^m (tile U) into acc.
+template <bool FULL, bool DENSE>
+__device__ __forceinline__ void adj_item(const Tile& T, const KSr& ks, const StepCtx& x,
+                                         const float* U, bool img, const float* gx,
+                                         const float* gy, float gs, int lr0, int j, float acc[6]) {
+  const int ny = x.ny;
+  float wx[3][6], wy[3][6], vx_[3][6], vy_[3][6];
+  float* cur = const_cast<float*>(x.cur);
+  float* Uu = const_cast<float*>(U);
+  load_row6(T.comp(cur, 0) + T.at(lr0, 0), j, ny, wx[0]);
+  load_row6(T.comp(cur, 1) + T.at(lr0, 0), j, ny, wy[0]);
+  load_row6(T.comp(cur, 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
+  load_row6(T.comp(cur, 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
+  if (img) {
+    load_row6(T.comp(Uu, 0) + T.at(lr0, 0), j, ny, vx_[0]);
+    load_row6(T.comp(Uu, 1) + T.at(lr0, 0), j, ny, vy_[0]);
+    load_row6(T.comp(Uu, 0) + T.at(lr0 + 1, 0), j, ny, vx_[1]);
+    load_row6(T.comp(Uu, 1) + T.at(lr0 + 1, 0), j, ny, vy_[1]);
+  }
+#pragma unroll
+  for (int q4 = 0; q4 < 4; ++q4) {
+    const int lr = lr0 + q4;
+    if (!FULL && lr >= x.rows) break;
+    const int s = lr + 1;
+    load_row6(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
+    load_row6(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
+    Quad st;
+    quad_stencils(wx, wy, st);
+    float4* px = reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j));
+    float4* py = reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j));
+    const float4 pvx = *px, pvy = *py;
+    float vx[4], vy[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float lx, ly;
+      lq(ks, st, q, lx, ly);
+      vx[q] = (2.f * st.cx[q] - at4(pvx, q)) + lx;
+      vy[q] = (2.f * st.cy[q] - at4(pvy, q)) + ly;
+    }
+    if (DENSE && gx != nullptr) {
+      const float4 a4 = *reinterpret_cast<const float4*>(gx + (size_t)lr * ny + j);
+      const float4 b4 = *reinterpret_cast<const float4*>(gy + (size_t)lr * ny + j);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        vx[q] += gs * at4(a4, q);
+        vy[q] += gs * at4(b4, q);
+      }
+    }
+    const float4 nvx = f4(vx), nvy = f4(vy);
+    *px = nvx;
+    *py = nvy;
+    if (lr == 0 && x.up_nb) {
+      const int o = x.nxt_off + T.at(x.R + 1, j);
+      *reinterpret_cast<float4*>(x.up_nb + o) = nvx;
+      *reinterpret_cast<float4*>(x.up_nb + o + T.plane) = nvy;
+    }
+    if (lr == x.rows - 1 && x.dn_nb) {
+      const int o = x.nxt_off + T.at(0, j);
+      *reinterpret_cast<float4*>(x.dn_nb + o) = nvx;
+      *reinterpret_cast<float4*>(x.dn_nb + o + T.plane) = nvy;
+    }
+    if (img) {
+      load_row6(T.comp(Uu, 0) + T.at(s + 1, 0), j, ny, vx_[2]);
+      load_row6(T.comp(Uu, 1) + T.at(s + 1, 0), j, ny, vy_[2]);
+      Quad su;
+      quad_stencils(vx_, vy_, su);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float l1x = st.cx[q], l1y = st.cy[q];  // lam^{m+1} at the cell
+        acc[0] += l1x * su.xx_x[q];
+        acc[1] += l1y * su.yy_y[q];
+        acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
+        acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
+        acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
+        acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
+      }
+      shift6(vx_);
+      shift6(vy_);
+    }
+    shift6(wx);
+    shift6(wy);
   }
 }
 
@@ -234,11 +400,16 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   cluster.sync();  // every CTA initialised before any DSMEM push
 
   const int nloc = min(*rec_count, kResMaxRec);
-  const int ncp = ny / 2;                      // column pairs
+  const int ncq = ny / 4;                      // column quads
   const int ngr = (rows + 3) / 4;              // row groups of 4
-  const int nitems = ncp * ngr;
-  float* up_nb = (rank > 0) ? cluster.map_shared_rank(smem, rank - 1) : nullptr;
-  float* dn_nb = (rank < CL - 1) ? cluster.map_shared_rank(smem, rank + 1) : nullptr;
+  const int nitems = ncq * ngr;
+  StepCtx x;
+  x.up_nb = (rank > 0) ? cluster.map_shared_rank(smem, rank - 1) : nullptr;
+  x.dn_nb = (rank < CL - 1) ? cluster.map_shared_rank(smem, rank + 1) : nullptr;
+  x.rows = rows;
+  x.R = R;
+  x.ny = ny;
+  const uint32_t own_bytes = (uint32_t)((size_t)rows * ny * sizeof(float));
 
   if (is_fwd) {
     // ================================================================ forward role
@@ -246,100 +417,58 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     float amp_next = (f.i0 < f.i1) ? sig[f.i0] : 0.f;
     for (int i = f.i0; i < f.i1; ++i) {
       const bool odd = ((i - f.i0) & 1) != 0;
-      float* cur = odd ? L1 : L0;
-      float* nxt = odd ? L0 : L1;
-      const int nxt_off = (int)(nxt - smem);
+      x.cur = odd ? L1 : L0;
+      x.nxt = odd ? L0 : L1;
+      x.nxt_off = (int)(x.nxt - smem);
       const float amp = amp_next * kappa;
       amp_next = (i + 1 < f.i1) ? sig[i + 1] : 0.f;  // in flight during this step
-      float* st_out = f.states ? f.states + (size_t)(i - f.i0) * f.state_stride + shot_off : nullptr;
-      float* ck0 = nullptr;
-      float* ck1 = nullptr;
+      for (int it = tid; it < nitems; it += kResThreads) {
+        const int qc = it % ncq, g = it / ncq;
+        if (4 * g + 4 <= rows) fwd_item<true>(T, ks, x, F, amp, c.src_comp, 4 * g, 4 * qc);
+        else fwd_item<false>(T, ks, x, F, amp, c.src_comp, 4 * g, 4 * qc);
+      }
+      // the bulk stores issued after the previous barrier read the level this
+      // CTA overwrites next step: make sure they are done reading
+      if (tid == 0) bulk_wait_read_all();
+      cluster.sync();
+      // u^{i+1} (own rows of nxt) to global memory through the bulk-copy engine
+      float* dst[4] = {nullptr, nullptr, nullptr, nullptr};
+      ptrdiff_t dst_y[4] = {(ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N};  // y plane offset
+      if (f.states) dst[0] = f.states + (size_t)(i - f.i0) * f.state_stride + shot_off;
       if (f.ckpt != nullptr) {
         if ((i + 1) % f.ck_k == 0 && (i + 1) / f.ck_k <= f.ck_nseg - 1)
-          ck0 = f.ckpt + ((size_t)((i + 1) / f.ck_k - 1) * 2 + 0) * f.state_stride + shot_off;
+          dst[1] = f.ckpt + ((size_t)((i + 1) / f.ck_k - 1) * 2 + 0) * f.state_stride + shot_off;
         if ((i + 2) % f.ck_k == 0 && (i + 2) / f.ck_k <= f.ck_nseg - 1)
-          ck1 = f.ckpt + ((size_t)((i + 2) / f.ck_k - 1) * 2 + 1) * f.state_stride + shot_off;
+          dst[2] = f.ckpt + ((size_t)((i + 2) / f.ck_k - 1) * 2 + 1) * f.state_stride + shot_off;
       }
       const bool rec_step = (i % c.stride) == 0;
       const int frame = i / c.stride;
-      for (int it = tid; it < nitems; it += kResThreads) {
-        const int p = it % ncp, g = it / ncp;
-        const int j = 2 * p;
-        const int lr0 = 4 * g;
-        float wx[3][4], wy[3][4];
-        load_row(T.comp(cur, 0) + T.at(lr0, 0), j, ny, wx[0]);
-        load_row(T.comp(cur, 1) + T.at(lr0, 0), j, ny, wy[0]);
-        load_row(T.comp(cur, 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
-        load_row(T.comp(cur, 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
-#pragma unroll
-        for (int q4 = 0; q4 < 4; ++q4) {
-          const int lr = lr0 + q4;  // local row
-          if (lr >= rows) break;
-          const int s = lr + 1;
-          load_row(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
-          load_row(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
-          Pair st;
-          pair_stencils(wx, wy, st);
-          float2* px = reinterpret_cast<float2*>(T.comp(nxt, 0) + T.at(s, j));
-          float2* py = reinterpret_cast<float2*>(T.comp(nxt, 1) + T.at(s, j));
-          const float2 prevx = *px, prevy = *py;
-          float vx[2], vy[2];
-          const int gi = r0 + lr;
-          const float2 fl = *reinterpret_cast<const float2*>(F + lr * ny + j);
-#pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            float lx, ly;
-            lq(ks, st, q, lx, ly);
-            const float pxv = q ? prevx.y : prevx.x, pyv = q ? prevy.y : prevy.x;
-            vx[q] = (2.f * st.cx[q] - pxv) + lx;
-            vy[q] = (2.f * st.cy[q] - pyv) + ly;
-            const float fz = amp * (q ? fl.y : fl.x);
-            if (c.src_comp == 0) vx[q] += fz; else vy[q] += fz;
-          }
-          const float2 nvx = make_float2(vx[0], vx[1]), nvy = make_float2(vy[0], vy[1]);
-          *px = nvx;
-          *py = nvy;
-          if (lr == 0 && up_nb) {
-            const int o = nxt_off + T.at(R + 1, j);
-            *reinterpret_cast<float2*>(up_nb + o) = nvx;
-            *reinterpret_cast<float2*>(up_nb + o + T.plane) = nvy;
-          }
-          if (lr == rows - 1 && dn_nb) {
-            const int o = nxt_off + T.at(0, j);
-            *reinterpret_cast<float2*>(dn_nb + o) = nvx;
-            *reinterpret_cast<float2*>(dn_nb + o + T.plane) = nvy;
-          }
-          const size_t go = (size_t)gi * ny + j;
-          if (st_out) {
-            *reinterpret_cast<float2*>(st_out + go) = nvx;
-            *reinterpret_cast<float2*>(st_out + N + go) = nvy;
-          }
-          if (ck0) {
-            *reinterpret_cast<float2*>(ck0 + go) = nvx;
-            *reinterpret_cast<float2*>(ck0 + N + go) = nvy;
-          }
-          if (ck1) {
-            *reinterpret_cast<float2*>(ck1 + go) = nvx;
-            *reinterpret_cast<float2*>(ck1 + N + go) = nvy;
-          }
-          if (DENSE && rec_step && f.hist_x) {
-            const size_t ho = ((size_t)shot * c.nt_out + frame) * N + go;
-            *reinterpret_cast<float2*>(f.hist_x + ho) = nvx;
-            *reinterpret_cast<float2*>(f.hist_y + ho) = nvy;
-          }
-          shift_windows(wx, wy);
-        }
+      if (DENSE && rec_step && f.hist_x) {
+        dst[3] = f.hist_x + ((size_t)shot * c.nt_out + frame) * N;
+        dst_y[3] = f.hist_y - f.hist_x;  // the y history relative to the x history
       }
-      cluster.sync();
+      if (tid == 0 && (dst[0] || dst[1] || dst[2] || dst[3])) {
+        fence_proxy_async();
+        const float* srcx = T.comp(x.nxt, 0) + T.at(1, 0);
+        const float* srcy = T.comp(x.nxt, 1) + T.at(1, 0);
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+          if (!dst[d]) continue;
+          bulk_s2g(dst[d] + (size_t)r0 * ny, srcx, own_bytes);
+          bulk_s2g(dst[d] + dst_y[d] + (size_t)r0 * ny, srcy, own_bytes);
+        }
+        bulk_commit();
+      }
       if (!DENSE && rec_step && f.tr_x) {
         for (int e = tid; e < nloc; e += kResThreads) {
           const int off = rec_list[2 * e], r = rec_list[2 * e + 1];
           const size_t o = ((size_t)shot * c.nt_out + frame) * c.nrec + r;
-          f.tr_x[o] = T.comp(nxt, 0)[off];
-          f.tr_y[o] = T.comp(nxt, 1)[off];
+          f.tr_x[o] = T.comp(x.nxt, 0)[off];
+          f.tr_y[o] = T.comp(x.nxt, 1)[off];
         }
       }
     }
+    if (tid == 0) bulk_wait_all();
     return;
   }
 
@@ -363,14 +492,17 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   const int m_top_img = min(a.m_hi, c.nt - 1);  // highest m with an imaging term
   if (m_top_img >= a.m_lo + 1) prefetch(m_top_img);
 
-  // residuals of the receivers this thread injects (entries tid, tid + kResThreads),
+  // residuals of the receivers this thread injects (entries tid + h * kResThreads),
   // loaded one recording step ahead
-  float gnx[2] = {0.f, 0.f}, gny[2] = {0.f, 0.f};
+  constexpr int kRecPerThread = (kResMaxRec + kResThreads - 1) / kResThreads;
+  float gnx[kRecPerThread], gny[kRecPerThread];
+#pragma unroll
+  for (int h = 0; h < kRecPerThread; ++h) { gnx[h] = 0.f; gny[h] = 0.f; }
   int next_src = a.m_hi - ((a.m_hi - 1) % c.stride);  // highest m <= m_hi with a frame
   auto load_g = [&](int m) {
     const int frame = (m - 1) / c.stride;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < kRecPerThread; ++h) {
       const int e = tid + h * kResThreads;
       if (e < nloc) {
         const size_t go = ((size_t)shot * c.nt_out + frame) * c.nrec + rec_list[2 * e + 1];
@@ -381,16 +513,21 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   };
   if (!DENSE && next_src >= a.m_lo + 1) load_g(next_src);
 
-  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  // Imaging sums: this thread's cells of one step in FP32 (acc), accumulated
+  // over steps as an unevaluated FP32 pair hi + lo (TwoSum, exact up to the
+  // pair's ~48-bit precision), converted to FP64 once per launch and reduced
+  // in FP64 across threads, CTAs and launches.
+  float acc[6], hi[6], lo[6];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) { acc[t] = 0.f; hi[t] = 0.f; lo[t] = 0.f; }
   double acc64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  int since_flush = 0;
   int last_level = 0;
   for (int m = a.m_hi; m >= a.m_lo + 1; --m) {
     const bool odd = ((a.m_hi - m) & 1) != 0;
-    float* cur = odd ? L1 : L0;  // lam^{m+1}
-    float* nxt = odd ? L0 : L1;  // lam^{m+2}, becomes lam^m
+    x.cur = odd ? L1 : L0;  // lam^{m+1}
+    x.nxt = odd ? L0 : L1;  // lam^{m+2}, becomes lam^m
     last_level = odd ? 0 : 1;
-    const int nxt_off = (int)(nxt - smem);
+    x.nxt_off = (int)(x.nxt - smem);
     const bool img = (m <= c.nt - 1);
     if (img && m - 1 >= a.m_lo + 1) prefetch(m - 1);
     const bool src_step = ((m - 1) % c.stride) == 0;
@@ -399,110 +536,50 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: subtract g from the own
       // copy of lam^{m+2}, which only the owning thread reads this step
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < kRecPerThread; ++h) {
         const int e = tid + h * kResThreads;
         if (e < nloc) {
           const int off = rec_list[2 * e];
-          atomicAdd(&T.comp(nxt, 0)[off], -gs * gnx[h]);
-          atomicAdd(&T.comp(nxt, 1)[off], -gs * gny[h]);
+          atomicAdd(&T.comp(x.nxt, 0)[off], -gs * gnx[h]);
+          atomicAdd(&T.comp(x.nxt, 1)[off], -gs * gny[h]);
         }
       }
       next_src = m - c.stride;
       if (next_src >= a.m_lo + 1) load_g(next_src);
       __syncthreads();
     }
-    float* U = (m & 1) ? U1 : U0;
+    const float* U = (m & 1) ? U1 : U0;
     if (img) {
       mbar_wait_bounded(&mbar[m & 1], phase[m & 1], c.err);
       phase[m & 1] ^= 1u;
     }
-    for (int it = tid; it < nitems; it += kResThreads) {
-      const int p = it % ncp, g = it / ncp;
-      const int j = 2 * p;
-      const int lr0 = 4 * g;
-      float wx[3][4], wy[3][4], vx_[3][4], vy_[3][4];
-      load_row(T.comp(cur, 0) + T.at(lr0, 0), j, ny, wx[0]);
-      load_row(T.comp(cur, 1) + T.at(lr0, 0), j, ny, wy[0]);
-      load_row(T.comp(cur, 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
-      load_row(T.comp(cur, 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
-      if (img) {
-        load_row(T.comp(U, 0) + T.at(lr0, 0), j, ny, vx_[0]);
-        load_row(T.comp(U, 1) + T.at(lr0, 0), j, ny, vy_[0]);
-        load_row(T.comp(U, 0) + T.at(lr0 + 1, 0), j, ny, vx_[1]);
-        load_row(T.comp(U, 1) + T.at(lr0 + 1, 0), j, ny, vy_[1]);
-      }
-#pragma unroll
-      for (int q4 = 0; q4 < 4; ++q4) {
-        const int lr = lr0 + q4;
-        if (lr >= rows) break;
-        const int s = lr + 1;
-        load_row(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
-        load_row(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
-        Pair st;
-        pair_stencils(wx, wy, st);
-        float2* px = reinterpret_cast<float2*>(T.comp(nxt, 0) + T.at(s, j));
-        float2* py = reinterpret_cast<float2*>(T.comp(nxt, 1) + T.at(s, j));
-        const float2 prevx = *px, prevy = *py;
-        const int gi = r0 + lr;
-        float vx[2], vy[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          float lx, ly;
-          lq(ks, st, q, lx, ly);
-          const float pxv = q ? prevx.y : prevx.x, pyv = q ? prevy.y : prevy.x;
-          vx[q] = (2.f * st.cx[q] - pxv) + lx;
-          vy[q] = (2.f * st.cy[q] - pyv) + ly;
-        }
-        if (DENSE && src_step) {
-          const size_t go = ((size_t)shot * c.nt_out + frame) * N + (size_t)gi * ny + j;
-          const float2 gx = *reinterpret_cast<const float2*>(a.g_x + go);
-          const float2 gy = *reinterpret_cast<const float2*>(a.g_y + go);
-          vx[0] += gs * gx.x; vx[1] += gs * gx.y;
-          vy[0] += gs * gy.x; vy[1] += gs * gy.y;
-        }
-        const float2 nvx = make_float2(vx[0], vx[1]), nvy = make_float2(vy[0], vy[1]);
-        *px = nvx;
-        *py = nvy;
-        if (lr == 0 && up_nb) {
-          const int o = nxt_off + T.at(R + 1, j);
-          *reinterpret_cast<float2*>(up_nb + o) = nvx;
-          *reinterpret_cast<float2*>(up_nb + o + T.plane) = nvy;
-        }
-        if (lr == rows - 1 && dn_nb) {
-          const int o = nxt_off + T.at(0, j);
-          *reinterpret_cast<float2*>(dn_nb + o) = nvx;
-          *reinterpret_cast<float2*>(dn_nb + o + T.plane) = nvy;
-        }
-        if (img) {
-          load_row(T.comp(U, 0) + T.at(s + 1, 0), j, ny, vx_[2]);
-          load_row(T.comp(U, 1) + T.at(s + 1, 0), j, ny, vy_[2]);
-          Pair su;
-          pair_stencils(vx_, vy_, su);
-#pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            const float l1x = st.cx[q], l1y = st.cy[q];  // lam^{m+1} at the cell
-            acc[0] += l1x * su.xx_x[q];
-            acc[1] += l1y * su.yy_y[q];
-            acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
-            acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
-            acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
-            acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
-          }
-          shift_windows(vx_, vy_);
-        }
-        shift_windows(wx, wy);
-      }
+    const float* gxr = nullptr;
+    const float* gyr = nullptr;
+    if (DENSE && src_step) {
+      gxr = a.g_x + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
+      gyr = a.g_y + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
     }
-    // FP32 over at most 16 steps of this thread's cells, FP64 from there on
-    if (++since_flush == 16) {
+    for (int it = tid; it < nitems; it += kResThreads) {
+      const int qc = it % ncq, g = it / ncq;
+      if (4 * g + 4 <= rows)
+        adj_item<true, DENSE>(T, ks, x, U, img, gxr, gyr, gs, 4 * g, 4 * qc, acc);
+      else
+        adj_item<false, DENSE>(T, ks, x, U, img, gxr, gyr, gs, 4 * g, 4 * qc, acc);
+    }
+    if (img) {
 #pragma unroll
-      for (int t = 0; t < 6; ++t) { acc64[t] += (double)acc[t]; acc[t] = 0.f; }
-      since_flush = 0;
+      for (int t = 0; t < 6; ++t) {  // TwoSum(hi, acc) -> (hi, lo)
+        const float sum = hi[t] + acc[t];
+        const float bp = sum - hi[t];
+        lo[t] += (hi[t] - (sum - bp)) + (acc[t] - bp);
+        hi[t] = sum;
+        acc[t] = 0.f;
+      }
     }
     cluster.sync();
   }
 #pragma unroll
-  for (int t = 0; t < 6; ++t) acc64[t] += (double)acc[t];
+  for (int t = 0; t < 6; ++t) acc64[t] = (double)hi[t] + (double)lo[t];
 
   // lam^{m_lo+1} (last written level) and lam^{m_lo+2} -> lam_save
   if (a.m_hi >= a.m_lo + 1) {

@@ -9,7 +9,7 @@
 
 namespace ernn {
 
-constexpr int kResThreads = 512;  // threads per CTA
+constexpr int kResThreads = 256;  // threads per CTA (each owns 4 x 4-cell items)
 constexpr int kResMaxRec = 1024;  // receivers one CTA can own
 
 struct ResCommon {

@@ -125,8 +125,12 @@ def test_resident_and_step_paths_agree():
     wx, wy = weights(case)
     a = run_gpu(case, wx, wy, ckpt_k=30, path=E.PATH_STEP)
     b = run_gpu(case, wx, wy, ckpt_k=30, path=E.PATH_RESIDENT)
-    for x, y in zip(a, b):
-        assert rel(x, y) <= 1e-5
+    r = run_oracle(case, wx, wy)
+    for x, y, z in zip(a, b, r):
+        # each path against the FP64 run; the two FP32 paths sum the imaging
+        # products in different orders, so they agree to that rounding
+        assert rel(x, z) <= 2e-5 and rel(y, z) <= 2e-5, (rel(x, z), rel(y, z))
+        assert rel(x, y) <= 4e-5
 
 
 def test_resident_path_rejects_unsupported_problem():
