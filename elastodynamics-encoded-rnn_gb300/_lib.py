@@ -54,6 +54,8 @@ SIGNATURES = {
     "ernn_adjoint": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
                                     _P, _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, _P,
                                     _P]),
+    "ernn_forward_static": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
+                                           _P, _P, _P]),
     "ernn_launch_count": (ctypes.c_uint64, []),
     "ernn_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "ernn_profile_read": (ctypes.c_int, [_P, _P, _P]),

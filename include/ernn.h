@@ -153,6 +153,23 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
                  const float* g_uy, const void* tape, size_t tape_bytes, void* scratch,
                  size_t scratch_bytes, double* grad_C, float* grad_field, void* stream);
 
+/* Forward time loop that allocates nothing, for callers that cannot call
+ * cudaMalloc: code running while another framework captures a CUDA graph on
+ * the stream, real-time loops that cannot afford the device synchronisation
+ * of an allocation, FFI hosts without a device allocator.  Same problem,
+ * inputs, outputs and results as ernn_forward(with_tape = 0) on the per-step
+ * kernels; the two-level wavefield lives in an 8 MiB file-scope device array
+ * that every GPU loading the library keeps until exit.  Problems needing
+ * more than that (256 B + 2 x nshots x 2 x nx x ny x 4 B, each rounded up to
+ * 256 B) are rejected with ERNN_ERR_WORKSPACE.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current: make it before any stream capture; `stream` must belong to the
+ * current device.  All calls share the array, so calls that overlap on the
+ * GPU race; serialise them.  Produces no tape: there is no adjoint for it.
+ * No counterpart in the reference. */
+int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, float* out_uy,
+                        void* stream);
+
 /* Number of kernels this library has launched since it was loaded. (host call)
  * Diagnostic; no counterpart in the reference. */
 uint64_t ernn_launch_count(void);
