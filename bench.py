@@ -214,7 +214,7 @@ def run_ernn(args, dist):
     torch.cuda.set_device(dev)
     lib = E.load_library()
     w = make_workload(args)
-    inv = Hn.Inversion(w, dev)
+    inv = Hn.make_inversion(w, dev)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(max(args.warmup, 0)):
         inv.step()
@@ -251,7 +251,7 @@ def run_ernn(args, dist):
     # ---- e2e through the public API: pinned host traces in, loss + gradient out
     obs_h = [o.detach().cpu().pin_memory() for o in inv.obs]
     obs_d = [torch.empty_like(o) for o in inv.obs]
-    out_h = torch.empty(7, dtype=torch.float64).pin_memory()
+    out_h = torch.empty(1 + inv.gradient().numel(), dtype=torch.float64).pin_memory()
     e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
     dist.barrier()
@@ -262,7 +262,7 @@ def run_ernn(args, dist):
         for hsrc, ddst in zip(obs_h, obs_d):
             ddst.copy_(hsrc, non_blocking=True)
         loss = inv.step(obs_d)
-        res = torch.cat([loss.detach().reshape(1), inv.params.theta.grad.double()])
+        res = torch.cat([loss.detach().reshape(1), inv.gradient().double().reshape(-1)])
         out_h.copy_(res, non_blocking=True)
         e2e_ev[k][1].record()
     torch.cuda.synchronize()
@@ -271,15 +271,13 @@ def run_ernn(args, dist):
     d2h = out_h.numel() * out_h.element_size()
 
     # ---- forward-only throughput (no tape)
-    geom_f = inv.geom
-    C = inv.params().detach()
     fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
     with torch.no_grad():
         for k in range(args.steps):
             flush.zero_()
             fev[k][0].record()
-            E.propagate(C, inv.rho, geom_f)
+            inv.forward_only()
             fev[k][1].record()
     torch.cuda.synchronize()
     fwd_ms = dist.max(sum(a.elapsed_time(b) for a, b in fev) / args.steps)

@@ -189,6 +189,13 @@ class Inversion:
         self.opt.step()
         return loss
 
+    def forward_only(self):
+        with torch.no_grad():
+            return propagate(self.params().detach(), self.rho, self.geom)
+
+    def gradient(self):
+        return self.params.theta.grad
+
     def constants(self):
         return self.params().detach().double().cpu().numpy()
 
@@ -196,3 +203,52 @@ class Inversion:
         C, T = self.constants(), self.w.C_true
         sc = scales(T)
         return np.abs(C - T) / sc
+
+
+class DamageInversion:
+    """One inversion iteration of the degradation-map workload: D(x) trained by
+    Adam with C(x) = (1 - D(x)) C0 (initial guess D = 0)."""
+
+    def __init__(self, w: Workload, device, lr=1e-2, seed=0, nt=None):
+        if w.D_true is None:
+            raise ValueError("workload has no degradation map")
+        self.w = w
+        self.device = device
+        self.geom = geometry(w, device, nt)
+        self.obs = observed(w, self.geom, device, seed=seed)
+        self.rho = torch.tensor(RHO, device=device)
+        self.C0 = torch.tensor(w.C_true, dtype=torch.float32, device=device)
+        self.D = torch.nn.Parameter(torch.zeros((w.nx, w.ny), device=device))
+        self.opt = torch.optim.Adam([self.D], lr=lr)
+
+    def step(self, obs=None):
+        obs = self.obs if obs is None else obs
+        self.opt.zero_grad(set_to_none=True)
+        ux, uy = propagate(self.C0, self.rho, self.geom, D=self.D)
+        loss = trace_misfit(ux, uy, obs[0], obs[1])
+        loss.backward()
+        self.opt.step()
+        return loss
+
+    def forward_only(self):
+        with torch.no_grad():
+            return propagate(self.C0, self.rho, self.geom, D=self.D.detach())
+
+    def gradient(self):
+        return self.D.grad
+
+
+def make_inversion(w: Workload, device, **kw):
+    """The inversion iteration matching the workload (constants or degradation map)."""
+    return DamageInversion(w, device, **kw) if w.D_true is not None else Inversion(w, device, **kw)
+
+
+def run_inversion(w: Workload, device, iters=200, lr=1e-2, seed=0):
+    """Adam on normalised constants for `iters` iterations; returns the final
+    constants, their errors relative to each constant's scale, and the loss history."""
+    inv = Inversion(w, device, lr=lr, seed=seed)
+    losses = []
+    for _ in range(iters):
+        losses.append(inv.step())
+    losses = [float(v) for v in torch.stack(losses).cpu()]
+    return inv.constants(), inv.relative_errors(), losses
