@@ -14,17 +14,19 @@ namespace {
 
 constexpr size_t kAlign = 256;
 constexpr double kPi = 3.14159265358979323846;
+// segment length of the resident reverse pass when the tape keeps every state
+constexpr int kResStoreAllSegment = 128;
 inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 // Workspace plan of one problem.
 struct Plan {
-  int S, nx, ny, nt, k, nseg, nt_out, nblocks, npart;
+  int S, nx, ny, nt, k, nseg, nt_out, nblocks, npart, kres;
   bool store_all;
   size_t N, state_bytes;
   // tape
   size_t t_coef, t_A, t_B, t_store, t_total_tape, t_total_notape;
   // adjoint scratch
-  size_t s_coef, s_LA, s_LB, s_seg, s_gacc, s_part, s_total;
+  size_t s_coef, s_LA, s_LB, s_seg, s_lbuf, s_gacc, s_part, s_total;
 };
 
 Plan make_plan(const ErnnProblem& p) {
@@ -54,11 +56,16 @@ Plan make_plan(const ErnnProblem& p) {
   // two recompute segments: the cluster-resident path recomputes segment j-1
   // while the adjoint consumes segment j
   pl.s_seg = off; if (!pl.store_all) off += (size_t)2 * pl.k * pl.state_bytes;
+  // lam buffers of the resident reverse pass: two segments of kres steps
+  pl.kres = pl.store_all ? (p.nt < kResStoreAllSegment ? p.nt : kResStoreAllSegment) : pl.k;
+  pl.s_lbuf = off; off += (size_t)2 * pl.kres * pl.state_bytes;
   pl.s_gacc = off;
   if (p.mode == kModeDField) off += align_up((size_t)p.nshots * pl.N * sizeof(float));
   if (p.mode == kModeFields) off += align_up((size_t)p.nshots * 6 * pl.N * sizeof(float));
   pl.s_part = off;
-  pl.npart = pl.nblocks > p.nshots * 16 ? pl.nblocks : p.nshots * 16;
+  // partial-sum rows: per-step path one per block; resident path one per
+  // imaging CTA (at most 8 clusters of 16 per shot)
+  pl.npart = pl.nblocks > p.nshots * 16 * 8 ? pl.nblocks : p.nshots * 16 * 8;
   if (p.mode == kModeScalar) off += align_up((size_t)pl.npart * 8 * sizeof(double));
   pl.s_total = off;
   return pl;
@@ -154,60 +161,78 @@ int resident_forward(const ErnnProblem& p, const Plan& pl, ResCommon& rc, float*
   const bool dense = (p.record == kRecordFields);
   if (dense) { f.hist_x = out_ux; f.hist_y = out_uy; }
   else { f.tr_x = out_ux; f.tr_y = out_uy; }
-  ResAdj a;
+  ResLam a;
   std::memset(&a, 0, sizeof(a));
-  ERNN_CUDA(launch_resident(rc, f, a, true, false, dense, st));
+  ResImg g;
+  std::memset(&g, 0, sizeof(g));
+  ERNN_CUDA(launch_resident(rc, f, a, g, true, false, false, dense, st));
   return ERNN_OK;
 }
 
+// Reverse pass of the resident path, in segments of ks steps, one launch per
+// segment j (from the last): LAM runs the adjoint over segment j and stores
+// every lam into lbuf[j & 1]; FWD recomputes segment j from its checkpoint
+// into ubuf[j & 1] (not needed when the tape holds every state); IMG forms the
+// imaging sums of segment j + 1 from the buffers of the previous launch.
 int resident_adjoint(const ErnnProblem& p, const Plan& pl, ResCommon& rc, const float* g_ux,
                      const float* g_uy, void* tape, void* scratch, double* partials,
-                     cudaStream_t st) {
+                     int* img_rows, cudaStream_t st) {
   const size_t ss = pl.state_bytes / sizeof(float);
   const bool dense = (p.record == kRecordFields);
-  ResAdj a;
-  std::memset(&a, 0, sizeof(a));
-  a.state_stride = ss;
-  a.lam_save = fat(scratch, pl.s_LA);
-  a.save_stride = ss;  // LB follows LA
-  a.g_x = g_ux; a.g_y = g_uy;
-  a.partials = partials;
-  ResFwd f;
-  std::memset(&f, 0, sizeof(f));
-  f.state_stride = ss;
-  if (pl.store_all) {
-    a.m_hi = p.nt; a.m_lo = 0;
-    a.u_states = fat(tape, pl.t_store);
-    a.u_base = 1;
-    a.first = 1;
-    ERNN_CUDA(launch_resident(rc, f, a, false, true, dense, st));
-    return ERNN_OK;
-  }
-  auto seg = [&](int j) { return fat(scratch, pl.s_seg + (size_t)(j & 1) * pl.k * pl.state_bytes); };
+  const int ks = pl.kres;
+  const int nseg = (p.nt + ks - 1) / ks;
+  auto lbuf = [&](int j) { return fat(scratch, pl.s_lbuf + (size_t)(j & 1) * ks * pl.state_bytes); };
+  auto ubuf = [&](int j) -> float* {
+    if (pl.store_all) return fat(tape, pl.t_store + (size_t)j * ks * pl.state_bytes);  // u^{jk+1}..
+    return fat(scratch, pl.s_seg + (size_t)(j & 1) * pl.k * pl.state_bytes);
+  };
   auto ck = [&](int j, int lev) -> const float* {
     if (j == 0) return nullptr;
     if (lev == 1 && j * pl.k - 1 == 0) return nullptr;  // u^0 = 0 (k == 1)
     return fat(tape, pl.t_store + ((size_t)(j - 1) * 2 + lev) * pl.state_bytes);
   };
-  auto set_recompute = [&](int j) {  // steps of segment j; u^nt is never imaged
-    f.i0 = j * pl.k;
-    f.i1 = (j + 1) * pl.k < p.nt - 1 ? (j + 1) * pl.k : p.nt - 1;
-    f.init_cur = ck(j, 0);
-    f.init_prev = ck(j, 1);
-    f.states = seg(j);
-  };
-  const int last = pl.nseg - 1;
-  set_recompute(last);
-  if (f.i1 > f.i0) ERNN_CUDA(launch_resident(rc, f, a, true, false, dense, st));
-  for (int j = last; j >= 0; --j) {
-    a.m_hi = (j + 1) * pl.k < p.nt ? (j + 1) * pl.k : p.nt;
-    a.m_lo = j * pl.k;
-    a.u_states = seg(j);
-    a.u_base = j * pl.k + 1;
-    a.first = (j == last) ? 1 : 0;
-    const bool overlap = j >= 1;
-    if (overlap) set_recompute(j - 1);
-    ERNN_CUDA(launch_resident(rc, f, a, overlap, true, dense, st));
+  ResLam a;
+  std::memset(&a, 0, sizeof(a));
+  a.lam_save = fat(scratch, pl.s_LA);
+  a.save_stride = ss;  // LB follows LA
+  a.g_x = g_ux; a.g_y = g_uy;
+  a.state_stride = ss;
+  ResFwd f;
+  std::memset(&f, 0, sizeof(f));
+  f.state_stride = ss;
+  ResImg g;
+  std::memset(&g, 0, sizeof(g));
+  g.state_stride = ss;
+  g.partials = partials;
+  *img_rows = resident_img_clusters(rc) * rc.S * rc.CL;
+  for (int j = nseg - 1; j >= -1; --j) {
+    const bool run_lam = j >= 0;
+    bool run_fwd = false;
+    if (run_lam) {
+      a.m_hi = (j + 1) * ks < p.nt ? (j + 1) * ks : p.nt;
+      a.m_lo = j * ks;
+      a.first = (j == nseg - 1) ? 1 : 0;
+      a.lbuf = lbuf(j);
+      a.slot_base = j * ks + 2;
+      a.store_init = (a.m_hi <= p.nt - 1) ? 1 : 0;
+      if (!pl.store_all) {  // recompute u^{jk+1} .. u^{min((j+1)k, nt-1)}
+        f.i0 = j * pl.k;
+        f.i1 = (j + 1) * pl.k < p.nt - 1 ? (j + 1) * pl.k : p.nt - 1;
+        f.init_cur = ck(j, 0);
+        f.init_prev = ck(j, 1);
+        f.states = ubuf(j);
+        run_fwd = f.i1 > f.i0;
+      }
+    }
+    const int jj = j + 1;  // segment imaged in this launch
+    g.n_lo = jj * ks + 1;
+    g.n_hi = (jj + 1) * ks < p.nt - 1 ? (jj + 1) * ks : p.nt - 1;
+    const bool run_img = jj <= nseg - 1 && g.n_hi >= g.n_lo;
+    if (run_img) {
+      g.lbuf = lbuf(jj);
+      g.ubuf = ubuf(jj);
+    }
+    ERNN_CUDA(launch_resident(rc, f, a, g, run_fwd, run_lam, run_img, dense, st));
   }
   return ERNN_OK;
 }
@@ -385,8 +410,10 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   if (p->path != ERNN_PATH_STEP) {
     ResCommon res;
     if (pick_resident(*p, *in, coef, res)) {
-      if ((rc = resident_adjoint(*p, pl, res, g_ux, g_uy, tape, scratch, partials, st))) return rc;
-      ERNN_CUDA(launch_finalize_scalar(partials, p->nshots * res.CL, coef, grad_C, st));
+      int img_rows = 0;
+      if ((rc = resident_adjoint(*p, pl, res, g_ux, g_uy, tape, scratch, partials, &img_rows, st)))
+        return rc;
+      ERNN_CUDA(launch_finalize_scalar(partials, img_rows, coef, grad_C, st));
       return ERNN_OK;
     }
     if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;

@@ -5,22 +5,22 @@
 // Partition: CTA c of the cluster owns grid rows [c R, c R + R) (x), all ny
 // columns.  Its shared memory holds two levels of the field (ping-pong) with
 // one halo row above and below:  buf[level][comp][R + 2][ny].
-// One step: every thread computes a 4 x 2 block of cells from the current
-// level, writes the new values into the other level (which holds the level
-// before, read by the same thread first), and pushes its CTA's first and last
-// row into the halo rows of the neighbouring CTAs through DSMEM stores.  One
-// cluster barrier (release/acquire) per step publishes the pushes; no step
-// touches global memory except for outputs (traces, history, checkpoints,
-// stored states).
+// One step: every thread computes 4 x 4-cell items from the current level,
+// writes the new values into the other level (which holds the level before,
+// read by the same thread first), and pushes its CTA's first and last row
+// into the halo rows of the neighbouring CTAs through DSMEM stores.  One
+// cluster barrier (release/acquire) per step publishes the pushes.  States
+// that must reach global memory leave through TMA bulk copies.
 //
-// The adjoint role streams u^m (the forward state the imaging condition needs,
-// with halo rows) from global memory with TMA bulk copies into a
-// double-buffered tile, completed on an mbarrier: the copy of u^{m-1} is in
-// flight while step m computes.
-//
-// A launch runs up to two roles per shot, selected by blockIdx.z: a forward
-// role (steps i0..i1-1) and an adjoint role (m = m_hi .. m_lo+1), so the
-// recomputation of checkpoint segment j-1 overlaps the adjoint of segment j.
+// A launch runs up to three roles, selected by blockIdx.z:
+//   FWD  steps i0..i1-1 of the forward recursion (the forward pass, or the
+//        recomputation of a checkpoint segment into a segment buffer);
+//   LAM  steps m_hi..m_lo+1 of the adjoint recursion, which needs no forward
+//        state, storing every lam it produces into a lam buffer;
+//   IMG  the imaging condition of the previous segment: products of
+//        lam^{n+1} with the stencils of u^n, independent across n and cells,
+//        spread over all remaining SMs.
+// Within a launch the roles share no data, so no cluster waits on another.
 //
 // Scalar constants only (the per-cell modes use the per-step kernels).
 #include <cooperative_groups.h>
@@ -37,57 +37,8 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-
-// 1D bulk copy global -> shared (this CTA), completing `bytes` on `bar`.
-// dst, src 16-byte aligned, bytes a multiple of 16.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait: gives up after ~2^31 cycles (about a second), records the
-// timeout in *err and returns so that every barrier of the kernel is still
-// matched.
-__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
-  if (mbar_try_wait(bar, parity)) return;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > (1ll << 31)) {
-      atomicExch(err, 5 /* ERNN_ERR_TIMEOUT */);
-      return;
-    }
-  }
 }
 
 // 1D bulk copy shared (this CTA) -> global in the current bulk group.
@@ -229,26 +180,18 @@ __device__ __forceinline__ void fwd_item(const Tile& T, const KSr& ks, const Ste
   }
 }
 
-// Adjoint: one 4 x 4 item; lam^m into nxt and the imaging sums of
-// lam^{m+1} against u^m (tile U) into acc.
+// Adjoint: one 4 x 4 item, lam^m into nxt.
 template <bool FULL, bool DENSE>
-__device__ __forceinline__ void adj_item(const Tile& T, const KSr& ks, const StepCtx& x,
-                                         const float* U, bool img, const float* gx,
-                                         const float* gy, float gs, int lr0, int j, float acc[6]) {
+__device__ __forceinline__ void lam_item(const Tile& T, const KSr& ks, const StepCtx& x,
+                                         const float* gx, const float* gy, float gs, int lr0,
+                                         int j) {
   const int ny = x.ny;
-  float wx[3][6], wy[3][6], vx_[3][6], vy_[3][6];
+  float wx[3][6], wy[3][6];
   float* cur = const_cast<float*>(x.cur);
-  float* Uu = const_cast<float*>(U);
   load_row6(T.comp(cur, 0) + T.at(lr0, 0), j, ny, wx[0]);
   load_row6(T.comp(cur, 1) + T.at(lr0, 0), j, ny, wy[0]);
   load_row6(T.comp(cur, 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
   load_row6(T.comp(cur, 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
-  if (img) {
-    load_row6(T.comp(Uu, 0) + T.at(lr0, 0), j, ny, vx_[0]);
-    load_row6(T.comp(Uu, 1) + T.at(lr0, 0), j, ny, vy_[0]);
-    load_row6(T.comp(Uu, 0) + T.at(lr0 + 1, 0), j, ny, vx_[1]);
-    load_row6(T.comp(Uu, 1) + T.at(lr0 + 1, 0), j, ny, vy_[1]);
-  }
 #pragma unroll
   for (int q4 = 0; q4 < 4; ++q4) {
     const int lr = lr0 + q4;
@@ -291,39 +234,126 @@ __device__ __forceinline__ void adj_item(const Tile& T, const KSr& ks, const Ste
       *reinterpret_cast<float4*>(x.dn_nb + o) = nvx;
       *reinterpret_cast<float4*>(x.dn_nb + o + T.plane) = nvy;
     }
-    if (img) {
-      load_row6(T.comp(Uu, 0) + T.at(s + 1, 0), j, ny, vx_[2]);
-      load_row6(T.comp(Uu, 1) + T.at(s + 1, 0), j, ny, vy_[2]);
-      Quad su;
-      quad_stencils(vx_, vy_, su);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float l1x = st.cx[q], l1y = st.cy[q];  // lam^{m+1} at the cell
-        acc[0] += l1x * su.xx_x[q];
-        acc[1] += l1y * su.yy_y[q];
-        acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
-        acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
-        acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
-        acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
-      }
-      shift6(vx_);
-      shift6(vy_);
-    }
     shift6(wx);
     shift6(wy);
   }
 }
 
+// Row window [j-1 .. j+4] of row i of a global plane (zero outside the grid).
+__device__ __forceinline__ void load_grow6(const float* __restrict__ plane, int i, int j, int nx,
+                                           int ny, float w[6]) {
+  if (i < 0 || i >= nx) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[k] = 0.f;
+    return;
+  }
+  const float* p = plane + (size_t)i * ny;
+  const float4 m = __ldg(reinterpret_cast<const float4*>(p + j));
+  w[0] = (j >= 1) ? __ldg(p + j - 1) : 0.f;
+  w[1] = m.x;
+  w[2] = m.y;
+  w[3] = m.z;
+  w[4] = m.w;
+  w[5] = (j + 4 < ny) ? __ldg(p + j + 4) : 0.f;
+}
+
+// Imaging of one 4 x 4 item of step n: sum over its cells of lam^{n+1} times
+// the derivatives of A u^n with respect to the six constants.
+__device__ __forceinline__ void img_item(const float* __restrict__ lam, const float* __restrict__ u,
+                                         size_t N, int nx, int ny, int i0, int j, float acc[6]) {
+  float vx[3][6], vy[3][6];
+  load_grow6(u, i0 - 1, j, nx, ny, vx[0]);
+  load_grow6(u + N, i0 - 1, j, nx, ny, vy[0]);
+  load_grow6(u, i0, j, nx, ny, vx[1]);
+  load_grow6(u + N, i0, j, nx, ny, vy[1]);
+#pragma unroll
+  for (int q4 = 0; q4 < 4; ++q4) {
+    const int i = i0 + q4;
+    if (i >= nx) break;
+    load_grow6(u, i + 1, j, nx, ny, vx[2]);
+    load_grow6(u + N, i + 1, j, nx, ny, vy[2]);
+    Quad su;
+    quad_stencils(vx, vy, su);
+    const float4 lx4 = __ldg(reinterpret_cast<const float4*>(lam + (size_t)i * ny + j));
+    const float4 ly4 = __ldg(reinterpret_cast<const float4*>(lam + N + (size_t)i * ny + j));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float l1x = at4(lx4, q), l1y = at4(ly4, q);
+      acc[0] += l1x * su.xx_x[q];
+      acc[1] += l1y * su.yy_y[q];
+      acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
+      acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
+      acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
+      acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
+    }
+    shift6(vx);
+    shift6(vy);
+  }
+}
+
+// FP64 block reduction of six per-thread sums into one row of partials.
+__device__ __forceinline__ void block_reduce6(const double v6[6], double* __restrict__ row) {
+  __shared__ double red[kResThreads / 32][6];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    double v = v6[t];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][t] = v;
+  }
+  __syncthreads();
+  if (tid < 6) {
+    double v = 0.0;
+    for (int w = 0; w < kResThreads / 32; ++w) v += red[w][tid];
+    row[tid] += v;
+  }
+}
+
+// IMG role: items (shot, n, row group, column quad) spread over all IMG CTAs;
+// products summed in FP32 over an item's 16 cells, in FP64 from there on.
+__device__ void imaging_role(const ResCommon& c, const ResImg& g, int cta, int ncta) {
+  const size_t N = (size_t)c.nx * c.ny;
+  const int ngr = (c.nx + 3) / 4, ncq = c.ny / 4;
+  const int nn = g.n_hi - g.n_lo + 1;
+  const long long per_n = (long long)ngr * ncq;
+  const long long total = (long long)c.S * nn * per_n;
+  double acc64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (long long it = (long long)cta * kResThreads + threadIdx.x; it < total;
+       it += (long long)ncta * kResThreads) {
+    const int shot = (int)(it / ((long long)nn * per_n));
+    const long long r = it - (long long)shot * nn * per_n;
+    const int dn = (int)(r / per_n);
+    const int rem = (int)(r - (long long)dn * per_n);
+    const int gi = rem / ncq, qc = rem - gi * ncq;
+    const size_t slot = (size_t)dn * g.state_stride + (size_t)shot * 2 * N;
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    img_item(g.lbuf + slot, g.ubuf + slot, N, c.nx, c.ny, 4 * gi, 4 * qc, acc);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) acc64[t] += (double)acc[t];
+  }
+  block_reduce6(acc64, g.partials + (size_t)cta * 8);
+}
+
 // ---------------------------------------------------------------- kernel
 template <bool DENSE>
 __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommon c, const ResFwd f,
-                                                                   const ResAdj a, int fwd_z) {
+                                                                   const ResLam a, const ResImg g,
+                                                                   const ResRoles roles) {
+  const int z = (int)blockIdx.z;
+  if (roles.z_img >= 0 && z >= roles.z_img) {
+    // IMG role: no cluster features, no shared state
+    const int cta = ((z - roles.z_img) * (int)gridDim.y + (int)blockIdx.y) * (int)gridDim.x +
+                    (int)blockIdx.x;
+    const int ncta = (roles.n_img_z * (int)gridDim.y) * (int)gridDim.x;
+    imaging_role(c, g, cta, ncta);
+    return;
+  }
   extern __shared__ __align__(128) float smem[];
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int CL = c.CL;
   const int shot = blockIdx.y;
-  const bool is_fwd = ((int)blockIdx.z == fwd_z);
+  const bool is_fwd = (z == roles.z_fwd);
   const int tid = threadIdx.x;
   const int nx = c.nx, ny = c.ny, R = c.R;
   const size_t N = (size_t)nx * ny;
@@ -334,21 +364,17 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
 
   float* L0 = smem;
   float* L1 = smem + level_floats;
-  float* U0 = smem + 2 * level_floats;  // adjoint role: u^m tiles
-  float* U1 = smem + 3 * level_floats;
   float* F = smem + 2 * level_floats;   // forward role: source load of the own rows [R][ny]
-  const int extra = is_fwd ? R * ny : 2 * level_floats;
-  int* rec_list = reinterpret_cast<int*>(smem + 2 * level_floats + extra);  // [kResMaxRec][2]
+  int* rec_list = reinterpret_cast<int*>(F + R * ny);  // [kResMaxRec][2]
   int* rec_count = rec_list + 2 * kResMaxRec;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(rec_count + 4);  // 8-byte aligned (see host)
 
   const KSr ks{c.coef->k11, c.coef->k22, c.coef->kq12, c.coef->k16,
                c.coef->k26, c.coef->k66, c.coef->k16h, c.coef->k26h};
   const float kappa = c.coef->kappa;
   const size_t shot_off = (size_t)shot * 2 * N;
 
-  // -------- initial state: zero everything this role uses, then load
-  for (int e = tid; e < 2 * level_floats + extra; e += kResThreads) smem[e] = 0.f;
+  // -------- initial state: zero the levels and the load, then load
+  for (int e = tid; e < 2 * level_floats + R * ny; e += kResThreads) smem[e] = 0.f;
   if (tid == 0) *rec_count = 0;
   __syncthreads();
   if (is_fwd && c.bx > 0 && c.by > 0) {
@@ -386,16 +412,10 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     const int s = rem / ny, j = rem - s * ny;
     const int gi = r0 + s - 1;
     if (gi < 0 || gi >= nx) continue;
-    const size_t g = shot_off + (size_t)comp * N + (size_t)gi * ny + j;
-    if (init_cur) T.comp(L0, comp)[T.at(s, j)] = init_cur[g];
-    if (init_prev && s >= 1 && s <= rows) T.comp(L1, comp)[T.at(s, j)] = init_prev[g];
+    const size_t gidx = shot_off + (size_t)comp * N + (size_t)gi * ny + j;
+    if (init_cur) T.comp(L0, comp)[T.at(s, j)] = init_cur[gidx];
+    if (init_prev && s >= 1 && s <= rows) T.comp(L1, comp)[T.at(s, j)] = init_prev[gidx];
   }
-  if (!is_fwd && tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
-    fence_mbar_init();
-  }
-  fence_proxy_async();
   __syncthreads();
   cluster.sync();  // every CTA initialised before any DSMEM push
 
@@ -410,9 +430,15 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   x.R = R;
   x.ny = ny;
   const uint32_t own_bytes = (uint32_t)((size_t)rows * ny * sizeof(float));
+  // own rows of a level -> global state at dst (x plane, y plane at +N)
+  auto store_level = [&](const float* level, float* dst, ptrdiff_t y_off) {
+    bulk_s2g(dst + (size_t)r0 * ny, T.comp(const_cast<float*>(level), 0) + T.at(1, 0), own_bytes);
+    bulk_s2g(dst + y_off + (size_t)r0 * ny, T.comp(const_cast<float*>(level), 1) + T.at(1, 0),
+             own_bytes);
+  };
 
   if (is_fwd) {
-    // ================================================================ forward role
+    // ================================================================ FWD role
     const float* sig = c.src_signal + (size_t)shot * c.nt;
     float amp_next = (f.i0 < f.i1) ? sig[f.i0] : 0.f;
     for (int i = f.i0; i < f.i1; ++i) {
@@ -423,9 +449,9 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       const float amp = amp_next * kappa;
       amp_next = (i + 1 < f.i1) ? sig[i + 1] : 0.f;  // in flight during this step
       for (int it = tid; it < nitems; it += kResThreads) {
-        const int qc = it % ncq, g = it / ncq;
-        if (4 * g + 4 <= rows) fwd_item<true>(T, ks, x, F, amp, c.src_comp, 4 * g, 4 * qc);
-        else fwd_item<false>(T, ks, x, F, amp, c.src_comp, 4 * g, 4 * qc);
+        const int qc = it % ncq, gq = it / ncq;
+        if (4 * gq + 4 <= rows) fwd_item<true>(T, ks, x, F, amp, c.src_comp, 4 * gq, 4 * qc);
+        else fwd_item<false>(T, ks, x, F, amp, c.src_comp, 4 * gq, 4 * qc);
       }
       // the bulk stores issued after the previous barrier read the level this
       // CTA overwrites next step: make sure they are done reading
@@ -449,14 +475,9 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       }
       if (tid == 0 && (dst[0] || dst[1] || dst[2] || dst[3])) {
         fence_proxy_async();
-        const float* srcx = T.comp(x.nxt, 0) + T.at(1, 0);
-        const float* srcy = T.comp(x.nxt, 1) + T.at(1, 0);
 #pragma unroll
-        for (int d = 0; d < 4; ++d) {
-          if (!dst[d]) continue;
-          bulk_s2g(dst[d] + (size_t)r0 * ny, srcx, own_bytes);
-          bulk_s2g(dst[d] + dst_y[d] + (size_t)r0 * ny, srcy, own_bytes);
-        }
+        for (int d = 0; d < 4; ++d)
+          if (dst[d]) store_level(x.nxt, dst[d], dst_y[d]);
         bulk_commit();
       }
       if (!DENSE && rec_step && f.tr_x) {
@@ -472,26 +493,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     return;
   }
 
-  // ================================================================== adjoint role
+  // ================================================================== LAM role
   const float gs = c.coef->gscale;
-  const int r_lo = max(r0 - 1, 0), r_hi = min(r0 + rows + 1, nx);
-  const int dst_row = r_lo - (r0 - 1);
-  const uint32_t copy_bytes = (uint32_t)((r_hi - r_lo) * ny * sizeof(float));
-  uint32_t phase[2] = {0u, 0u};
-  auto prefetch = [&](int m) {  // u^m -> U[m & 1]
-    if (tid == 0) {
-      float* dst = (m & 1) ? U1 : U0;
-      const float* src = a.u_states + (size_t)(m - a.u_base) * a.state_stride + shot_off;
-      fence_proxy_async();
-      mbar_arrive_expect_tx(&mbar[m & 1], 2 * copy_bytes);
-      bulk_g2s(dst + T.at(dst_row, 0), src + (size_t)r_lo * ny, copy_bytes, &mbar[m & 1]);
-      bulk_g2s(dst + T.plane + T.at(dst_row, 0), src + N + (size_t)r_lo * ny, copy_bytes,
-               &mbar[m & 1]);
-    }
-  };
-  const int m_top_img = min(a.m_hi, c.nt - 1);  // highest m with an imaging term
-  if (m_top_img >= a.m_lo + 1) prefetch(m_top_img);
-
   // residuals of the receivers this thread injects (entries tid + h * kResThreads),
   // loaded one recording step ahead
   constexpr int kRecPerThread = (kResMaxRec + kResThreads - 1) / kResThreads;
@@ -512,15 +515,13 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     }
   };
   if (!DENSE && next_src >= a.m_lo + 1) load_g(next_src);
-
-  // Imaging sums: this thread's cells of one step in FP32 (acc), accumulated
-  // over steps as an unevaluated FP32 pair hi + lo (TwoSum, exact up to the
-  // pair's ~48-bit precision), converted to FP64 once per launch and reduced
-  // in FP64 across threads, CTAs and launches.
-  float acc[6], hi[6], lo[6];
-#pragma unroll
-  for (int t = 0; t < 6; ++t) { acc[t] = 0.f; hi[t] = 0.f; lo[t] = 0.f; }
-  double acc64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  // lam^{m_hi+1} is the imaging partner of u^{m_hi}: store it first
+  if (tid == 0 && a.lbuf && a.store_init) {
+    fence_proxy_async();
+    store_level(L0, a.lbuf + (size_t)(a.m_hi + 1 - a.slot_base) * a.state_stride + shot_off,
+                (ptrdiff_t)N);
+    bulk_commit();
+  }
   int last_level = 0;
   for (int m = a.m_hi; m >= a.m_lo + 1; --m) {
     const bool odd = ((a.m_hi - m) & 1) != 0;
@@ -528,8 +529,6 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     x.nxt = odd ? L0 : L1;  // lam^{m+2}, becomes lam^m
     last_level = odd ? 0 : 1;
     x.nxt_off = (int)(x.nxt - smem);
-    const bool img = (m <= c.nt - 1);
-    if (img && m - 1 >= a.m_lo + 1) prefetch(m - 1);
     const bool src_step = ((m - 1) % c.stride) == 0;
     const int frame = (m - 1) / c.stride;
     if (!DENSE && src_step) {
@@ -548,11 +547,6 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       if (next_src >= a.m_lo + 1) load_g(next_src);
       __syncthreads();
     }
-    const float* U = (m & 1) ? U1 : U0;
-    if (img) {
-      mbar_wait_bounded(&mbar[m & 1], phase[m & 1], c.err);
-      phase[m & 1] ^= 1u;
-    }
     const float* gxr = nullptr;
     const float* gyr = nullptr;
     if (DENSE && src_step) {
@@ -560,26 +554,20 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       gyr = a.g_y + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
     }
     for (int it = tid; it < nitems; it += kResThreads) {
-      const int qc = it % ncq, g = it / ncq;
-      if (4 * g + 4 <= rows)
-        adj_item<true, DENSE>(T, ks, x, U, img, gxr, gyr, gs, 4 * g, 4 * qc, acc);
-      else
-        adj_item<false, DENSE>(T, ks, x, U, img, gxr, gyr, gs, 4 * g, 4 * qc, acc);
+      const int qc = it % ncq, gq = it / ncq;
+      if (4 * gq + 4 <= rows) lam_item<true, DENSE>(T, ks, x, gxr, gyr, gs, 4 * gq, 4 * qc);
+      else lam_item<false, DENSE>(T, ks, x, gxr, gyr, gs, 4 * gq, 4 * qc);
     }
-    if (img) {
-#pragma unroll
-      for (int t = 0; t < 6; ++t) {  // TwoSum(hi, acc) -> (hi, lo)
-        const float sum = hi[t] + acc[t];
-        const float bp = sum - hi[t];
-        lo[t] += (hi[t] - (sum - bp)) + (acc[t] - bp);
-        hi[t] = sum;
-        acc[t] = 0.f;
-      }
-    }
+    if (tid == 0) bulk_wait_read_all();
     cluster.sync();
+    if (tid == 0 && a.lbuf && m - a.slot_base >= 0) {
+      fence_proxy_async();
+      store_level(x.nxt, a.lbuf + (size_t)(m - a.slot_base) * a.state_stride + shot_off,
+                  (ptrdiff_t)N);
+      bulk_commit();
+    }
   }
-#pragma unroll
-  for (int t = 0; t < 6; ++t) acc64[t] = (double)hi[t] + (double)lo[t];
+  if (tid == 0) bulk_wait_all();
 
   // lam^{m_lo+1} (last written level) and lam^{m_lo+2} -> lam_save
   if (a.m_hi >= a.m_lo + 1) {
@@ -589,34 +577,18 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       const int comp = e / (rows * ny);
       const int rem = e - comp * rows * ny;
       const int lr = rem / ny, j = rem - lr * ny;
-      const size_t g = shot_off + (size_t)comp * N + (size_t)(r0 + lr) * ny + j;
-      a.lam_save[g] = T.comp(last, comp)[T.at(lr + 1, j)];
-      a.lam_save[a.save_stride + g] = T.comp(before, comp)[T.at(lr + 1, j)];
+      const size_t gidx = shot_off + (size_t)comp * N + (size_t)(r0 + lr) * ny + j;
+      a.lam_save[gidx] = T.comp(last, comp)[T.at(lr + 1, j)];
+      a.lam_save[a.save_stride + gidx] = T.comp(before, comp)[T.at(lr + 1, j)];
     }
-  }
-  // FP64 block reduction of the imaging sums, once per launch
-  __shared__ double red[kResThreads / 32][6];
-  const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-  for (int t = 0; t < 6; ++t) {
-    double v = acc64[t];
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (lane == 0) red[warp][t] = v;
-  }
-  __syncthreads();
-  if (tid < 6) {
-    double v = 0.0;
-    for (int w = 0; w < kResThreads / 32; ++w) v += red[w][tid];
-    a.partials[((size_t)shot * CL + rank) * 8 + tid] += v;
   }
 }
 
 // ---------------------------------------------------------------- host side
-size_t resident_smem_bytes(const ResCommon& c, bool with_adjoint) {
+size_t resident_smem_bytes(const ResCommon& c) {
   const size_t level = 2 * (size_t)(c.R + 2) * c.ny * sizeof(float);
-  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 2 * sizeof(uint64_t) + 16;
-  const size_t fwd = 2 * level + (size_t)c.R * c.ny * sizeof(float);
-  return (with_adjoint ? 4 * level : fwd) + tail;
+  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 16;
+  return 2 * level + (size_t)c.R * c.ny * sizeof(float) + tail;
 }
 
 static cudaError_t configure(const void* fn, size_t smem) {
@@ -625,18 +597,39 @@ static cudaError_t configure(const void* fn, size_t smem) {
   return cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 }
 
+static int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 1;
+  }
+  return n;
+}
+
+int resident_img_clusters(const ResCommon& c) {
+  // IMG clusters per shot row of the grid: fill the SMs the FWD and LAM
+  // clusters leave free, at least one, at most eight
+  const int free_sm = sm_count() - 2 * c.S * c.CL;
+  int z = free_sm / (c.CL * c.S);
+  if (z < 1) z = 1;
+  if (z > 8) z = 8;
+  return z;
+}
+
 bool resident_feasible(const ResCommon& c, bool dense) {
   if (c.CL < 1 || c.CL > 16 || c.ny % 4 != 0 || c.nrec > kResMaxRec) return false;
   if ((c.CL - 1) * c.R >= c.nx) return false;  // every CTA owns >= 1 row
-  const size_t smem = resident_smem_bytes(c, true);
-  if (smem > 227 * 1024) return false;
+  const size_t smem = resident_smem_bytes(c);
+  if (smem > 220 * 1024) return false;
   const void* fn = dense ? (const void*)resident_kernel<true> : (const void*)resident_kernel<false>;
   if (configure(fn, smem) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(c.CL, 1, 2);
+  cfg.gridDim = dim3(c.CL, 1, 1);
   cfg.blockDim = dim3(kResThreads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cudaLaunchAttribute attr[1];
@@ -654,15 +647,24 @@ bool resident_feasible(const ResCommon& c, bool dense) {
   return clusters >= 1;
 }
 
-cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResAdj& a, bool run_fwd,
-                            bool run_adj, bool dense, cudaStream_t st) {
-  if (!run_fwd && !run_adj) return cudaSuccess;
-  const size_t smem = resident_smem_bytes(c, run_adj);
+cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResLam& a, const ResImg& g,
+                            bool run_fwd, bool run_lam, bool run_img, bool dense, cudaStream_t st) {
+  if (!run_fwd && !run_lam && !run_img) return cudaSuccess;
+  const size_t smem = resident_smem_bytes(c);
   const void* fn = dense ? (const void*)resident_kernel<true> : (const void*)resident_kernel<false>;
-  cudaError_t e = configure(fn, resident_smem_bytes(c, true));
+  cudaError_t e = configure(fn, smem);
   if (e != cudaSuccess) return e;
+  ResRoles roles{-1, -1, -1, 0};
+  int z = 0;
+  if (run_lam) roles.z_lam = z++;
+  if (run_fwd) roles.z_fwd = z++;
+  if (run_img) {
+    roles.z_img = z;
+    roles.n_img_z = resident_img_clusters(c);
+    z += roles.n_img_z;
+  }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(c.CL, c.S, (run_fwd && run_adj) ? 2 : 1);
+  cfg.gridDim = dim3(c.CL, c.S, z);
   cfg.blockDim = dim3(kResThreads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
@@ -673,15 +675,15 @@ cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResAdj& a
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  // blockIdx.z == fwd_z runs the forward role
-  const int fwd_z = run_fwd ? (run_adj ? 1 : 0) : -1;
-  const int cls = run_adj ? kProfAdjoint : kProfForward;
+  const int cls = (run_lam || run_img) ? kProfAdjoint : kProfForward;
   const double cells = (double)c.S * c.nx * c.ny;
-  const double bytes = cells * ((run_fwd ? alg_bytes_forward(kModeScalar) * (f.i1 - f.i0) : 0.0) +
-                                (run_adj ? alg_bytes_adjoint(kModeScalar) * (a.m_hi - a.m_lo) : 0.0));
+  const double bytes =
+      cells * ((run_fwd ? alg_bytes_forward(kModeScalar) * (f.i1 - f.i0) : 0.0) +
+               (run_lam ? 24.0 * (a.m_hi - a.m_lo) : 0.0) +   // lam recursion: 3 x 8 B
+               (run_img ? 16.0 * (g.n_hi - g.n_lo + 1) : 0.0));  // imaging: read lam, u
   return tracked_launch(cls, st, [&] {
-    if (dense) cudaLaunchKernelEx(&cfg, resident_kernel<true>, c, f, a, fwd_z);
-    else cudaLaunchKernelEx(&cfg, resident_kernel<false>, c, f, a, fwd_z);
+    if (dense) cudaLaunchKernelEx(&cfg, resident_kernel<true>, c, f, a, g, roles);
+    else cudaLaunchKernelEx(&cfg, resident_kernel<false>, c, f, a, g, roles);
   }, bytes);
 }
 

@@ -40,23 +40,39 @@ struct ResFwd {
   float* tr_y;
 };
 
-// Adjoint role: m = m_hi down to m_lo + 1, imaging against u^m.
-struct ResAdj {
+// LAM role: m = m_hi down to m_lo + 1 of the adjoint recursion.
+struct ResLam {
   int m_hi, m_lo;
-  const float* u_states;   // u^m at u_states + (m - u_base) * state_stride
-  int u_base;
-  size_t state_stride;
   float* lam_save;         // level 0: lam^{m+1}, level 1: lam^{m+2} (in and out)
   size_t save_stride;      // floats between the two levels
   int first;               // 1: start from lam = 0
   const float* g_x;
   const float* g_y;
-  double* partials;        // [S][CL][8]
+  float* lbuf;             // lam^m -> lbuf + (m - slot_base) * state_stride (slots >= 0), or nullptr
+  int slot_base;
+  int store_init;          // also store lam^{m_hi+1} into slot m_hi + 1 - slot_base
+  size_t state_stride;
 };
 
-size_t resident_smem_bytes(const ResCommon& c, bool with_adjoint);
+// IMG role: imaging pairs (lam^{n+1}, u^n) for n = n_lo .. n_hi, slot n - n_lo.
+struct ResImg {
+  int n_lo, n_hi;
+  const float* lbuf;
+  const float* ubuf;
+  size_t state_stride;
+  double* partials;        // [IMG CTAs][8]
+};
+
+// blockIdx.z of each role (-1: absent); IMG occupies n_img_z planes from z_img.
+struct ResRoles {
+  int z_fwd, z_lam, z_img, n_img_z;
+};
+
+size_t resident_smem_bytes(const ResCommon& c);
 bool resident_feasible(const ResCommon& c, bool dense);
-cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResAdj& a, bool run_fwd,
-                            bool run_adj, bool dense, cudaStream_t st);
+// IMG clusters along z for one launch (total IMG CTAs = this x S x CL)
+int resident_img_clusters(const ResCommon& c);
+cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResLam& a, const ResImg& g,
+                            bool run_fwd, bool run_lam, bool run_img, bool dense, cudaStream_t st);
 
 }  // namespace ernn

@@ -76,8 +76,9 @@ def test_workspace_sizes_follow_checkpoint_plan():
     assert lib.ernn_tape_bytes(ctypes.byref(p), 1) == 256 + 2 * align(state) + 100 * align(state)
     s_seg = lib.ernn_adjoint_scratch_bytes(ctypes.byref(_problem(ckpt_k=10)))
     s_all = lib.ernn_adjoint_scratch_bytes(ctypes.byref(_problem(ckpt_k=100)))
-    # two recompute segments (the resident path overlaps recompute and adjoint)
-    assert s_seg - s_all == 2 * 10 * align(state)
+    # segmented: two recompute segments and two lam segments of k = 10 states;
+    # store-all: no recompute segments, two lam segments of min(nt, 128) = 100
+    assert s_seg - s_all == (2 * 10 + 2 * 10 - 2 * 100) * align(state)
     assert lib.ernn_tape_bytes(ctypes.byref(_problem(nx=0)), 1) == 0
 
 
