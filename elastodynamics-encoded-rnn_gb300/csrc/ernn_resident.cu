@@ -41,6 +41,64 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the halo rows the neighbours store into this CTA: gives
+// up after ~2^31 cycles (about a second), records ERNN_ERR_TIMEOUT in *err,
+// and from then on every later wait of the launch returns at once, so the
+// kernel still ends (with the error recorded) instead of spinning.
+__device__ __forceinline__ void halo_wait(uint64_t* bar, uint32_t parity, int* err) {
+  if (mbar_try_wait_cluster(bar, parity)) return;
+  if (*(volatile int*)err != 0) return;
+  const long long t0 = clock64();
+  while (!mbar_try_wait_cluster(bar, parity)) {
+    if (clock64() - t0 > (1ll << 31)) {
+      atomicExch(err, 5 /* ERNN_ERR_TIMEOUT */);
+      return;
+    }
+  }
+}
+
+// shared::cluster address of the same shared-memory offset in CTA `rank`
+__device__ __forceinline__ uint32_t map_rank(uint32_t local, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+  return r;
+}
+
+// 16-byte store into another CTA's shared memory, completing 16 bytes of
+// transaction count on that CTA's mbarrier
+__device__ __forceinline__ void st_async16(uint32_t addr, const float4& v, uint32_t bar) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+          addr),
+      "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(bar)
+      : "memory");
+}
+
 // 1D bulk copy shared (this CTA) -> global in the current bulk group.
 __device__ __forceinline__ void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
   asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
@@ -118,124 +176,132 @@ __device__ __forceinline__ float at4(const float4& v, int q) {
   return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w;
 }
 
-// Per-step context of one CTA.
+// Per-step context of one CTA.  Levels form a ring of three: cur (read with
+// its halo), prev (the level before, own rows), nxt (written).
 struct StepCtx {
-  const float* cur;   // level read with its halo (u^n or lam^{m+1})
-  float* nxt;         // level holding the previous value, overwritten by the new one
-  int nxt_off;        // nxt - smem (for DSMEM pushes)
-  float* up_nb;       // smem of CTA rank-1 (generic address) or nullptr
-  float* dn_nb;       // smem of CTA rank+1 or nullptr
+  const float* cur;
+  const float* prev;
+  float* nxt;
+  uint32_t nxt_off_b;   // byte offset of nxt from the shared-memory base
+  uint32_t up_base;     // shared::cluster address of the base in CTA rank-1 (0: none)
+  uint32_t dn_base;     // ... in CTA rank+1 (0: none)
+  uint32_t up_bar;      // shared::cluster address of the nxt-level mbarrier in rank-1
+  uint32_t dn_bar;
   int rows, R, ny;
 };
 
-// Forward: one 4-row x 4-column item starting at local row lr0, column j.
-template <bool FULL>
-__device__ __forceinline__ void fwd_item(const Tile& T, const KSr& ks, const StepCtx& x,
-                                         const float* __restrict__ F, float amp, int src_comp,
-                                         int lr0, int j) {
+// Inputs of the right-hand side: FWD adds amp * F (one component), LAM adds
+// gs * g at recording steps of the dense history.
+struct Rhs {
+  const float* F;
+  float amp;
+  int src_comp;
+  const float* gx;
+  const float* gy;
+  float gs;
+};
+
+// One row lr (local) of one column quad j: windows w[0..1] hold halo rows
+// lr, lr+1 on entry; loads halo row lr+2, computes, stores, pushes boundary
+// rows to the neighbours, shifts the windows.
+template <bool LAM, bool DENSE>
+__device__ __forceinline__ void row_step(const Tile& T, const KSr& ks, const StepCtx& x,
+                                         const Rhs& rhs, int lr, int j, float wx[3][6],
+                                         float wy[3][6]) {
   const int ny = x.ny;
-  float wx[3][6], wy[3][6];
-  load_row6(T.comp(const_cast<float*>(x.cur), 0) + T.at(lr0, 0), j, ny, wx[0]);
-  load_row6(T.comp(const_cast<float*>(x.cur), 1) + T.at(lr0, 0), j, ny, wy[0]);
-  load_row6(T.comp(const_cast<float*>(x.cur), 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
-  load_row6(T.comp(const_cast<float*>(x.cur), 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
+  const int s = lr + 1;
+  float* cur = const_cast<float*>(x.cur);
+  load_row6(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
+  load_row6(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
+  Quad st;
+  quad_stencils(wx, wy, st);
+  const float4 pvx = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(x.prev), 0) + T.at(s, j));
+  const float4 pvy = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(x.prev), 1) + T.at(s, j));
+  float vx[4], vy[4];
 #pragma unroll
-  for (int q4 = 0; q4 < 4; ++q4) {
-    const int lr = lr0 + q4;
-    if (!FULL && lr >= x.rows) break;
-    const int s = lr + 1;
-    load_row6(T.comp(const_cast<float*>(x.cur), 0) + T.at(s + 1, 0), j, ny, wx[2]);
-    load_row6(T.comp(const_cast<float*>(x.cur), 1) + T.at(s + 1, 0), j, ny, wy[2]);
-    Quad st;
-    quad_stencils(wx, wy, st);
-    float4* px = reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j));
-    float4* py = reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j));
-    const float4 pvx = *px, pvy = *py;
-    const float4 fl = *reinterpret_cast<const float4*>(F + lr * ny + j);
-    float vx[4], vy[4];
+  for (int q = 0; q < 4; ++q) {
+    float lx, ly;
+    lq(ks, st, q, lx, ly);
+    vx[q] = (2.f * st.cx[q] - at4(pvx, q)) + lx;
+    vy[q] = (2.f * st.cy[q] - at4(pvy, q)) + ly;
+  }
+  if (!LAM) {
+    const float4 fl = *reinterpret_cast<const float4*>(rhs.F + lr * ny + j);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      float lx, ly;
-      lq(ks, st, q, lx, ly);
-      vx[q] = (2.f * st.cx[q] - at4(pvx, q)) + lx;
-      vy[q] = (2.f * st.cy[q] - at4(pvy, q)) + ly;
-      const float fz = amp * at4(fl, q);
-      if (src_comp == 0) vx[q] += fz; else vy[q] += fz;
+      const float fz = rhs.amp * at4(fl, q);
+      if (rhs.src_comp == 0) vx[q] += fz; else vy[q] += fz;
     }
-    const float4 nvx = f4(vx), nvy = f4(vy);
-    *px = nvx;
-    *py = nvy;
-    if (lr == 0 && x.up_nb) {
-      const int o = x.nxt_off + T.at(x.R + 1, j);
-      *reinterpret_cast<float4*>(x.up_nb + o) = nvx;
-      *reinterpret_cast<float4*>(x.up_nb + o + T.plane) = nvy;
+  } else if (DENSE && rhs.gx != nullptr) {
+    const float4 a4 = *reinterpret_cast<const float4*>(rhs.gx + (size_t)lr * ny + j);
+    const float4 b4 = *reinterpret_cast<const float4*>(rhs.gy + (size_t)lr * ny + j);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      vx[q] += rhs.gs * at4(a4, q);
+      vy[q] += rhs.gs * at4(b4, q);
     }
-    if (lr == x.rows - 1 && x.dn_nb) {
-      const int o = x.nxt_off + T.at(0, j);
-      *reinterpret_cast<float4*>(x.dn_nb + o) = nvx;
-      *reinterpret_cast<float4*>(x.dn_nb + o + T.plane) = nvy;
-    }
-    shift6(wx);
-    shift6(wy);
   }
+  const float4 nvx = f4(vx), nvy = f4(vy);
+  *reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j)) = nvx;
+  *reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j)) = nvy;
+  if (lr == 0 && x.up_base) {  // into rank-1's bottom halo row
+    const uint32_t o = x.nxt_off_b + 4u * (uint32_t)T.at(x.R + 1, j);
+    st_async16(x.up_base + o, nvx, x.up_bar);
+    st_async16(x.up_base + o + 4u * (uint32_t)T.plane, nvy, x.up_bar);
+  }
+  if (lr == x.rows - 1 && x.dn_base) {  // into rank+1's top halo row
+    const uint32_t o = x.nxt_off_b + 4u * (uint32_t)T.at(0, j);
+    st_async16(x.dn_base + o, nvx, x.dn_bar);
+    st_async16(x.dn_base + o + 4u * (uint32_t)T.plane, nvy, x.dn_bar);
+  }
+  shift6(wx);
+  shift6(wy);
 }
 
-// Adjoint: one 4 x 4 item, lam^m into nxt.
-template <bool FULL, bool DENSE>
-__device__ __forceinline__ void lam_item(const Tile& T, const KSr& ks, const StepCtx& x,
-                                         const float* gx, const float* gy, float gs, int lr0,
-                                         int j) {
-  const int ny = x.ny;
+// Rows [a, b) of column quad j (interior rows only touch own rows of cur).
+template <bool LAM, bool DENSE>
+__device__ __forceinline__ void rows_step(const Tile& T, const KSr& ks, const StepCtx& x,
+                                          const Rhs& rhs, int a, int b, int j) {
+  if (a >= b) return;
   float wx[3][6], wy[3][6];
   float* cur = const_cast<float*>(x.cur);
-  load_row6(T.comp(cur, 0) + T.at(lr0, 0), j, ny, wx[0]);
-  load_row6(T.comp(cur, 1) + T.at(lr0, 0), j, ny, wy[0]);
-  load_row6(T.comp(cur, 0) + T.at(lr0 + 1, 0), j, ny, wx[1]);
-  load_row6(T.comp(cur, 1) + T.at(lr0 + 1, 0), j, ny, wy[1]);
+  load_row6(T.comp(cur, 0) + T.at(a, 0), j, x.ny, wx[0]);
+  load_row6(T.comp(cur, 1) + T.at(a, 0), j, x.ny, wy[0]);
+  load_row6(T.comp(cur, 0) + T.at(a + 1, 0), j, x.ny, wx[1]);
+  load_row6(T.comp(cur, 1) + T.at(a + 1, 0), j, x.ny, wy[1]);
+  int lr = a;
+  for (; lr + 4 <= b; lr += 4) {
 #pragma unroll
-  for (int q4 = 0; q4 < 4; ++q4) {
-    const int lr = lr0 + q4;
-    if (!FULL && lr >= x.rows) break;
-    const int s = lr + 1;
-    load_row6(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
-    load_row6(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
-    Quad st;
-    quad_stencils(wx, wy, st);
-    float4* px = reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j));
-    float4* py = reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j));
-    const float4 pvx = *px, pvy = *py;
-    float vx[4], vy[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      float lx, ly;
-      lq(ks, st, q, lx, ly);
-      vx[q] = (2.f * st.cx[q] - at4(pvx, q)) + lx;
-      vy[q] = (2.f * st.cy[q] - at4(pvy, q)) + ly;
-    }
-    if (DENSE && gx != nullptr) {
-      const float4 a4 = *reinterpret_cast<const float4*>(gx + (size_t)lr * ny + j);
-      const float4 b4 = *reinterpret_cast<const float4*>(gy + (size_t)lr * ny + j);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        vx[q] += gs * at4(a4, q);
-        vy[q] += gs * at4(b4, q);
-      }
-    }
-    const float4 nvx = f4(vx), nvy = f4(vy);
-    *px = nvx;
-    *py = nvy;
-    if (lr == 0 && x.up_nb) {
-      const int o = x.nxt_off + T.at(x.R + 1, j);
-      *reinterpret_cast<float4*>(x.up_nb + o) = nvx;
-      *reinterpret_cast<float4*>(x.up_nb + o + T.plane) = nvy;
-    }
-    if (lr == x.rows - 1 && x.dn_nb) {
-      const int o = x.nxt_off + T.at(0, j);
-      *reinterpret_cast<float4*>(x.dn_nb + o) = nvx;
-      *reinterpret_cast<float4*>(x.dn_nb + o + T.plane) = nvy;
-    }
-    shift6(wx);
-    shift6(wy);
+    for (int q = 0; q < 4; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, lr + q, j, wx, wy);
+  }
+  for (; lr < b; ++lr) row_step<LAM, DENSE>(T, ks, x, rhs, lr, j, wx, wy);
+}
+
+// One step of the ring: interior rows first (no halo needed), then wait for
+// the neighbours' boundary rows of cur, then the two boundary rows (which
+// are pushed to the neighbours).  Work unit: (column quad, chunk of rows).
+template <bool LAM, bool DENSE>
+__device__ __forceinline__ void ring_step(const Tile& T, const KSr& ks, const StepCtx& x,
+                                          const Rhs& rhs, uint64_t* cur_bar, uint32_t parity,
+                                          bool wait, int* err) {
+  const int ncq = x.ny / 4;
+  const int nchunk = max(1, kResThreads / ncq);
+  const int rc = (x.rows + nchunk - 1) / nchunk;
+  const int items = ncq * nchunk;
+  const int last = x.rows - 1;
+  for (int it = threadIdx.x; it < items; it += kResThreads) {
+    const int qc = it % ncq, ch = it / ncq;
+    const int ra = ch * rc, rb = min(ra + rc, x.rows);
+    rows_step<LAM, DENSE>(T, ks, x, rhs, max(ra, 1), min(rb, last), 4 * qc);
+  }
+  if (wait) halo_wait(cur_bar, parity, err);
+  __syncwarp();
+  for (int it = threadIdx.x; it < items; it += kResThreads) {
+    const int qc = it % ncq, ch = it / ncq;
+    const int ra = ch * rc, rb = min(ra + rc, x.rows);
+    if (ra >= rb) continue;
+    if (ra == 0) rows_step<LAM, DENSE>(T, ks, x, rhs, 0, 1, 4 * qc);
+    if (rb == x.rows && last > 0) rows_step<LAM, DENSE>(T, ks, x, rhs, last, last + 1, 4 * qc);
   }
 }
 
@@ -362,11 +428,11 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   Tile T{R, ny, rows, (R + 2) * ny};
   const int level_floats = 2 * T.plane;
 
-  float* L0 = smem;
-  float* L1 = smem + level_floats;
-  float* F = smem + 2 * level_floats;   // forward role: source load of the own rows [R][ny]
+  float* L[3] = {smem, smem + level_floats, smem + 2 * level_floats};  // ring of levels
+  float* F = smem + 3 * level_floats;   // FWD role: source load of the own rows [R][ny]
   int* rec_list = reinterpret_cast<int*>(F + R * ny);  // [kResMaxRec][2]
   int* rec_count = rec_list + 2 * kResMaxRec;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(rec_count + 4);  // [3], 8-byte aligned
 
   const KSr ks{c.coef->k11, c.coef->k22, c.coef->kq12, c.coef->k16,
                c.coef->k26, c.coef->k66, c.coef->k16h, c.coef->k26h};
@@ -374,8 +440,12 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   const size_t shot_off = (size_t)shot * 2 * N;
 
   // -------- initial state: zero the levels and the load, then load
-  for (int e = tid; e < 2 * level_floats + R * ny; e += kResThreads) smem[e] = 0.f;
-  if (tid == 0) *rec_count = 0;
+  for (int e = tid; e < 3 * level_floats + R * ny; e += kResThreads) smem[e] = 0.f;
+  if (tid == 0) {
+    *rec_count = 0;
+    for (int l = 0; l < 3; ++l) mbar_init(&bar[l], 1);
+    fence_mbar_init();
+  }
   __syncthreads();
   if (is_fwd && c.bx > 0 && c.by > 0) {
     // the shot's load restricted to the own rows, kept in shared memory so the
@@ -405,7 +475,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   }
   const float* init_cur = is_fwd ? f.init_cur : (a.first ? nullptr : a.lam_save);
   const float* init_prev = is_fwd ? f.init_prev : (a.first ? nullptr : a.lam_save + a.save_stride);
-  // current level with halo rows, previous level own rows
+  // step 0 reads L[0] (with halo rows, from global memory) and L[2] (own rows)
   for (int e = tid; e < 2 * (rows + 2) * ny; e += kResThreads) {
     const int comp = e / ((rows + 2) * ny);
     const int rem = e - comp * (rows + 2) * ny;
@@ -413,50 +483,66 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     const int gi = r0 + s - 1;
     if (gi < 0 || gi >= nx) continue;
     const size_t gidx = shot_off + (size_t)comp * N + (size_t)gi * ny + j;
-    if (init_cur) T.comp(L0, comp)[T.at(s, j)] = init_cur[gidx];
-    if (init_prev && s >= 1 && s <= rows) T.comp(L1, comp)[T.at(s, j)] = init_prev[gidx];
+    if (init_cur) T.comp(L[0], comp)[T.at(s, j)] = init_cur[gidx];
+    if (init_prev && s >= 1 && s <= rows) T.comp(L[2], comp)[T.at(s, j)] = init_prev[gidx];
   }
   __syncthreads();
-  cluster.sync();  // every CTA initialised before any DSMEM push
+  cluster.sync();  // every CTA initialised (levels, mbarriers) before any push
 
   const int nloc = min(*rec_count, kResMaxRec);
-  const int ncq = ny / 4;                      // column quads
-  const int ngr = (rows + 3) / 4;              // row groups of 4
-  const int nitems = ncq * ngr;
+  const bool has_up = rank > 0, has_dn = rank < CL - 1;
+  // bytes each ring step receives: both components of one row per neighbour
+  const uint32_t halo_bytes = (uint32_t)((has_up ? 1 : 0) + (has_dn ? 1 : 0)) * 2u * (uint32_t)ny * 4u;
+  const uint32_t base_b = smem_u32(smem);
   StepCtx x;
-  x.up_nb = (rank > 0) ? cluster.map_shared_rank(smem, rank - 1) : nullptr;
-  x.dn_nb = (rank < CL - 1) ? cluster.map_shared_rank(smem, rank + 1) : nullptr;
+  x.up_base = has_up ? map_rank(base_b, rank - 1) : 0u;
+  x.dn_base = has_dn ? map_rank(base_b, rank + 1) : 0u;
   x.rows = rows;
   x.R = R;
   x.ny = ny;
+  uint32_t parity[3] = {0u, 0u, 0u};
+  auto set_levels = [&](int t) {
+    x.cur = L[t % 3];
+    x.prev = L[(t + 2) % 3];
+    x.nxt = L[(t + 1) % 3];
+    x.nxt_off_b = (uint32_t)((t + 1) % 3) * (uint32_t)level_floats * 4u;
+    const uint32_t lbar = smem_u32(&bar[(t + 1) % 3]);
+    x.up_bar = has_up ? map_rank(lbar, rank - 1) : 0u;
+    x.dn_bar = has_dn ? map_rank(lbar, rank + 1) : 0u;
+  };
+  // this step's wait: the neighbours pushed cur's halo during their step t-1
+  auto step_wait = [&](int t) -> bool { return t >= 1 && halo_bytes > 0; };
+  auto expect_next = [&](int t) {  // halo of nxt arrives during the neighbours' step t
+    if (tid == 0 && halo_bytes > 0) mbar_arrive_expect_tx(&bar[(t + 1) % 3], halo_bytes);
+  };
   const uint32_t own_bytes = (uint32_t)((size_t)rows * ny * sizeof(float));
-  // own rows of a level -> global state at dst (x plane, y plane at +N)
+  // own rows of a level -> global state at dst (x plane, y plane at y_off)
   auto store_level = [&](const float* level, float* dst, ptrdiff_t y_off) {
     bulk_s2g(dst + (size_t)r0 * ny, T.comp(const_cast<float*>(level), 0) + T.at(1, 0), own_bytes);
     bulk_s2g(dst + y_off + (size_t)r0 * ny, T.comp(const_cast<float*>(level), 1) + T.at(1, 0),
              own_bytes);
   };
+  int t_last = -1;
 
   if (is_fwd) {
     // ================================================================ FWD role
     const float* sig = c.src_signal + (size_t)shot * c.nt;
     float amp_next = (f.i0 < f.i1) ? sig[f.i0] : 0.f;
+    Rhs rhs{F, 0.f, c.src_comp, nullptr, nullptr, 0.f};
     for (int i = f.i0; i < f.i1; ++i) {
-      const bool odd = ((i - f.i0) & 1) != 0;
-      x.cur = odd ? L1 : L0;
-      x.nxt = odd ? L0 : L1;
-      x.nxt_off = (int)(x.nxt - smem);
-      const float amp = amp_next * kappa;
+      const int t = i - f.i0;
+      set_levels(t);
+      expect_next(t);
+      rhs.amp = amp_next * kappa;
       amp_next = (i + 1 < f.i1) ? sig[i + 1] : 0.f;  // in flight during this step
-      for (int it = tid; it < nitems; it += kResThreads) {
-        const int qc = it % ncq, gq = it / ncq;
-        if (4 * gq + 4 <= rows) fwd_item<true>(T, ks, x, F, amp, c.src_comp, 4 * gq, 4 * qc);
-        else fwd_item<false>(T, ks, x, F, amp, c.src_comp, 4 * gq, 4 * qc);
-      }
-      // the bulk stores issued after the previous barrier read the level this
-      // CTA overwrites next step: make sure they are done reading
+      const bool w = step_wait(t);
+      ring_step<false, false>(T, ks, x, rhs, &bar[t % 3], parity[t % 3], w, c.err);
+      if (w) parity[t % 3] ^= 1u;
+      // bulk stores issued after the previous step read a level overwritten two
+      // steps from now: make sure they are done reading before the barrier
       if (tid == 0) bulk_wait_read_all();
-      cluster.sync();
+      __syncthreads();
+      t_last = t;
       // u^{i+1} (own rows of nxt) to global memory through the bulk-copy engine
       float* dst[4] = {nullptr, nullptr, nullptr, nullptr};
       ptrdiff_t dst_y[4] = {(ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N};  // y plane offset
@@ -489,90 +575,88 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
         }
       }
     }
-    if (tid == 0) bulk_wait_all();
-    return;
-  }
-
-  // ================================================================== LAM role
-  const float gs = c.coef->gscale;
-  // residuals of the receivers this thread injects (entries tid + h * kResThreads),
-  // loaded one recording step ahead
-  constexpr int kRecPerThread = (kResMaxRec + kResThreads - 1) / kResThreads;
-  float gnx[kRecPerThread], gny[kRecPerThread];
+  } else {
+    // ================================================================ LAM role
+    const float gs = c.coef->gscale;
+    // residuals of the receivers this thread injects (entries tid + h * kResThreads),
+    // loaded one recording step ahead
+    constexpr int kRecPerThread = (kResMaxRec + kResThreads - 1) / kResThreads;
+    float gnx[kRecPerThread], gny[kRecPerThread];
 #pragma unroll
-  for (int h = 0; h < kRecPerThread; ++h) { gnx[h] = 0.f; gny[h] = 0.f; }
-  int next_src = a.m_hi - ((a.m_hi - 1) % c.stride);  // highest m <= m_hi with a frame
-  auto load_g = [&](int m) {
-    const int frame = (m - 1) / c.stride;
-#pragma unroll
-    for (int h = 0; h < kRecPerThread; ++h) {
-      const int e = tid + h * kResThreads;
-      if (e < nloc) {
-        const size_t go = ((size_t)shot * c.nt_out + frame) * c.nrec + rec_list[2 * e + 1];
-        gnx[h] = a.g_x[go];
-        gny[h] = a.g_y[go];
-      }
-    }
-  };
-  if (!DENSE && next_src >= a.m_lo + 1) load_g(next_src);
-  // lam^{m_hi+1} is the imaging partner of u^{m_hi}: store it first
-  if (tid == 0 && a.lbuf && a.store_init) {
-    fence_proxy_async();
-    store_level(L0, a.lbuf + (size_t)(a.m_hi + 1 - a.slot_base) * a.state_stride + shot_off,
-                (ptrdiff_t)N);
-    bulk_commit();
-  }
-  int last_level = 0;
-  for (int m = a.m_hi; m >= a.m_lo + 1; --m) {
-    const bool odd = ((a.m_hi - m) & 1) != 0;
-    x.cur = odd ? L1 : L0;  // lam^{m+1}
-    x.nxt = odd ? L0 : L1;  // lam^{m+2}, becomes lam^m
-    last_level = odd ? 0 : 1;
-    x.nxt_off = (int)(x.nxt - smem);
-    const bool src_step = ((m - 1) % c.stride) == 0;
-    const int frame = (m - 1) / c.stride;
-    if (!DENSE && src_step) {
-      // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: subtract g from the own
-      // copy of lam^{m+2}, which only the owning thread reads this step
+    for (int h = 0; h < kRecPerThread; ++h) { gnx[h] = 0.f; gny[h] = 0.f; }
+    int next_src = a.m_hi - ((a.m_hi - 1) % c.stride);  // highest m <= m_hi with a frame
+    auto load_g = [&](int m) {
+      const int frame = (m - 1) / c.stride;
 #pragma unroll
       for (int h = 0; h < kRecPerThread; ++h) {
         const int e = tid + h * kResThreads;
         if (e < nloc) {
-          const int off = rec_list[2 * e];
-          atomicAdd(&T.comp(x.nxt, 0)[off], -gs * gnx[h]);
-          atomicAdd(&T.comp(x.nxt, 1)[off], -gs * gny[h]);
+          const size_t go = ((size_t)shot * c.nt_out + frame) * c.nrec + rec_list[2 * e + 1];
+          gnx[h] = a.g_x[go];
+          gny[h] = a.g_y[go];
         }
       }
-      next_src = m - c.stride;
-      if (next_src >= a.m_lo + 1) load_g(next_src);
-      __syncthreads();
-    }
-    const float* gxr = nullptr;
-    const float* gyr = nullptr;
-    if (DENSE && src_step) {
-      gxr = a.g_x + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
-      gyr = a.g_y + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
-    }
-    for (int it = tid; it < nitems; it += kResThreads) {
-      const int qc = it % ncq, gq = it / ncq;
-      if (4 * gq + 4 <= rows) lam_item<true, DENSE>(T, ks, x, gxr, gyr, gs, 4 * gq, 4 * qc);
-      else lam_item<false, DENSE>(T, ks, x, gxr, gyr, gs, 4 * gq, 4 * qc);
-    }
-    if (tid == 0) bulk_wait_read_all();
-    cluster.sync();
-    if (tid == 0 && a.lbuf && m - a.slot_base >= 0) {
+    };
+    if (!DENSE && next_src >= a.m_lo + 1) load_g(next_src);
+    // lam^{m_hi+1} is the imaging partner of u^{m_hi}: store it first
+    if (tid == 0 && a.lbuf && a.store_init) {
       fence_proxy_async();
-      store_level(x.nxt, a.lbuf + (size_t)(m - a.slot_base) * a.state_stride + shot_off,
+      store_level(L[0], a.lbuf + (size_t)(a.m_hi + 1 - a.slot_base) * a.state_stride + shot_off,
                   (ptrdiff_t)N);
       bulk_commit();
     }
+    Rhs rhs{nullptr, 0.f, 0, nullptr, nullptr, gs};
+    for (int m = a.m_hi; m >= a.m_lo + 1; --m) {
+      const int t = a.m_hi - m;  // cur = lam^{m+1}, prev = lam^{m+2}, nxt = lam^m
+      set_levels(t);
+      expect_next(t);
+      const bool src_step = ((m - 1) % c.stride) == 0;
+      const int frame = (m - 1) / c.stride;
+      if (!DENSE && src_step) {
+        // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: subtract g from the own
+        // copy of lam^{m+2}, which only the owning thread reads this step
+#pragma unroll
+        for (int h = 0; h < kRecPerThread; ++h) {
+          const int e = tid + h * kResThreads;
+          if (e < nloc) {
+            const int off = rec_list[2 * e];
+            atomicAdd(&T.comp(const_cast<float*>(x.prev), 0)[off], -gs * gnx[h]);
+            atomicAdd(&T.comp(const_cast<float*>(x.prev), 1)[off], -gs * gny[h]);
+          }
+        }
+        next_src = m - c.stride;
+        if (next_src >= a.m_lo + 1) load_g(next_src);
+        __syncthreads();
+      }
+      rhs.gx = nullptr;
+      rhs.gy = nullptr;
+      if (DENSE && src_step) {
+        rhs.gx = a.g_x + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
+        rhs.gy = a.g_y + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
+      }
+      const bool w = step_wait(t);
+      ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], parity[t % 3], w, c.err);
+      if (w) parity[t % 3] ^= 1u;
+      if (tid == 0) bulk_wait_read_all();
+      __syncthreads();
+      t_last = t;
+      if (tid == 0 && a.lbuf && m - a.slot_base >= 0) {
+        fence_proxy_async();
+        store_level(x.nxt, a.lbuf + (size_t)(m - a.slot_base) * a.state_stride + shot_off,
+                    (ptrdiff_t)N);
+        bulk_commit();
+      }
+    }
   }
+  // The neighbours' last pushes land in this CTA's level of step t_last + 1:
+  // wait for them before this CTA's shared memory goes away.
+  if (t_last >= 0 && halo_bytes > 0) halo_wait(&bar[(t_last + 1) % 3], parity[(t_last + 1) % 3], c.err);
   if (tid == 0) bulk_wait_all();
-
-  // lam^{m_lo+1} (last written level) and lam^{m_lo+2} -> lam_save
-  if (a.m_hi >= a.m_lo + 1) {
-    float* last = last_level ? L1 : L0;
-    float* before = last_level ? L0 : L1;
+  __syncthreads();
+  if (!is_fwd && a.m_hi >= a.m_lo + 1) {
+    // lam^{m_lo+1} (level of step t_last + 1) and lam^{m_lo+2} -> lam_save
+    float* last = L[(t_last + 1) % 3];
+    float* before = L[t_last % 3];
     for (int e = tid; e < 2 * rows * ny; e += kResThreads) {
       const int comp = e / (rows * ny);
       const int rem = e - comp * rows * ny;
@@ -582,13 +666,14 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       a.lam_save[a.save_stride + gidx] = T.comp(before, comp)[T.at(lr + 1, j)];
     }
   }
+  cluster.sync();  // no CTA leaves while a neighbour may still address it
 }
 
 // ---------------------------------------------------------------- host side
 size_t resident_smem_bytes(const ResCommon& c) {
   const size_t level = 2 * (size_t)(c.R + 2) * c.ny * sizeof(float);
-  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 16;
-  return 2 * level + (size_t)c.R * c.ny * sizeof(float) + tail;
+  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 3 * sizeof(uint64_t) + 16;
+  return 3 * level + (size_t)c.R * c.ny * sizeof(float) + tail;
 }
 
 static cudaError_t configure(const void* fn, size_t smem) {
