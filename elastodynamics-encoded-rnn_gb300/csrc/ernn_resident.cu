@@ -258,28 +258,50 @@ __device__ __forceinline__ void row_step(const Tile& T, const KSr& ks, const Ste
   shift6(wy);
 }
 
-// Rows [a, b) of column quad j (interior rows only touch own rows of cur).
-template <bool LAM, bool DENSE>
-__device__ __forceinline__ void rows_step(const Tile& T, const KSr& ks, const StepCtx& x,
-                                          const Rhs& rhs, int a, int b, int j) {
-  if (a >= b) return;
-  float wx[3][6], wy[3][6];
+// Load the windows of halo rows s, s+1 (local rows s-1, s) of column quad j.
+__device__ __forceinline__ void load_windows(const Tile& T, const StepCtx& x, int s, int j,
+                                             float wx[3][6], float wy[3][6]) {
   float* cur = const_cast<float*>(x.cur);
-  load_row6(T.comp(cur, 0) + T.at(a, 0), j, x.ny, wx[0]);
-  load_row6(T.comp(cur, 1) + T.at(a, 0), j, x.ny, wy[0]);
-  load_row6(T.comp(cur, 0) + T.at(a + 1, 0), j, x.ny, wx[1]);
-  load_row6(T.comp(cur, 1) + T.at(a + 1, 0), j, x.ny, wy[1]);
-  int lr = a;
-  for (; lr + 4 <= b; lr += 4) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, lr + q, j, wx, wy);
-  }
-  for (; lr < b; ++lr) row_step<LAM, DENSE>(T, ks, x, rhs, lr, j, wx, wy);
+  load_row6(T.comp(cur, 0) + T.at(s, 0), j, x.ny, wx[0]);
+  load_row6(T.comp(cur, 1) + T.at(s, 0), j, x.ny, wy[0]);
+  load_row6(T.comp(cur, 0) + T.at(s + 1, 0), j, x.ny, wx[1]);
+  load_row6(T.comp(cur, 1) + T.at(s + 1, 0), j, x.ny, wy[1]);
 }
 
-// One step of the ring: interior rows first (no halo needed), then wait for
-// the neighbours' boundary rows of cur, then the two boundary rows (which
-// are pushed to the neighbours).  Work unit: (column quad, chunk of rows).
+// Rows a .. a+n-1 with windows already holding local rows a-1, a; on return
+// they hold rows a+n-1, a+n.  Counts up to 4 are unrolled (window shifts
+// become register renames).
+template <bool LAM, bool DENSE>
+__device__ __forceinline__ void rows_from(const Tile& T, const KSr& ks, const StepCtx& x,
+                                          const Rhs& rhs, int a, int n, int j, float wx[3][6],
+                                          float wy[3][6]) {
+  switch (n) {
+    case 0: return;
+    case 1:
+      row_step<LAM, DENSE>(T, ks, x, rhs, a, j, wx, wy);
+      return;
+    case 2:
+#pragma unroll
+      for (int q = 0; q < 2; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+      return;
+    case 3:
+#pragma unroll
+      for (int q = 0; q < 3; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+      return;
+    case 4:
+#pragma unroll
+      for (int q = 0; q < 4; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+      return;
+    default:
+      for (int q = 0; q < n; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+  }
+}
+
+// One step of the ring: interior rows first (they only read own rows of
+// cur), then wait for the neighbours' boundary rows of cur, then the two
+// boundary rows (pushed to the neighbours).  Work unit: (column quad, chunk
+// of consecutive rows); the chunk holding the last row keeps its windows
+// across the wait.
 template <bool LAM, bool DENSE>
 __device__ __forceinline__ void ring_step(const Tile& T, const KSr& ks, const StepCtx& x,
                                           const Rhs& rhs, uint64_t* cur_bar, uint32_t parity,
@@ -289,19 +311,55 @@ __device__ __forceinline__ void ring_step(const Tile& T, const KSr& ks, const St
   const int rc = (x.rows + nchunk - 1) / nchunk;
   const int items = ncq * nchunk;
   const int last = x.rows - 1;
+  if (items <= kResThreads) {
+    // one unit per thread: carry the windows over the wait
+    const int it = threadIdx.x;
+    const bool active = it < items;
+    const int qc = active ? it % ncq : 0, ch = active ? it / ncq : 0;
+    const int ra = ch * rc, rb = min(ra + rc, x.rows);
+    const int ia = max(ra, 1), ib = min(rb, last);
+    float wx[3][6], wy[3][6];
+    if (active && ia < ib) {
+      load_windows(T, x, ia, 4 * qc, wx, wy);
+      rows_from<LAM, DENSE>(T, ks, x, rhs, ia, ib - ia, 4 * qc, wx, wy);
+    }
+    if (wait) halo_wait(cur_bar, parity, err);
+    if (active && ra < rb) {
+      if (rb == x.rows && last > 0) {
+        if (!(ia < ib)) load_windows(T, x, last, 4 * qc, wx, wy);  // local rows last-1, last
+        rows_from<LAM, DENSE>(T, ks, x, rhs, last, 1, 4 * qc, wx, wy);
+      }
+      if (ra == 0) {
+        load_windows(T, x, 0, 4 * qc, wx, wy);  // halo row 0, local row 0
+        rows_from<LAM, DENSE>(T, ks, x, rhs, 0, 1, 4 * qc, wx, wy);
+      }
+    }
+    return;
+  }
   for (int it = threadIdx.x; it < items; it += kResThreads) {
     const int qc = it % ncq, ch = it / ncq;
     const int ra = ch * rc, rb = min(ra + rc, x.rows);
-    rows_step<LAM, DENSE>(T, ks, x, rhs, max(ra, 1), min(rb, last), 4 * qc);
+    const int ia = max(ra, 1), ib = min(rb, last);
+    if (ia < ib) {
+      float wx[3][6], wy[3][6];
+      load_windows(T, x, ia, 4 * qc, wx, wy);
+      rows_from<LAM, DENSE>(T, ks, x, rhs, ia, ib - ia, 4 * qc, wx, wy);
+    }
   }
   if (wait) halo_wait(cur_bar, parity, err);
-  __syncwarp();
   for (int it = threadIdx.x; it < items; it += kResThreads) {
     const int qc = it % ncq, ch = it / ncq;
     const int ra = ch * rc, rb = min(ra + rc, x.rows);
     if (ra >= rb) continue;
-    if (ra == 0) rows_step<LAM, DENSE>(T, ks, x, rhs, 0, 1, 4 * qc);
-    if (rb == x.rows && last > 0) rows_step<LAM, DENSE>(T, ks, x, rhs, last, last + 1, 4 * qc);
+    float wx[3][6], wy[3][6];
+    if (ra == 0) {
+      load_windows(T, x, 0, 4 * qc, wx, wy);
+      rows_from<LAM, DENSE>(T, ks, x, rhs, 0, 1, 4 * qc, wx, wy);
+    }
+    if (rb == x.rows && last > 0) {
+      load_windows(T, x, last, 4 * qc, wx, wy);
+      rows_from<LAM, DENSE>(T, ks, x, rhs, last, 1, 4 * qc, wx, wy);
+    }
   }
 }
 
@@ -428,7 +486,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   Tile T{R, ny, rows, (R + 2) * ny};
   const int level_floats = 2 * T.plane;
 
-  float* L[3] = {smem, smem + level_floats, smem + 2 * level_floats};  // ring of levels
+  // ring of three levels: level l starts at smem + l * level_floats
+  auto Lv = [&](int l) { return smem + l * level_floats; };
   float* F = smem + 3 * level_floats;   // FWD role: source load of the own rows [R][ny]
   int* rec_list = reinterpret_cast<int*>(F + R * ny);  // [kResMaxRec][2]
   int* rec_count = rec_list + 2 * kResMaxRec;
@@ -483,8 +542,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     const int gi = r0 + s - 1;
     if (gi < 0 || gi >= nx) continue;
     const size_t gidx = shot_off + (size_t)comp * N + (size_t)gi * ny + j;
-    if (init_cur) T.comp(L[0], comp)[T.at(s, j)] = init_cur[gidx];
-    if (init_prev && s >= 1 && s <= rows) T.comp(L[2], comp)[T.at(s, j)] = init_prev[gidx];
+    if (init_cur) T.comp(Lv(0), comp)[T.at(s, j)] = init_cur[gidx];
+    if (init_prev && s >= 1 && s <= rows) T.comp(Lv(2), comp)[T.at(s, j)] = init_prev[gidx];
   }
   __syncthreads();
   cluster.sync();  // every CTA initialised (levels, mbarriers) before any push
@@ -500,11 +559,11 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   x.rows = rows;
   x.R = R;
   x.ny = ny;
-  uint32_t parity[3] = {0u, 0u, 0u};
+  uint32_t parity_bits = 0u;  // bit l: phase parity of bar[l]
   auto set_levels = [&](int t) {
-    x.cur = L[t % 3];
-    x.prev = L[(t + 2) % 3];
-    x.nxt = L[(t + 1) % 3];
+    x.cur = Lv(t % 3);
+    x.prev = Lv((t + 2) % 3);
+    x.nxt = Lv((t + 1) % 3);
     x.nxt_off_b = (uint32_t)((t + 1) % 3) * (uint32_t)level_floats * 4u;
     const uint32_t lbar = smem_u32(&bar[(t + 1) % 3]);
     x.up_bar = has_up ? map_rank(lbar, rank - 1) : 0u;
@@ -536,8 +595,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       rhs.amp = amp_next * kappa;
       amp_next = (i + 1 < f.i1) ? sig[i + 1] : 0.f;  // in flight during this step
       const bool w = step_wait(t);
-      ring_step<false, false>(T, ks, x, rhs, &bar[t % 3], parity[t % 3], w, c.err);
-      if (w) parity[t % 3] ^= 1u;
+      ring_step<false, false>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err);
+      if (w) parity_bits ^= 1u << (t % 3);
       // bulk stores issued after the previous step read a level overwritten two
       // steps from now: make sure they are done reading before the barrier
       if (tid == 0) bulk_wait_read_all();
@@ -601,7 +660,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     // lam^{m_hi+1} is the imaging partner of u^{m_hi}: store it first
     if (tid == 0 && a.lbuf && a.store_init) {
       fence_proxy_async();
-      store_level(L[0], a.lbuf + (size_t)(a.m_hi + 1 - a.slot_base) * a.state_stride + shot_off,
+      store_level(Lv(0), a.lbuf + (size_t)(a.m_hi + 1 - a.slot_base) * a.state_stride + shot_off,
                   (ptrdiff_t)N);
       bulk_commit();
     }
@@ -635,8 +694,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
         rhs.gy = a.g_y + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
       }
       const bool w = step_wait(t);
-      ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], parity[t % 3], w, c.err);
-      if (w) parity[t % 3] ^= 1u;
+      ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err);
+      if (w) parity_bits ^= 1u << (t % 3);
       if (tid == 0) bulk_wait_read_all();
       __syncthreads();
       t_last = t;
@@ -650,13 +709,14 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   }
   // The neighbours' last pushes land in this CTA's level of step t_last + 1:
   // wait for them before this CTA's shared memory goes away.
-  if (t_last >= 0 && halo_bytes > 0) halo_wait(&bar[(t_last + 1) % 3], parity[(t_last + 1) % 3], c.err);
+  if (t_last >= 0 && halo_bytes > 0)
+    halo_wait(&bar[(t_last + 1) % 3], (parity_bits >> ((t_last + 1) % 3)) & 1u, c.err);
   if (tid == 0) bulk_wait_all();
   __syncthreads();
   if (!is_fwd && a.m_hi >= a.m_lo + 1) {
     // lam^{m_lo+1} (level of step t_last + 1) and lam^{m_lo+2} -> lam_save
-    float* last = L[(t_last + 1) % 3];
-    float* before = L[t_last % 3];
+    float* last = Lv((t_last + 1) % 3);
+    float* before = Lv(t_last % 3);
     for (int e = tid; e < 2 * rows * ny; e += kResThreads) {
       const int comp = e / (rows * ny);
       const int rem = e - comp * rows * ny;
