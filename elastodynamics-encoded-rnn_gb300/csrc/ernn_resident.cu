@@ -25,6 +25,10 @@
 // Scalar constants only (the per-cell modes use the per-step kernels).
 #include <cooperative_groups.h>
 
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "ernn_launch.h"
 #include "ernn_resident.h"
 
@@ -736,10 +740,22 @@ size_t resident_smem_bytes(const ResCommon& c) {
   return 3 * level + (size_t)c.R * c.ny * sizeof(float) + tail;
 }
 
+// Raise the kernel's dynamic shared-memory limit to at least `smem` (once per
+// kernel and size; the limit only grows).
 static cudaError_t configure(const void* fn, size_t smem) {
+  static std::mutex mu;
+  static std::vector<std::pair<const void*, size_t>> done;
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto& kv : done)
+    if (kv.first == fn && kv.second >= smem) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  for (auto& kv : done)
+    if (kv.first == fn) { kv.second = smem; return cudaSuccess; }
+  done.push_back({fn, smem});
+  return cudaSuccess;
 }
 
 static int sm_count() {
@@ -763,11 +779,33 @@ int resident_img_clusters(const ResCommon& c) {
   return z;
 }
 
+// Feasibility answers per (kernel, cluster size, shared memory): the
+// attribute and occupancy queries run once, so later calls (for example
+// during stream capture) make no CUDA runtime calls here.
+struct FeasKey {
+  bool dense;
+  int CL;
+  size_t smem;
+};
+static std::mutex g_feas_mu;
+static std::vector<std::pair<FeasKey, bool>> g_feas;
+
+static bool feasible_uncached(const ResCommon& c, bool dense, size_t smem);
+
 bool resident_feasible(const ResCommon& c, bool dense) {
   if (c.CL < 1 || c.CL > 16 || c.ny % 4 != 0 || c.nrec > kResMaxRec) return false;
   if ((c.CL - 1) * c.R >= c.nx) return false;  // every CTA owns >= 1 row
   const size_t smem = resident_smem_bytes(c);
   if (smem > 220 * 1024) return false;
+  std::lock_guard<std::mutex> lock(g_feas_mu);
+  for (const auto& kv : g_feas)
+    if (kv.first.dense == dense && kv.first.CL == c.CL && kv.first.smem == smem) return kv.second;
+  const bool ok = feasible_uncached(c, dense, smem);
+  g_feas.push_back({FeasKey{dense, c.CL, smem}, ok});
+  return ok;
+}
+
+static bool feasible_uncached(const ResCommon& c, bool dense, size_t smem) {
   const void* fn = dense ? (const void*)resident_kernel<true> : (const void*)resident_kernel<false>;
   if (configure(fn, smem) != cudaSuccess) {
     cudaGetLastError();

@@ -8,6 +8,10 @@ Workloads (synthetic inputs; no dataset is involved):
              256 receivers per shot
   damage512  512x512, 3000 steps, C = (1 - D) C0, 8 top sources, 128
              receivers on the top and bottom edges
+  multi64    64 independent inversions, side drawn from {128, 192, ..., 768},
+             5.2 x side steps, C0 scaled by U(0.8, 1.2) per constant and
+             rotated by U(0, 90) degrees, 1 source and 32 receivers each; one
+             Adam iteration over all of them captured in a CUDA graph
 dx = dz = 0.1 mm, dt = 5 ns, rho = 1560 kg/m^3, 5-cycle Hann 1 MHz tone-burst
 vertical force (Gaussian point load of the reference's source model, a = 5e6
 m^-2) on the top edge (y = ny - 1).  Observations: the same forward at the
@@ -252,3 +256,96 @@ def run_inversion(w: Workload, device, iters=200, lr=1e-2, seed=0):
         losses.append(inv.step())
     losses = [float(v) for v in torch.stack(losses).cpu()]
     return inv.constants(), inv.relative_errors(), losses
+
+
+def multi_instances(n=64, seed=0, sides=None):
+    """Workloads of the uneven multi-inversion configuration (seeded)."""
+    rng = np.random.default_rng(seed)
+    if sides is None:
+        sides = rng.choice(np.arange(128, 769, 64), size=n)
+    out = []
+    for i, side in enumerate(sides):
+        side = int(side)
+        C0 = C_ORTHO * rng.uniform(0.8, 1.2, size=6)
+        C = materials.rotate(C0, float(rng.uniform(0.0, 90.0)))
+        nt = int(round(5.2 * side))
+        out.append(Workload(f"inst{i}_{side}", side, side, nt, C, [(side // 2, side - 1)],
+                            _top(32, side, side)))
+    return out
+
+
+class MultiInversion:
+    """Many independent scalar-constant inversions advanced as one iteration:
+    each instance's forward, misfit and hand adjoint run on one of `nstreams`
+    CUDA streams, one Adam step updates every instance, and the whole iteration
+    is captured once in a CUDA graph and replayed (`step`)."""
+
+    def __init__(self, ws, device, lr=1e-2, seed=0, nstreams=8, graph=True):
+        from .propagate import choose_ckpt_k
+        self.ws = ws
+        self.device = device
+        self.invs = []
+        for k, w in enumerate(ws):
+            inv = Inversion(w, device, lr=lr, seed=seed + k)
+            # fix the checkpoint interval now (the choice queries free memory)
+            inv.geom.ckpt_k = choose_ckpt_k(inv.geom, 0, device, budget_fraction=0.4 / len(ws))
+            self.invs.append(inv)
+        params = [inv.params.theta for inv in self.invs]
+        self.opt = torch.optim.Adam(params, lr=lr, capturable=graph)
+        self.streams = [torch.cuda.Stream(device) for _ in range(nstreams)]
+        self.obs = [o for inv in self.invs for o in inv.obs]
+        self.cell_steps = sum(w.cell_steps for w in ws)
+        self.graph = None
+        self.loss = None
+        if graph:
+            self._capture()
+
+    def _eager_step(self):
+        self.opt.zero_grad(set_to_none=False)
+        main = torch.cuda.current_stream(self.device)
+        losses = []
+        for k, inv in enumerate(self.invs):
+            s = self.streams[k % len(self.streams)]
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                ux, uy = propagate(inv.params(), inv.rho, inv.geom)
+                lk = trace_misfit(ux, uy, inv.obs[0], inv.obs[1])
+                lk.backward()
+            losses.append(lk)
+        for s in self.streams:
+            main.wait_stream(s)
+        self.opt.step()
+        return torch.stack([l.detach() for l in losses]).sum()
+
+    def _capture(self):
+        # warm up on a side stream (allocator pools, autograd, library caches)
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                self._eager_step()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        torch.cuda.synchronize(self.device)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = self._eager_step()
+
+    def step(self, obs=None):
+        if obs is not None:
+            for dst, src in zip(self.obs, obs):
+                if dst.data_ptr() != src.data_ptr():
+                    dst.copy_(src, non_blocking=True)
+        if self.graph is None:
+            return self._eager_step()
+        self.graph.replay()
+        return self.loss
+
+    def forward_only(self):
+        with torch.no_grad():
+            return [propagate(inv.params().detach(), inv.rho, inv.geom) for inv in self.invs]
+
+    def gradient(self):
+        return torch.cat([inv.params.theta.grad for inv in self.invs])
+
+    def relative_errors(self):
+        return np.stack([inv.relative_errors() for inv in self.invs])
