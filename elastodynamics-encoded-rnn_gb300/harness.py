@@ -161,10 +161,20 @@ class NormalisedConstants(torch.nn.Module):
         return self.theta * self.scale
 
 
-def initial_guess(w: Workload, seed=0, spread=0.2):
-    """Each constant perturbed uniformly by +-spread (seeded)."""
+def initial_guess(w: Workload, seed=0, spread=0.2, max_draws=100):
+    """Each constant perturbed uniformly by +-spread (seeded).  Perturbing the
+    six constants of a rotated material independently can leave a stiffness
+    that is not positive-definite (the time loop then diverges): such draws
+    are rejected and redrawn from the same seeded stream."""
     rng = np.random.default_rng(seed)
-    return w.C_true * rng.uniform(1 - spread, 1 + spread, size=6)
+    for _ in range(max_draws):
+        C = w.C_true * rng.uniform(1 - spread, 1 + spread, size=6)
+        try:
+            materials.check_stability(C, RHO, H, DT)
+            return C
+        except ValueError:
+            continue
+    raise ValueError("no stable initial guess found")
 
 
 def scales(C_true):
