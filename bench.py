@@ -39,6 +39,9 @@ L2_BYTES = 129 * 1024 * 1024
 FLUSH_BYTES = 256 * 1024 * 1024
 
 
+PATHS = {"auto": 0, "step": 1, "resident": 2, "tiled": 3}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -51,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nt", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--ckpt", type=int, default=None, help="override the checkpoint interval")
+    ap.add_argument("--path", choices=list(PATHS), default="auto",
+                    help="kernel path of the library (auto picks per problem)")
     ap.add_argument("--plain", action="store_true",
                     help="only run warmup + steps iterations (no timing, no JSON): a profiling target")
     return ap.parse_args()
@@ -63,6 +68,7 @@ def make_workload(args):
         w.nt = args.nt
     if args.ckpt is not None:
         w.ckpt_k = args.ckpt
+    w.path = PATHS[args.path]
     return w
 
 
@@ -294,10 +300,14 @@ def run_ernn(args, dist):
     alg_bytes = tot_bytes / max(nlaunch, 1)        # algorithmic bytes per launch (library-counted)
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    resident = nlaunch < w.nt                        # one launch per pass, not per step
-    kernel_name = ("resident_kernel" if resident else
-                   {"forward": "fwd_step_kernel", "adjoint": "adj_step_kernel"}[cls])
+    used = int(lib.ernn_last_path())
+    kernel_name = {E.PATH_RESIDENT: {"forward": "resident_kernel", "adjoint": "resident_kernel"},
+                   E.PATH_TILED: {"forward": "tma_fwd_kernel", "adjoint": "tma_adj_kernel"}}.get(
+        used, {"forward": "fwd_step_kernel", "adjoint": "adj_step_kernel"})[cls]
     traffic = profiled_traffic(kernel_name, args.workload)
+    state_mb = w.nshots * 2 * w.nx * w.ny * 4 / 2**20
+    l2_note = ("working set (three state levels) is L2-resident at this size; bytes are algorithmic"
+               if 3 * state_mb < 100 else "state levels exceed L2; bytes are algorithmic")
 
     rec = {
         "metric": "Gcell-steps/s fwd+adj (hand adjoint, one Adam iteration)",
@@ -316,6 +326,7 @@ def run_ernn(args, dist):
                                f"{len(w.rec_cells)} receivers, {'D-field' if w.D_true is not None else 'scalar constants'}, "
                                f"ckpt every {inv.geom.ckpt_k} steps",
                    "cell_steps_per_iter": w.cell_steps,
+                   "kernel_path": {0: "auto", 1: "step", 2: "resident", 3: "tiled"}[int(lib.ernn_last_path())],
                    "l2": "flushed between timed iterations (256 MiB write)",
                    "parallelism": f"replicas x{dist.world}"},
         "e2e": {"value": round(dist.world * w.cell_steps / (e2e_ms * 1e-3) / 1e9, 4),
@@ -331,7 +342,7 @@ def run_ernn(args, dist):
                      "frac": round(achieved / peak, 4),
                      "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
                      "launch_us": round(per_launch_ms * 1e3, 3), "launches_per_iter": nlaunch,
-                     "note": "working set is L2-resident at this size; bytes are algorithmic"},
+                     "note": l2_note},
         "clocks": clk,
         "loss": float(inv.step().item()),
     }

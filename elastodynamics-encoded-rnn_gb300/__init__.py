@@ -15,9 +15,9 @@ Public surface:
       configurations.
 """
 from . import _lib, materials, sources
-from ._lib import PATH_AUTO, PATH_RESIDENT, PATH_STEP
+from ._lib import PATH_AUTO, PATH_RESIDENT, PATH_STEP, PATH_TILED
 from .propagate import (MODE_DFIELD, MODE_FIELDS, MODE_SCALAR, RECORD_FIELDS,
-                        RECORD_RECEIVERS, ErnnPropagate, Geometry,
+                        RECORD_RECEIVERS, ErnnPropagate, Geometry, check_device_status,
                         elastic_operator_with_force, propagate)
 from .simulators import (CFRPWaveSimulatorRicker, DegradationSimulator, ShotGatherSimulator,
                          SpatiallyVaryingAnisotropicSimulator)
@@ -27,7 +27,7 @@ __all__ = [
     "DegradationSimulator", "ErnnPropagate", "Geometry", "propagate",
     "elastic_operator_with_force", "sources", "materials", "MODE_SCALAR", "MODE_DFIELD",
     "MODE_FIELDS", "RECORD_FIELDS", "RECORD_RECEIVERS", "PATH_AUTO", "PATH_STEP",
-    "PATH_RESIDENT", "load_library",
+    "PATH_RESIDENT", "PATH_TILED", "check_device_status", "load_library",
 ]
 
 

@@ -12,7 +12,7 @@ from . import _build
 
 MODE_SCALAR, MODE_DFIELD, MODE_FIELDS = 0, 1, 2
 RECORD_FIELDS, RECORD_RECEIVERS = 0, 1
-PATH_AUTO, PATH_STEP, PATH_RESIDENT = 0, 1, 2
+PATH_AUTO, PATH_STEP, PATH_RESIDENT, PATH_TILED = 0, 1, 2, 3
 
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "workspace too small", 3: "CUDA runtime error",
@@ -57,6 +57,10 @@ SIGNATURES = {
     "ernn_forward_static": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
                                            _P, _P, _P]),
     "ernn_launch_count": (ctypes.c_uint64, []),
+    "ernn_last_path": (ctypes.c_int32, []),
+    "ernn_device_status": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p]),
+    "ernn_wait_selftest": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]),
     "ernn_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "ernn_profile_read": (ctypes.c_int, [_P, _P, _P]),
 }

@@ -2,12 +2,15 @@
 // host-side time-loop driver: step schedule, checkpoint/recompute plan,
 // workspace layout.  Every launch goes on the caller's stream; nothing here
 // synchronises the host or allocates device memory.
+#include <atomic>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 
 #include "ernn.h"
 #include "ernn_launch.h"
 #include "ernn_resident.h"
+#include "ernn_tma.h"
 
 namespace ernn {
 namespace {
@@ -82,7 +85,7 @@ int validate(const ErnnProblem* p) {
   if (p->record == kRecordReceivers && p->nrec < 1) return ERNN_ERR_INVALID;
   if (p->src_comp != 0 && p->src_comp != 1) return ERNN_ERR_INVALID;
   if (p->src_bx < 0 || p->src_by < 0) return ERNN_ERR_INVALID;
-  if (p->path < ERNN_PATH_AUTO || p->path > ERNN_PATH_RESIDENT || p->reserved != 0)
+  if (p->path < ERNN_PATH_AUTO || p->path > ERNN_PATH_TILED || p->reserved != 0)
     return ERNN_ERR_INVALID;
   if (!(p->h > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->h) || !std::isfinite(p->dt))
     return ERNN_ERR_INVALID;
@@ -121,6 +124,28 @@ FwdStep base_fwd(const ErnnProblem& p, const ErnnInputs& in, const Coef* coef, i
   a.rec_idx = in.rec_idx;
   a.nrec = p.nrec;
   return a;
+}
+
+std::atomic<int32_t> g_last_path{ERNN_PATH_AUTO};
+
+// Tiled per-step kernels: requested (ERNN_PATH_TILED, an error when the
+// problem is not eligible) or chosen by ERNN_PATH_AUTO when eligible and one
+// step has at least one tile per SM.
+int use_tiled(const ErnnProblem& p, int* tiled) {
+  *tiled = 0;
+  if (p.path == ERNN_PATH_STEP) return ERNN_OK;
+  const bool ok = tma_eligible(p.mode, p.nx, p.ny, p.nshots);
+  if (p.path == ERNN_PATH_TILED) {
+    if (!ok) return ERNN_ERR_UNSUPPORTED;
+    *tiled = 1;
+    return ERNN_OK;
+  }
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return ERNN_ERR_CUDA;
+  *tiled = ok && tma_tiles(p.nx, p.ny, p.nshots) >= (size_t)sms;
+  return ERNN_OK;
 }
 
 // Cluster-resident configuration: CL CTAs of R rows each.  Returns false when
@@ -329,12 +354,20 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
   Coef* coef = reinterpret_cast<Coef*>(at(tape, pl.t_coef));
   ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st));
 
-  if (p->path != ERNN_PATH_STEP) {
+  if (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT) {
     ResCommon res;
-    if (pick_resident(*p, *in, coef, res))
+    if (pick_resident(*p, *in, coef, res)) {
+      g_last_path.store(ERNN_PATH_RESIDENT, std::memory_order_relaxed);
       return resident_forward(*p, pl, res, out_ux, out_uy, tape, with_tape, st);
+    }
     if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;
   }
+  int tiled = 0;
+  if ((rc = use_tiled(*p, &tiled))) return rc;
+  g_last_path.store(tiled ? ERNN_PATH_TILED : ERNN_PATH_STEP, std::memory_order_relaxed);
+  auto fwd_step = [&](const FwdStep& s) {
+    return tiled ? launch_tma_fwd(s, &coef->err, st) : launch_fwd_step(p->mode, s, st);
+  };
 
   const bool store_all = with_tape && pl.store_all;
   float* A = fat(tape, pl.t_A);
@@ -369,7 +402,7 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
     } else if (i >= 1 && (i - 1) % p->stride == 0) {
       a.gframe = (i - 1) / p->stride; a.tr_x = out_ux; a.tr_y = out_uy;
     }
-    ERNN_CUDA(launch_fwd_step(p->mode, a, st));
+    ERNN_CUDA(fwd_step(a));
     last = a.out;
   }
   if (receivers && (p->nt - 1) % p->stride == 0) {
@@ -407,9 +440,10 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   if (p->mode != kModeScalar) ERNN_CUDA(cudaMemsetAsync(gacc, 0, pl.s_part - pl.s_gacc, st));
   else ERNN_CUDA(cudaMemsetAsync(partials, 0, pl.s_total - pl.s_part, st));
 
-  if (p->path != ERNN_PATH_STEP) {
+  if (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT) {
     ResCommon res;
     if (pick_resident(*p, *in, coef, res)) {
+      g_last_path.store(ERNN_PATH_RESIDENT, std::memory_order_relaxed);
       int img_rows = 0;
       if ((rc = resident_adjoint(*p, pl, res, g_ux, g_uy, tape, scratch, partials, &img_rows, st)))
         return rc;
@@ -418,6 +452,9 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     }
     if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;
   }
+  int tiled = 0;
+  if ((rc = use_tiled(*p, &tiled))) return rc;
+  g_last_path.store(tiled ? ERNN_PATH_TILED : ERNN_PATH_STEP, std::memory_order_relaxed);
 
   auto stored = [&](int n) { return fat(tape, pl.t_store + (size_t)(n - 1) * pl.state_bytes); };
   auto ck = [&](int j, int lev) -> const float* {
@@ -445,7 +482,8 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     b.prev = b.out;
     b.u = (m <= p->nt - 1) ? um : nullptr;
     b.frame = ((m - 1) % p->stride == 0) ? (m - 1) / p->stride : -1;
-    return launch_adj_step(p->mode, b, st) == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
+    const cudaError_t e = tiled ? launch_tma_adj(b, &coef->err, st) : launch_adj_step(p->mode, b, st);
+    return e == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
   };
 
   if (pl.store_all) {
@@ -463,7 +501,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
         a.out = seg(i - i0);
         a.cur = (i == i0) ? ck(j, 0) : seg(i - i0 - 1);
         a.prev = (i == i0) ? ck(j, 1) : (i == i0 + 1 ? ck(j, 0) : seg(i - i0 - 2));
-        ERNN_CUDA(launch_fwd_step(p->mode, a, st));
+        ERNN_CUDA(tiled ? launch_tma_fwd(a, &coef->err, st) : launch_fwd_step(p->mode, a, st));
       }
       for (int m = i1; m >= i0 + 1; --m)
         if ((rc = adj_step(m, seg(m - 1 - i0)))) return rc;
@@ -478,6 +516,30 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
 }
 
 uint64_t ernn_launch_count(void) { return launches(); }
+
+int ernn_device_status(const ErnnProblem* p, const void* workspace, int is_scratch,
+                       int32_t* status_host, void* stream) {
+  int rc = validate(p);
+  if (rc) return rc;
+  if (workspace == nullptr || status_host == nullptr || (is_scratch != 0 && is_scratch != 1))
+    return ERNN_ERR_INVALID;
+  const Plan pl = make_plan(*p);
+  const char* w = static_cast<const char*>(workspace) + (is_scratch ? pl.s_coef : pl.t_coef) +
+                  offsetof(Coef, err);
+  ERNN_CUDA(cudaMemcpyAsync(status_host, w, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                            (cudaStream_t)stream));
+  return ERNN_OK;
+}
+
+int ernn_wait_selftest(int32_t* status_host, void* stream) {
+  if (status_host == nullptr) return ERNN_ERR_INVALID;
+  int v = -1;
+  ERNN_CUDA(wait_selftest(&v, (cudaStream_t)stream));
+  *status_host = v;
+  return ERNN_OK;
+}
+
+int32_t ernn_last_path(void) { return g_last_path.load(std::memory_order_relaxed); }
 
 int ernn_profile_enable(int enable) {
   profile_enable(enable != 0);

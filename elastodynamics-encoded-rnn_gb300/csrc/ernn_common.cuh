@@ -40,6 +40,12 @@ struct Coef {
   double pad2;
 };
 
+// Spin limit of every device-side wait on an mbarrier (about a second at the
+// part's clocks).  A wait that runs out records kDeviceTimeout in the call's
+// error word and returns; later waits of the launch return at once.
+constexpr long long kWaitLimitCycles = 1ll << 31;
+constexpr int kDeviceTimeout = 5;  // ERNN_ERR_TIMEOUT
+
 // Tile geometry of the per-step kernels: 32 rows (x) by 32 columns (y),
 // 256 threads as 8 row groups of one warp each; a thread owns 4 cells of
 // one column.

@@ -79,8 +79,8 @@ __device__ __forceinline__ void halo_wait(uint64_t* bar, uint32_t parity, int* e
   if (*(volatile int*)err != 0) return;
   const long long t0 = clock64();
   while (!mbar_try_wait_cluster(bar, parity)) {
-    if (clock64() - t0 > (1ll << 31)) {
-      atomicExch(err, 5 /* ERNN_ERR_TIMEOUT */);
+    if (clock64() - t0 > kWaitLimitCycles) {
+      atomicExch(err, kDeviceTimeout);
       return;
     }
   }

@@ -1,0 +1,589 @@
+// Per-step kernels for large grids (sm_103a), TMA-pipelined.
+//
+// One launch per time step, as the first per-step kernels, but each CTA is
+// persistent over a strided list of 64 (y) x 32 (x) tiles of the step and
+// streams them through a two-stage shared-memory pipeline: while a tile is
+// computed, the tensor-memory-accelerator loads of the next tile are in
+// flight (cp.async.bulk.tensor, completion on an mbarrier per stage).
+//
+// The halo box of a tile is 72 x 34 cells: rows x0-1 .. x0+32 and columns
+// y0-4 .. y0+67 (the innermost coordinate must be a multiple of four floats,
+// so the box reaches four columns to the left where one is needed).  Cells
+// outside the grid are filled with zeros by the copy engine: that is the
+// zero ghost ring of the scheme, with no predicated loads.
+//
+// Scalar constants (ERNN_MODE_SCALAR), ny % 4 == 0.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "ernn_launch.h"
+#include "ernn_tma.h"
+
+namespace ernn {
+
+namespace {
+
+constexpr int kTY = 64, kTX = 32;          // tile: 64 columns (y) by 32 rows (x)
+constexpr int kBW = kTY + 8, kBH = kTX + 2;  // halo box
+constexpr int kThreads = 256;              // 16 column quads x 16 row pairs
+constexpr int kHaloFloats = 2 * kBH * kBW;  // both components
+constexpr int kOwnFloats = 2 * kTX * kTY;
+
+__device__ __forceinline__ uint32_t s32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void bar_init(uint64_t* b) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(s32(b)) : "memory");
+}
+
+__device__ __forceinline__ void bar_expect(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s32(b)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(s32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait (about a second); on timeout records ERNN_ERR_TIMEOUT and
+// returns so that the CTA's barriers stay matched.
+__device__ __forceinline__ void bar_wait(uint64_t* b, uint32_t parity, int* err) {
+  if (bar_try(b, parity)) return;
+  if (*(volatile int*)err != 0) return;
+  const long long t0 = clock64();
+  while (!bar_try(b, parity)) {
+    if (clock64() - t0 > kWaitLimitCycles) {
+      atomicExch(err, kDeviceTimeout);
+      return;
+    }
+  }
+}
+
+// 3D tile load (columns, rows, component planes) into shared memory.
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                          uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(s32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(s32(b))
+      : "memory");
+}
+
+// TMA destinations start on 128-byte boundaries: the dynamic shared block is
+// allocated 128 bytes longer and its start rounded up.
+__device__ __forceinline__ float* aligned128(float* p) {
+  return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 127) & ~static_cast<uintptr_t>(127));
+}
+
+__device__ __forceinline__ void fence_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+struct Coefs {
+  float k11, k22, kq12, k16, k26, k66, k16h, k26h;
+};
+
+__device__ __forceinline__ Coefs coefs(const Coef* c) {
+  return Coefs{c->k11, c->k22, c->kq12, c->k16, c->k26, c->k66, c->k16h, c->k26h};
+}
+
+// window [j-1 .. j+4] of halo-box row r (box column of cell column j is j + 4)
+__device__ __forceinline__ void win(const float* __restrict__ box, int r, int j, float w[6]) {
+  const float* p = box + r * kBW + j + 4;
+  const float4 m = *reinterpret_cast<const float4*>(p);
+  w[0] = p[-1];
+  w[1] = m.x;
+  w[2] = m.y;
+  w[3] = m.z;
+  w[4] = m.w;
+  w[5] = p[4];
+}
+
+struct Sums4 {
+  float cx[4], cy[4], xx_x[4], yy_x[4], xy_x[4], xx_y[4], yy_y[4], xy_y[4];
+};
+
+__device__ __forceinline__ void sums4(const float ux[3][6], const float uy[3][6], Sums4& s) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int k = q + 1;
+    s.cx[q] = ux[1][k];
+    s.cy[q] = uy[1][k];
+    s.xx_x[q] = (ux[0][k] + ux[2][k]) - 2.f * ux[1][k];
+    s.yy_x[q] = (ux[1][k - 1] + ux[1][k + 1]) - 2.f * ux[1][k];
+    s.xy_x[q] = (ux[2][k + 1] + ux[0][k - 1]) - (ux[2][k - 1] + ux[0][k + 1]);
+    s.xx_y[q] = (uy[0][k] + uy[2][k]) - 2.f * uy[1][k];
+    s.yy_y[q] = (uy[1][k - 1] + uy[1][k + 1]) - 2.f * uy[1][k];
+    s.xy_y[q] = (uy[2][k + 1] + uy[0][k - 1]) - (uy[2][k - 1] + uy[0][k + 1]);
+  }
+}
+
+__device__ __forceinline__ void apply(const Coefs& k, const Sums4& s, int q, float& lx, float& ly) {
+  lx = k.k11 * s.xx_x[q] + k.k66 * s.yy_x[q] + k.kq12 * s.xy_y[q] + k.k16h * s.xy_x[q] +
+       k.k16 * s.xx_y[q] + k.k26 * s.yy_y[q];
+  ly = k.k66 * s.xx_y[q] + k.k22 * s.yy_y[q] + k.kq12 * s.xy_x[q] + k.k16 * s.xx_x[q] +
+       k.k26 * s.yy_x[q] + k.k26h * s.xy_y[q];
+}
+
+__device__ __forceinline__ void shift(float u[3][6]) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { u[0][k] = u[1][k]; u[1][k] = u[2][k]; }
+}
+
+__device__ __forceinline__ float g4(const float4& v, int q) {
+  return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w;
+}
+
+struct TileId {
+  int shot, x0, y0;
+};
+
+__device__ __forceinline__ TileId tile_of(int t, int tiles_x, int tiles_y) {
+  const int per_shot = tiles_x * tiles_y;
+  TileId id;
+  id.shot = t / per_shot;
+  const int r = t - id.shot * per_shot;
+  id.x0 = (r / tiles_y) * kTX;
+  id.y0 = (r % tiles_y) * kTY;
+  return id;
+}
+
+// ----------------------------------------------------------------- forward
+__global__ void __launch_bounds__(kThreads, 3)
+    tma_fwd_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
+                   const __grid_constant__ CUtensorMap prev_map, int tiles_x, int tiles_y, int has_prev,
+                   int* err) {
+  extern __shared__ float sm_raw[];
+  float* sm = aligned128(sm_raw);
+  constexpr int kStage = kHaloFloats + kOwnFloats;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * kStage);
+  const int tid = threadIdx.x;
+  const int nx = a.nx, ny = a.ny;
+  const size_t N = (size_t)nx * ny;
+  const int ntiles = a.S * tiles_x * tiles_y;
+  const uint32_t bytes = (uint32_t)(kHaloFloats + (has_prev ? kOwnFloats : 0)) * 4u;
+
+  // receiver gather of the input state u^i, spread over the grid
+  if (a.gframe >= 0) {
+    for (int e = blockIdx.x * kThreads + tid; e < a.S * a.nrec; e += gridDim.x * kThreads) {
+      const int s = e / a.nrec, r = e - s * a.nrec;
+      const int32_t idx = a.rec_idx[e];
+      const size_t o = ((size_t)s * a.nt_out + a.gframe) * a.nrec + r;
+      const bool ok = a.cur != nullptr && idx >= 0 && (size_t)idx < N;
+      a.tr_x[o] = ok ? a.cur[(size_t)s * 2 * N + idx] : 0.f;
+      a.tr_y[o] = ok ? a.cur[(size_t)s * 2 * N + N + idx] : 0.f;
+    }
+  }
+  if (tid == 0) {
+    bar_init(&bar[0]);
+    bar_init(&bar[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const Coefs ks = coefs(a.coef);
+  const float kappa = a.coef->kappa;
+  const bool has_src = a.bx > 0 && a.by > 0;
+  auto issue = [&](int k) {  // loads of this CTA's k-th tile into stage k & 1
+    const int t = blockIdx.x + k * gridDim.x;
+    if (t >= ntiles) return;
+    const TileId id = tile_of(t, tiles_x, tiles_y);
+    float* st = sm + (k & 1) * kStage;
+    fence_async();
+    bar_expect(&bar[k & 1], bytes);
+    tma_load3(st, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+    if (has_prev) tma_load3(st + kHaloFloats, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
+  };
+  if (tid == 0) issue(0);
+  const int qc = tid & 15, rg = tid >> 4;
+  const int j = 4 * qc;
+  for (int k = 0;; ++k) {
+    const int t = blockIdx.x + k * gridDim.x;
+    if (t >= ntiles) break;
+    if (tid == 0) issue(k + 1);
+    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
+    const TileId id = tile_of(t, tiles_x, tiles_y);
+    const float* hb = sm + (k & 1) * kStage;
+    const float* pb = hb + kHaloFloats;
+    const float amp = a.src_signal[(size_t)id.shot * a.nt + a.i] * kappa;
+    const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
+    float* out = a.out + (size_t)id.shot * 2 * N;
+    const int gj = id.y0 + j;
+    float wx[3][6], wy[3][6];
+    const int r0 = 2 * rg;  // tile rows r0, r0 + 1 -> box rows r0 + 1, r0 + 2
+    win(hb, r0, j, wx[0]);
+    win(hb + kBH * kBW, r0, j, wy[0]);
+    win(hb, r0 + 1, j, wx[1]);
+    win(hb + kBH * kBW, r0 + 1, j, wy[1]);
+#pragma unroll
+    for (int q2 = 0; q2 < 2; ++q2) {
+      const int r = r0 + q2;
+      win(hb, r + 2, j, wx[2]);
+      win(hb + kBH * kBW, r + 2, j, wy[2]);
+      Sums4 st;
+      sums4(wx, wy, st);
+      const int gi = id.x0 + r;
+      if (gi < nx && gj < ny) {
+        float4 pvx = make_float4(0.f, 0.f, 0.f, 0.f), pvy = pvx;
+        if (has_prev) {
+          pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
+          pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+        }
+        float vx[4], vy[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float lx, ly;
+          apply(ks, st, q, lx, ly);
+          vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
+          vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
+          if (has_src) {
+            const int sa = gi - ox, sb = gj + q - oy;
+            if (sa >= 0 && sa < a.bx && sb >= 0 && sb < a.by) {
+              const float f = amp * a.src_map[((size_t)id.shot * a.bx + sa) * a.by + sb];
+              if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
+            }
+          }
+        }
+        const float4 nvx = make_float4(vx[0], vx[1], vx[2], vx[3]);
+        const float4 nvy = make_float4(vy[0], vy[1], vy[2], vy[3]);
+        const size_t o = (size_t)gi * ny + gj;
+        *reinterpret_cast<float4*>(out + o) = nvx;
+        *reinterpret_cast<float4*>(out + N + o) = nvy;
+        if (a.copy0) {
+          *reinterpret_cast<float4*>(a.copy0 + (size_t)id.shot * 2 * N + o) = nvx;
+          *reinterpret_cast<float4*>(a.copy0 + (size_t)id.shot * 2 * N + N + o) = nvy;
+        }
+        if (a.copy1) {
+          *reinterpret_cast<float4*>(a.copy1 + (size_t)id.shot * 2 * N + o) = nvx;
+          *reinterpret_cast<float4*>(a.copy1 + (size_t)id.shot * 2 * N + N + o) = nvy;
+        }
+        if (a.frame >= 0) {
+          const size_t ho = ((size_t)id.shot * a.nt_out + a.frame) * N + o;
+          *reinterpret_cast<float4*>(a.hist_x + ho) = nvx;
+          *reinterpret_cast<float4*>(a.hist_y + ho) = nvy;
+        }
+      }
+      shift(wx);
+      shift(wy);
+    }
+    __syncthreads();  // stage k & 1 is free for the loads of tile k + 2
+  }
+}
+
+// ----------------------------------------------------------------- adjoint
+__global__ void __launch_bounds__(kThreads, 2)
+    tma_adj_kernel(const AdjStep a, const __grid_constant__ CUtensorMap cur_map,
+                   const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap u_map,
+                   int tiles_x, int tiles_y, int has_u, int* err) {
+  extern __shared__ float sm_raw[];
+  float* sm = aligned128(sm_raw);
+  constexpr int kStage = 2 * kHaloFloats + kOwnFloats;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * kStage);
+  __shared__ double red[kThreads / 32][6];
+  const int tid = threadIdx.x;
+  const int nx = a.nx, ny = a.ny;
+  const size_t N = (size_t)nx * ny;
+  const int ntiles = a.S * tiles_x * tiles_y;
+  const uint32_t bytes = (uint32_t)(kHaloFloats + kOwnFloats + (has_u ? kHaloFloats : 0)) * 4u;
+  if (tid == 0) {
+    bar_init(&bar[0]);
+    bar_init(&bar[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const Coefs ks = coefs(a.coef);
+  const float gs = a.coef->gscale;
+  auto issue = [&](int k) {
+    const int t = blockIdx.x + k * gridDim.x;
+    if (t >= ntiles) return;
+    const TileId id = tile_of(t, tiles_x, tiles_y);
+    float* st = sm + (k & 1) * kStage;
+    fence_async();
+    bar_expect(&bar[k & 1], bytes);
+    tma_load3(st, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+    tma_load3(st + kHaloFloats, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
+    if (has_u) tma_load3(st + kHaloFloats + kOwnFloats, &u_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+  };
+  if (tid == 0) issue(0);
+  const int qc = tid & 15, rg = tid >> 4;
+  const int j = 4 * qc;
+  // imaging sums: FP32 over a thread's 8 cells of a tile, accumulated over
+  // tiles as FP32 pairs (TwoSum), FP64 across threads and launches
+  float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int k = 0;; ++k) {
+    const int t = blockIdx.x + k * gridDim.x;
+    if (t >= ntiles) break;
+    if (tid == 0) issue(k + 1);
+    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
+    const TileId id = tile_of(t, tiles_x, tiles_y);
+    float* hb = sm + (k & 1) * kStage;
+    float* pb = hb + kHaloFloats;
+    const float* ub = pb + kOwnFloats;
+    // adjoint source at receiver cells: subtract it from this tile's copy of
+    // lam^{m+2} (lam^m = ... - lam^{m+2} + ... + g)
+    if (a.frame >= 0 && a.record == kRecordReceivers) {
+      for (int rr = tid; rr < a.nrec; rr += kThreads) {
+        const int32_t idx = a.rec_idx[(size_t)id.shot * a.nrec + rr];
+        if (idx < 0 || (size_t)idx >= N) continue;
+        const int gi = idx / ny, gjj = idx - gi * ny;
+        if (gi >= id.x0 && gi < id.x0 + kTX && gjj >= id.y0 && gjj < id.y0 + kTY) {
+          const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * a.nrec + rr;
+          atomicAdd(&pb[(gi - id.x0) * kTY + (gjj - id.y0)], -gs * a.g_x[go]);
+          atomicAdd(&pb[kTX * kTY + (gi - id.x0) * kTY + (gjj - id.y0)], -gs * a.g_y[go]);
+        }
+      }
+      __syncthreads();
+    }
+    float* out = a.out + (size_t)id.shot * 2 * N;
+    const int gj = id.y0 + j;
+    float wx[3][6], wy[3][6], vx_[3][6], vy_[3][6];
+    const int r0 = 2 * rg;
+    win(hb, r0, j, wx[0]);
+    win(hb + kBH * kBW, r0, j, wy[0]);
+    win(hb, r0 + 1, j, wx[1]);
+    win(hb + kBH * kBW, r0 + 1, j, wy[1]);
+    if (has_u) {
+      win(ub, r0, j, vx_[0]);
+      win(ub + kBH * kBW, r0, j, vy_[0]);
+      win(ub, r0 + 1, j, vx_[1]);
+      win(ub + kBH * kBW, r0 + 1, j, vy_[1]);
+    }
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q2 = 0; q2 < 2; ++q2) {
+      const int r = r0 + q2;
+      win(hb, r + 2, j, wx[2]);
+      win(hb + kBH * kBW, r + 2, j, wy[2]);
+      Sums4 st;
+      sums4(wx, wy, st);
+      const int gi = id.x0 + r;
+      const bool in = gi < nx && gj < ny;
+      if (in) {
+        const float4 pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
+        const float4 pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+        float vx[4], vy[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float lx, ly;
+          apply(ks, st, q, lx, ly);
+          vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
+          vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
+        }
+        const size_t o = (size_t)gi * ny + gj;
+        if (a.frame >= 0 && a.record == kRecordFields) {
+          const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * N + o;
+          const float4 gx = *reinterpret_cast<const float4*>(a.g_x + go);
+          const float4 gy = *reinterpret_cast<const float4*>(a.g_y + go);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            vx[q] += gs * g4(gx, q);
+            vy[q] += gs * g4(gy, q);
+          }
+        }
+        *reinterpret_cast<float4*>(out + o) = make_float4(vx[0], vx[1], vx[2], vx[3]);
+        *reinterpret_cast<float4*>(out + N + o) = make_float4(vy[0], vy[1], vy[2], vy[3]);
+      }
+      if (has_u) {
+        win(ub, r + 2, j, vx_[2]);
+        win(ub + kBH * kBW, r + 2, j, vy_[2]);
+        if (in) {
+          Sums4 su;
+          sums4(vx_, vy_, su);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float l1x = st.cx[q], l1y = st.cy[q];
+            acc[0] += l1x * su.xx_x[q];
+            acc[1] += l1y * su.yy_y[q];
+            acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
+            acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
+            acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
+            acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
+          }
+        }
+        shift(vx_);
+        shift(vy_);
+      }
+      shift(wx);
+      shift(wy);
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {  // TwoSum(hi, acc)
+      const float s = hi[q] + acc[q];
+      const float bp = s - hi[q];
+      lo[q] += (hi[q] - (s - bp)) + (acc[q] - bp);
+      hi[q] = s;
+    }
+    __syncthreads();  // stage k & 1 is free for the loads of tile k + 2
+  }
+  if (!has_u) return;
+  const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    double v = (double)hi[q] + (double)lo[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][q] = v;
+  }
+  __syncthreads();
+  if (tid < 6) {
+    double v = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) v += red[w][tid];
+    a.partials[(size_t)blockIdx.x * 8 + tid] += v;
+  }
+}
+
+// ------------------------------------------------------ wait self-test
+// One thread waits on an mbarrier that nothing arrives at (no copy is in
+// flight towards this CTA), through the same bounded wait as the tile loop.
+__global__ void wait_selftest_kernel(int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    bar_init(&bar);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    bar_wait(&bar, 0u, status);
+  }
+}
+
+__device__ int g_selftest_status;
+
+// ----------------------------------------------------------------- host
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static std::mutex mu;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (fn == nullptr) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// Tensor map over S shots of [comp][nx][ny] floats: dims (ny, nx, 2 S).
+bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int S, int bw, int bh) {
+  auto fn = encode_fn();
+  if (fn == nullptr || base == nullptr) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)2 * S};
+  const cuuint64_t strides[2] = {(cuuint64_t)ny * 4, (cuuint64_t)nx * ny * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 2};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int num_sms() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 1;
+  }
+  return n;
+}
+
+constexpr size_t kFwdSmem = 2 * (size_t)(kHaloFloats + kOwnFloats) * 4 + 16 + 128;
+constexpr size_t kAdjSmem = 2 * (size_t)(2 * kHaloFloats + kOwnFloats) * 4 + 16 + 128;
+
+cudaError_t set_smem() {
+  static std::once_flag once;
+  static cudaError_t result = cudaSuccess;
+  std::call_once(once, [] {
+    result = cudaFuncSetAttribute(tma_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+    if (result == cudaSuccess)
+      result = cudaFuncSetAttribute(tma_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAdjSmem);
+  });
+  return result;
+}
+
+}  // namespace
+
+cudaError_t wait_selftest(int* status_host, cudaStream_t st) {
+  const int zero = 0;
+  cudaError_t e = cudaMemcpyToSymbolAsync(g_selftest_status, &zero, sizeof(int), 0,
+                                          cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  int* dev_status = nullptr;
+  if ((e = cudaGetSymbolAddress(reinterpret_cast<void**>(&dev_status), g_selftest_status)) != cudaSuccess)
+    return e;
+  if ((e = tracked_launch(kProfOther, st, [&] { wait_selftest_kernel<<<1, 32, 0, st>>>(dev_status); })) !=
+      cudaSuccess)
+    return e;
+  if ((e = cudaMemcpyFromSymbolAsync(status_host, g_selftest_status, sizeof(int), 0,
+                                     cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  return cudaStreamSynchronize(st);
+}
+
+bool tma_eligible(int mode, int nx, int ny, int S) {
+  (void)nx;
+  (void)S;
+  return mode == kModeScalar && ny % 4 == 0 && encode_fn() != nullptr;
+}
+
+size_t tma_tiles(int nx, int ny, int S) {
+  return (size_t)S * ((nx + kTX - 1) / kTX) * ((ny + kTY - 1) / kTY);
+}
+
+namespace {
+inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+}  // namespace
+
+// Steps the tiled kernel cannot take (u^i == 0 at the first step, buffers
+// not on 16-byte boundaries) run on the first per-step kernel instead.
+cudaError_t launch_tma_fwd(const FwdStep& a, int* err, cudaStream_t st) {
+  const bool ok = a.cur != nullptr && a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) &&
+                  al16(a.copy0) && al16(a.copy1) && (a.frame < 0 || (al16(a.hist_x) && al16(a.hist_y)));
+  CUtensorMap cur_map, prev_map;
+  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
+      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, a.S, kTY, kTX))
+    return launch_fwd_step(kModeScalar, a, st);
+  cudaError_t e = set_smem();
+  if (e != cudaSuccess) return e;
+  const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
+  const int ntiles = a.S * tiles_x * tiles_y;
+  int grid = num_sms() * 3;
+  if (grid > ntiles) grid = ntiles;
+  const double cells = (double)a.S * a.nx * a.ny;
+  return tracked_launch(kProfForward, st, [&] {
+    tma_fwd_kernel<<<grid, kThreads, kFwdSmem, st>>>(a, cur_map, prev_map, tiles_x, tiles_y,
+                                                     a.prev ? 1 : 0, err);
+  }, cells * alg_bytes_forward(kModeScalar));
+}
+
+cudaError_t launch_tma_adj(const AdjStep& a, int* err, cudaStream_t st) {
+  const bool ok = a.ny % 4 == 0 && a.cur != nullptr && a.prev != nullptr && al16(a.cur) &&
+                  al16(a.prev) && al16(a.out) && al16(a.u) &&
+                  (a.frame < 0 || a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
+  CUtensorMap cur_map, prev_map, u_map;
+  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
+      !make_map(&prev_map, a.prev, a.nx, a.ny, a.S, kTY, kTX) ||
+      !make_map(&u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, kBW, kBH))
+    return launch_adj_step(kModeScalar, a, st);
+  cudaError_t e = set_smem();
+  if (e != cudaSuccess) return e;
+  const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
+  const int ntiles = a.S * tiles_x * tiles_y;
+  int grid = num_sms() * 2;
+  if (grid > ntiles) grid = ntiles;
+  const double cells = (double)a.S * a.nx * a.ny;
+  return tracked_launch(kProfAdjoint, st, [&] {
+    tma_adj_kernel<<<grid, kThreads, kAdjSmem, st>>>(a, cur_map, prev_map, u_map, tiles_x, tiles_y,
+                                                     a.u ? 1 : 0, err);
+  }, cells * alg_bytes_adjoint(kModeScalar));
+}
+
+}  // namespace ernn

@@ -49,6 +49,7 @@ class Workload:
     gaussian_param: float = 5e6
     D_true: np.ndarray | None = None
     extra: dict = field(default_factory=dict)
+    path: int = 0              # kernel path of the library (PATH_AUTO by default)
 
     @property
     def nshots(self):
@@ -119,7 +120,7 @@ def geometry(w: Workload, device, nt=None) -> Geometry:
     return Geometry(nx=w.nx, ny=w.ny, nt=nt, h=H, dt=DT,
                     src_signal=torch.tensor(np.repeat(sig[None], S, 0), device=device),
                     src_map=smap, src_origin=origin, stride=w.stride, src_comp=1, rec_idx=rec,
-                    ckpt_k=w.ckpt_k)
+                    ckpt_k=w.ckpt_k, path=w.path)
 
 
 def observed(w: Workload, geom: Geometry, device, noise=0.005, seed=0):

@@ -38,8 +38,9 @@ class Geometry:
     rec_idx:    (S, R) int32 flat receiver cells (i*ny + j), or None for the
                 dense history of the reference.
     ckpt_k:     checkpoint interval in steps (>= nt keeps every state).
-    path:       PATH_AUTO (cluster-resident when the problem fits, else one
-                kernel per step), PATH_STEP or PATH_RESIDENT.
+    path:       PATH_AUTO (cluster-resident when the problem fits, else the
+                tiled TMA kernels when eligible, else one plain kernel per
+                step), PATH_STEP, PATH_RESIDENT or PATH_TILED.
     """
     nx: int
     ny: int
@@ -153,6 +154,53 @@ def _require_cuda(*ts):
                                "libernn_gb300.so; there is no CPU path")
 
 
+class _DeviceStatus:
+    """Error words of the device-side waits (ERNN_ERR_TIMEOUT when a bounded
+    wait gave up), read back without stalling the stream: after each call a
+    4-byte copy into pinned memory is enqueued with an event behind it, and the
+    word is examined once the event has completed — at the next call, or in
+    check_device_status(), which waits for it.  Calls made while a CUDA graph
+    is being captured are not tracked."""
+
+    def __init__(self):
+        self.pending = []
+
+    def enqueue(self, fn: str, prob, workspace: torch.Tensor, is_scratch: int) -> None:
+        if torch.cuda.is_current_stream_capturing():
+            return
+        buf = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+        rc = _lib.load().ernn_device_status(ctypes.byref(prob), _ptr(workspace), is_scratch,
+                                            ctypes.c_void_p(buf.data_ptr()), _stream())
+        _lib.check("ernn_device_status", rc)
+        ev = torch.cuda.Event()
+        ev.record()
+        self.pending.append((fn, buf, ev))
+
+    def poll(self, wait: bool = False) -> None:
+        keep = []
+        for fn, buf, ev in self.pending:
+            if wait:
+                ev.synchronize()
+            elif not ev.query():
+                keep.append((fn, buf, ev))
+                continue
+            code = int(buf[0])
+            if code != 0:
+                self.pending = []
+                raise _lib.ErnnError(fn + " (device-side)", code,
+                                     _lib.load().ernn_error_string(code).decode())
+        self.pending = keep
+
+
+_STATUS = _DeviceStatus()
+
+
+def check_device_status() -> None:
+    """Wait for the status words of all earlier calls and raise ErnnError if a
+    bounded device-side wait of any of them gave up."""
+    _STATUS.poll(wait=True)
+
+
 class ErnnPropagate(torch.autograd.Function):
     """(C, D, rho) -> (out_ux, out_uy) through the fused CUDA time loop.
 
@@ -180,6 +228,7 @@ class ErnnPropagate(torch.autograd.Function):
         if D is not None and tuple(D.shape) != (geom.nx, geom.ny):
             raise ValueError("D must be (nx, ny)")
         geom.check(dev)
+        _STATUS.poll()
         lib = _lib.load()
         if geom.ckpt_k is None:
             geom.ckpt_k = choose_ckpt_k(geom, mode, dev)
@@ -195,6 +244,7 @@ class ErnnPropagate(torch.autograd.Function):
                                   _ptr(out_uy), _ptr(tape), ctypes.c_size_t(tape_bytes),
                                   int(want_grad), _stream())
             _lib.check("ernn_forward", rc)
+            _STATUS.enqueue("ernn_forward", prob, tape, 0)
         ctx.geom = geom
         ctx.mode = mode
         ctx.tape = tape if want_grad else None
@@ -229,6 +279,7 @@ class ErnnPropagate(torch.autograd.Function):
                                   _ptr(scratch), ctypes.c_size_t(scratch_bytes), _ptr(grad_C64),
                                   _ptr(grad_field), _stream())
             _lib.check("ernn_adjoint", rc)
+            _STATUS.enqueue("ernn_adjoint", prob, scratch, 1)
         if mode == MODE_SCALAR:
             return grad_C64.to(torch.float32), None, None, None, None
         if mode == MODE_FIELDS:

@@ -56,11 +56,15 @@ enum {
 };
 
 enum {
-  ERNN_PATH_AUTO = 0,     /* cluster-resident when the problem fits, else per-step */
+  ERNN_PATH_AUTO = 0,     /* cluster-resident when the problem fits, else tiled when
+                             eligible, else per-step */
   ERNN_PATH_STEP = 1,     /* one fused kernel launch per time step (any size, any mode) */
-  ERNN_PATH_RESIDENT = 2  /* one thread-block cluster per shot holds the state in
+  ERNN_PATH_RESIDENT = 2, /* one thread-block cluster per shot holds the state in
                              distributed shared memory for all steps (scalar constants,
                              ny % 4 == 0, state small enough); ERNN_ERR_UNSUPPORTED otherwise */
+  ERNN_PATH_TILED = 3     /* one launch per time step of persistent CTAs that stream
+                             64 x 32 tiles through TMA loads (scalar constants,
+                             ny % 4 == 0); ERNN_ERR_UNSUPPORTED otherwise */
 };
 
 /* One propagation problem.  Plain data; identical layout in C, C++, ctypes. */
@@ -173,6 +177,28 @@ int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, float* out_u
 /* Number of kernels this library has launched since it was loaded. (host call)
  * Diagnostic; no counterpart in the reference. */
 uint64_t ernn_launch_count(void);
+
+/* Device-side status of the last call that used `workspace`: the tape of
+ * ernn_forward (is_scratch == 0) or the scratch of ernn_adjoint
+ * (is_scratch == 1), for problem `p`.  Enqueues on `stream` a 4-byte
+ * device-to-host copy into *status_host (pinned host memory keeps it
+ * asynchronous); once the stream has passed it, the word is ERNN_OK, or
+ * ERNN_ERR_TIMEOUT when a bounded device-side wait of that call gave up (its
+ * outputs are then not valid).  No counterpart in the reference. */
+int ernn_device_status(const ErnnProblem* p, const void* workspace, int is_scratch,
+                       int32_t* status_host, void* stream);
+
+/* Failure path of the device-side waits, without a fault: one CTA waits on a
+ * barrier that nothing completes, with the same bounded wait as the
+ * propagation kernels, gives up after about a second and records
+ * ERNN_ERR_TIMEOUT; that word is copied into *status_host and `stream` is
+ * synchronised.  The context stays usable.  No counterpart in the reference. */
+int ernn_wait_selftest(int32_t* status_host, void* stream);
+
+/* ERNN_PATH_STEP, _RESIDENT or _TILED: the kernels that ran the time loop of
+ * the last ernn_forward / ernn_adjoint call of this process (ERNN_PATH_AUTO
+ * before any call). (host call)  Diagnostic; no counterpart in the reference. */
+int32_t ernn_last_path(void);
 
 /* Diagnostic kernel timing (no counterpart in the reference): while enabled,
  * every launch of the library is bracketed by CUDA events on its stream.

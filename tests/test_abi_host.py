@@ -56,7 +56,7 @@ def test_validation_rejects_bad_problems():
     assert lib.ernn_validate(ctypes.byref(_problem())) == 0
     bad = [dict(nx=0), dict(nt=0), dict(stride=0), dict(mode=3), dict(record=2),
            dict(nrec=0), dict(src_comp=2), dict(h=0.0), dict(dt=-1.0), dict(ckpt_k=0),
-           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=3), dict(reserved=1)]
+           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=4), dict(path=-1), dict(reserved=1)]
     for kw in bad:
         assert lib.ernn_validate(ctypes.byref(_problem(**kw))) == 1, kw
     assert lib.ernn_validate(None) == 1
@@ -143,3 +143,15 @@ def test_product_path_refuses_cpu_tensors():
                       src_map=torch.zeros(1, 2, 2), src_origin=torch.zeros(1, 2, dtype=torch.int32))
     with pytest.raises(RuntimeError, match="CUDA"):
         E.propagate(torch.ones(6), torch.tensor(1.0), geom)
+
+
+def test_device_status_validates_before_any_device_call():
+    lib = E._lib.load()
+    p = _problem()
+    st = ctypes.c_int32(0)
+    assert lib.ernn_device_status(None, ctypes.c_void_p(16), 0, ctypes.byref(st), None) == 1
+    assert lib.ernn_device_status(ctypes.byref(p), None, 0, ctypes.byref(st), None) == 1
+    assert lib.ernn_device_status(ctypes.byref(p), ctypes.c_void_p(16), 2, ctypes.byref(st), None) == 1
+    assert lib.ernn_device_status(ctypes.byref(p), ctypes.c_void_p(16), 0, None, None) == 1
+    assert lib.ernn_wait_selftest(None, None) == 1
+    assert lib.ernn_last_path() in (0, 1, 2, 3)

@@ -4,7 +4,9 @@ Tolerances (stated by the benchmark spec): forward relative L2 error
 <= 1e-4 against the FP64 run of the same scheme, gradient relative error
 <= 1e-4.  The FP32 CUDA path typically lands near 1e-6.
 """
+import ctypes
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -103,7 +105,49 @@ def test_resident_path_vs_fp64_oracle(name):
     assert rel(gg, rg) <= GRAD_TOL, rel(gg, rg)
 
 
-@pytest.mark.parametrize("path", [E.PATH_STEP, E.PATH_RESIDENT])
+# scalar-constant cases with ny % 4 == 0 on the tiled (TMA) per-step kernels:
+# tiles of 64 columns x 32 rows, ragged edges in both directions, tile
+# boundaries through the source box and through receiver cells
+TILED_CASES = {
+    "dense_ragged": dict(nx=45, ny=76),
+    "receivers_multishot": dict(nx=70, ny=132, record=O.RECORD_RECEIVERS, S=3, nrec=40),
+    "x_force_stride1": dict(nx=33, ny=68, nt=70, stride=1, src_comp=0),
+    "duplicate_receivers": dict(nx=40, ny=64, record=O.RECORD_RECEIVERS, nrec=6, dup_receiver=True),
+    "narrow": dict(nx=150, ny=8, nt=90, stride=5),
+    "single_tile": dict(nx=32, ny=64, nt=60),
+    "tiny": dict(nx=3, ny=4, nt=30, box=2),
+    "many_tiles": dict(nx=130, ny=260, nt=50, S=2, record=O.RECORD_RECEIVERS, nrec=30),
+}
+
+
+@pytest.mark.parametrize("name", list(TILED_CASES))
+def test_tiled_path_vs_fp64_oracle(name):
+    case = random_case(**TILED_CASES[name])
+    wx, wy = weights(case)
+    gx, gy, gg = run_gpu(case, wx, wy, path=E.PATH_TILED)
+    rx, ry, rg = run_oracle(case, wx, wy)
+    assert rel(gx, rx) <= FWD_TOL and rel(gy, ry) <= FWD_TOL, (rel(gx, rx), rel(gy, ry))
+    assert rel(gg, rg) <= GRAD_TOL, rel(gg, rg)
+
+
+def test_tiled_forward_matches_step_forward():
+    # same terms in the same order; the compilers' fused multiply-adds differ
+    # between the two kernels, so the states agree to FP32 rounding
+    case = random_case(nx=70, ny=132, nt=80, S=2, stride=3)
+    wx, wy = weights(case)
+    a = run_gpu(case, wx, wy, path=E.PATH_STEP)
+    b = run_gpu(case, wx, wy, path=E.PATH_TILED)
+    assert rel(a[0], b[0]) <= 1e-5 and rel(a[1], b[1]) <= 1e-5, (rel(a[0], b[0]), rel(a[1], b[1]))
+
+
+def test_tiled_path_rejects_unsupported_problem():
+    case = random_case(nx=20, ny=18, nt=10)  # ny % 4 != 0
+    wx, wy = weights(case)
+    with pytest.raises(E._lib.ErnnError):
+        run_gpu(case, wx, wy, path=E.PATH_TILED)
+
+
+@pytest.mark.parametrize("path", [E.PATH_STEP, E.PATH_RESIDENT, E.PATH_TILED])
 @pytest.mark.parametrize("k", [1, 2, 7, 50, 119, 120, 1000])
 def test_checkpoint_interval_does_not_change_results(k, path):
     case = random_case(nt=120, S=2, ny=32, record=O.RECORD_RECEIVERS)
@@ -112,7 +156,7 @@ def test_checkpoint_interval_does_not_change_results(k, path):
     got = run_gpu(case, wx, wy, ckpt_k=k, path=path)
     # recomputation replays the identical kernels: bit-identical forward outputs
     assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
-    if path == E.PATH_STEP:
+    if path != E.PATH_RESIDENT:
         assert np.array_equal(ref[2], got[2])
     else:
         # the resident path flushes its FP32 partial sums to FP64 at segment
@@ -120,17 +164,18 @@ def test_checkpoint_interval_does_not_change_results(k, path):
         assert rel(got[2], ref[2]) <= 1e-6
 
 
-def test_resident_and_step_paths_agree():
+def test_resident_tiled_and_step_paths_agree():
     case = random_case(nx=64, ny=64, nt=150, S=2, record=O.RECORD_RECEIVERS, nrec=16)
     wx, wy = weights(case)
     a = run_gpu(case, wx, wy, ckpt_k=30, path=E.PATH_STEP)
-    b = run_gpu(case, wx, wy, ckpt_k=30, path=E.PATH_RESIDENT)
     r = run_oracle(case, wx, wy)
-    for x, y, z in zip(a, b, r):
-        # each path against the FP64 run; the two FP32 paths sum the imaging
-        # products in different orders, so they agree to that rounding
-        assert rel(x, z) <= 2e-5 and rel(y, z) <= 2e-5, (rel(x, z), rel(y, z))
-        assert rel(x, y) <= 4e-5
+    for path in (E.PATH_RESIDENT, E.PATH_TILED):
+        b = run_gpu(case, wx, wy, ckpt_k=30, path=path)
+        for x, y, z in zip(a, b, r):
+            # each path against the FP64 run; the FP32 paths sum the imaging
+            # products in different orders, so they agree to that rounding
+            assert rel(x, z) <= 2e-5 and rel(y, z) <= 2e-5, (rel(x, z), rel(y, z))
+            assert rel(x, y) <= 4e-5
 
 
 def test_resident_path_rejects_unsupported_problem():
@@ -284,3 +329,29 @@ def test_launch_counter_counts_kernels():
     n0 = lib.ernn_launch_count()
     run_gpu(case, wx, wy, path=E.PATH_RESIDENT)    # one launch per pass
     assert 3 <= lib.ernn_launch_count() - n0 < 20
+
+
+def test_bounded_wait_gives_up_and_context_survives():
+    # a device-side wait that nothing completes returns ERNN_ERR_TIMEOUT after
+    # about a second instead of hanging; the context stays usable afterwards
+    lib = E._lib.load()
+    status = ctypes.c_int32(-1)
+    rc = lib.ernn_wait_selftest(ctypes.byref(status), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0 and status.value == 5, (rc, status.value)
+    case = random_case(nx=40, ny=64, nt=40)
+    wx, wy = weights(case)
+    gx, gy, gg = run_gpu(case, wx, wy, path=E.PATH_TILED)
+    rx, ry, rg = run_oracle(case, wx, wy)
+    assert rel(gx, rx) <= FWD_TOL and rel(gg, rg) <= GRAD_TOL
+    E.check_device_status()  # the status words of those calls are clear
+
+
+@pytest.mark.parametrize("path", [E.PATH_STEP, E.PATH_RESIDENT, E.PATH_TILED])
+def test_device_status_word_is_clear_after_calls(path):
+    case = random_case(nx=32, ny=32, nt=30, record=O.RECORD_RECEIVERS)
+    wx, wy = weights(case)
+    run_gpu(case, wx, wy, path=path)
+    status = sys.modules[E.ErnnPropagate.__module__]._STATUS
+    E.check_device_status()
+    assert status.pending == []
+    assert E._lib.load().ernn_last_path() == path
