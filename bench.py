@@ -294,6 +294,14 @@ def run_ernn(args, dist):
     torch.cuda.synchronize()
     prof = E._lib.profile_read()
     E._lib.profile(False)
+    per_class = {}
+    for c in ("forward", "adjoint"):
+        t_ms, n_l, b_tot = prof[c]
+        if n_l:
+            us = t_ms * 1e3 / n_l
+            gbs = b_tot / n_l / (us * 1e-6) / 1e9
+            per_class[c] = {"launches": n_l, "us_per_launch": round(us, 3), "ms_total": round(t_ms, 3),
+                            "achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks()[0], 4)}
     cls = max(("forward", "adjoint"), key=lambda c: prof[c][0])
     tot_ms, nlaunch, tot_bytes = prof[cls]
     per_launch_ms = tot_ms / max(nlaunch, 1)
@@ -342,7 +350,7 @@ def run_ernn(args, dist):
                      "frac": round(achieved / peak, 4),
                      "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
                      "launch_us": round(per_launch_ms * 1e3, 3), "launches_per_iter": nlaunch,
-                     "note": l2_note},
+                     "note": l2_note, "classes": per_class},
         "clocks": clk,
         "loss": float(inv.step().item()),
     }

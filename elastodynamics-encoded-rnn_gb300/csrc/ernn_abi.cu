@@ -29,7 +29,7 @@ struct Plan {
   // tape
   size_t t_coef, t_A, t_B, t_store, t_total_tape, t_total_notape;
   // adjoint scratch
-  size_t s_coef, s_LA, s_LB, s_seg, s_lbuf, s_gacc, s_part, s_total;
+  size_t s_coef, s_LA, s_LB, s_seg, s_lbuf, s_gacc, s_part, s_tflags, s_total;
 };
 
 Plan make_plan(const ErnnProblem& p) {
@@ -70,6 +70,9 @@ Plan make_plan(const ErnnProblem& p) {
   // imaging CTA (at most 8 clusters of 16 per shot)
   pl.npart = pl.nblocks > p.nshots * 16 * 8 ? pl.nblocks : p.nshots * 16 * 8;
   if (p.mode == kModeScalar) off += align_up((size_t)pl.npart * 8 * sizeof(double));
+  // receiver table of the tiled adjoint: one byte per (shot, 64 x 32 tile)
+  pl.s_tflags = off;
+  if (p.record == kRecordReceivers) off += align_up(tma_tiles(p.nx, p.ny, p.nshots));
   pl.s_total = off;
   return pl;
 }
@@ -130,7 +133,11 @@ std::atomic<int32_t> g_last_path{ERNN_PATH_AUTO};
 
 // Tiled per-step kernels: requested (ERNN_PATH_TILED, an error when the
 // problem is not eligible) or chosen by ERNN_PATH_AUTO when eligible and one
-// step has at least one tile per SM.
+// step has at least four 64 x 32 tiles per SM.  The tiled kernels are
+// persistent (2-3 CTAs of 72-111 KB shared memory per SM, each streaming
+// several tiles); below that size the plain per-step kernels, many small
+// CTAs per SM, hide latency better and share the GPU better with other
+// streams' work.
 int use_tiled(const ErnnProblem& p, int* tiled) {
   *tiled = 0;
   if (p.path == ERNN_PATH_STEP) return ERNN_OK;
@@ -144,7 +151,7 @@ int use_tiled(const ErnnProblem& p, int* tiled) {
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return ERNN_ERR_CUDA;
-  *tiled = ok && tma_tiles(p.nx, p.ny, p.nshots) >= (size_t)sms;
+  *tiled = ok && tma_tiles(p.nx, p.ny, p.nshots) >= 4 * (size_t)sms;
   return ERNN_OK;
 }
 
@@ -366,7 +373,7 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
   if ((rc = use_tiled(*p, &tiled))) return rc;
   g_last_path.store(tiled ? ERNN_PATH_TILED : ERNN_PATH_STEP, std::memory_order_relaxed);
   auto fwd_step = [&](const FwdStep& s) {
-    return tiled ? launch_tma_fwd(s, &coef->err, st) : launch_fwd_step(p->mode, s, st);
+    return tiled ? launch_tma_fwd(p->mode, s, &coef->err, st) : launch_fwd_step(p->mode, s, st);
   };
 
   const bool store_all = with_tape && pl.store_all;
@@ -438,7 +445,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   float* gacc = fat(scratch, pl.s_gacc);
   double* partials = reinterpret_cast<double*>(at(scratch, pl.s_part));
   if (p->mode != kModeScalar) ERNN_CUDA(cudaMemsetAsync(gacc, 0, pl.s_part - pl.s_gacc, st));
-  else ERNN_CUDA(cudaMemsetAsync(partials, 0, pl.s_total - pl.s_part, st));
+  else ERNN_CUDA(cudaMemsetAsync(partials, 0, pl.s_tflags - pl.s_part, st));
 
   if (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT) {
     ResCommon res;
@@ -473,6 +480,12 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   b.nt_out = pl.nt_out; b.record = p->record; b.nrec = p->nrec; b.rec_idx = in->rec_idx;
   b.partials = partials;
   b.gacc = gacc;
+  b.tile_flags = nullptr;
+  if (tiled && p->record == kRecordReceivers) {
+    uint8_t* flags = reinterpret_cast<uint8_t*>(at(scratch, pl.s_tflags));
+    ERNN_CUDA(launch_tile_flags(in->rec_idx, p->nshots, p->nrec, p->nx, p->ny, flags, st));
+    b.tile_flags = flags;
+  }
 
   auto adj_step = [&](int m, const float* um) -> int {
     const int idx = p->nt - m;
@@ -482,7 +495,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     b.prev = b.out;
     b.u = (m <= p->nt - 1) ? um : nullptr;
     b.frame = ((m - 1) % p->stride == 0) ? (m - 1) / p->stride : -1;
-    const cudaError_t e = tiled ? launch_tma_adj(b, &coef->err, st) : launch_adj_step(p->mode, b, st);
+    const cudaError_t e = tiled ? launch_tma_adj(p->mode, b, &coef->err, st) : launch_adj_step(p->mode, b, st);
     return e == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
   };
 
@@ -501,7 +514,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
         a.out = seg(i - i0);
         a.cur = (i == i0) ? ck(j, 0) : seg(i - i0 - 1);
         a.prev = (i == i0) ? ck(j, 1) : (i == i0 + 1 ? ck(j, 0) : seg(i - i0 - 2));
-        ERNN_CUDA(tiled ? launch_tma_fwd(a, &coef->err, st) : launch_fwd_step(p->mode, a, st));
+        ERNN_CUDA(tiled ? launch_tma_fwd(p->mode, a, &coef->err, st) : launch_fwd_step(p->mode, a, st));
       }
       for (int m = i1; m >= i0 + 1; --m)
         if ((rc = adj_step(m, seg(m - 1 - i0)))) return rc;

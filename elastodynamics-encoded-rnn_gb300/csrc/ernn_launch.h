@@ -54,6 +54,9 @@ struct AdjStep {
   const int32_t* rec_idx;
   double* partials;   // SCALAR: [block][8] FP64 running sums
   float* gacc;        // DFIELD: [S][N]; FIELDS: [S][6][N] running sums
+  // tiled kernels: non-zero for the 64 x 32 tiles (shot-major) holding a
+  // receiver, or nullptr (every tile scans the receivers)
+  const uint8_t* tile_flags;
 };
 
 dim3 step_grid(int nx, int ny, int S);

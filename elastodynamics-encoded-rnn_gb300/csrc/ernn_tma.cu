@@ -12,7 +12,8 @@
 // outside the grid are filled with zeros by the copy engine: that is the
 // zero ghost ring of the scheme, with no predicated loads.
 //
-// Scalar constants (ERNN_MODE_SCALAR), ny % 4 == 0.
+// Scalar constants (ERNN_MODE_SCALAR) and the degradation map (ERNN_MODE_DFIELD),
+// ny % 4 == 0.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -78,6 +79,19 @@ __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int
       " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(s32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(s32(b))
       : "memory");
+}
+
+// End of a warp's reads of stage k & 1: the last of the CTA's warps to get
+// there starts the loads of tile k + 2 into it, so no warp waits on the
+// others between tiles.  The values read from the stage are all consumed
+// (in registers) before a lane arrives.
+template <typename F>
+__device__ __forceinline__ void release(int* done, int k, F&& refill) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) {
+    const int old = atomicAdd(&done[k & 1], 1);
+    if (old % (kThreads / 32) == kThreads / 32 - 1) refill();
+  }
 }
 
 // TMA destinations start on 128-byte boundaries: the dynamic shared block is
@@ -159,7 +173,24 @@ __device__ __forceinline__ TileId tile_of(int t, int tiles_x, int tiles_y) {
   return id;
 }
 
+// 2D tile load (columns, rows) into shared memory: the degradation plane.
+__device__ __forceinline__ void tma_load2(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(s32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(s32(b))
+      : "memory");
+}
+
+__device__ __forceinline__ float4 one_minus(const float4 d) {
+  return make_float4(1.f - d.x, 1.f - d.y, 1.f - d.z, 1.f - d.w);
+}
+
 // ----------------------------------------------------------------- forward
+// Stage: halo box of u^i, own box of u^{i-1}.  DFIELD reads its 4 weights
+// per row straight from global memory (one plane shared by every shot, L2
+// resident).
+template <int MODE>
 __global__ void __launch_bounds__(kThreads, 3)
     tma_fwd_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, int tiles_x, int tiles_y, int has_prev,
@@ -185,9 +216,11 @@ __global__ void __launch_bounds__(kThreads, 3)
       a.tr_y[o] = ok ? a.cur[(size_t)s * 2 * N + N + idx] : 0.f;
     }
   }
+  __shared__ int done[2];
   if (tid == 0) {
     bar_init(&bar[0]);
     bar_init(&bar[1]);
+    done[0] = done[1] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -204,23 +237,36 @@ __global__ void __launch_bounds__(kThreads, 3)
     tma_load3(st, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
     if (has_prev) tma_load3(st + kHaloFloats, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
   };
-  if (tid == 0) issue(0);
+  if (tid == 0) {
+    issue(0);
+    issue(1);
+  }
   const int qc = tid & 15, rg = tid >> 4;
   const int j = 4 * qc;
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    if (tid == 0) issue(k + 1);
-    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
     const TileId id = tile_of(t, tiles_x, tiles_y);
-    const float* hb = sm + (k & 1) * kStage;
-    const float* pb = hb + kHaloFloats;
+    // per-tile scalars, loaded before the wait
     const float amp = a.src_signal[(size_t)id.shot * a.nt + a.i] * kappa;
     const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
-    float* out = a.out + (size_t)id.shot * 2 * N;
     const int gj = id.y0 + j;
-    float wx[3][6], wy[3][6];
     const int r0 = 2 * rg;  // tile rows r0, r0 + 1 -> box rows r0 + 1, r0 + 2
+    float4 w4[2];
+    if (MODE == kModeDField) {  // issued before the wait: overlaps the tile's loads
+#pragma unroll
+      for (int q2 = 0; q2 < 2; ++q2) {
+        const int gi = id.x0 + r0 + q2;
+        w4[q2] = (gi < nx && gj < ny)
+                     ? one_minus(__ldg(reinterpret_cast<const float4*>(a.field + (size_t)gi * ny + gj)))
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
+    const float* hb = sm + (k & 1) * kStage;
+    const float* pb = hb + kHaloFloats;
+    float* out = a.out + (size_t)id.shot * 2 * N;
+    float wx[3][6], wy[3][6];
     win(hb, r0, j, wx[0]);
     win(hb + kBH * kBW, r0, j, wy[0]);
     win(hb, r0 + 1, j, wx[1]);
@@ -244,6 +290,10 @@ __global__ void __launch_bounds__(kThreads, 3)
         for (int q = 0; q < 4; ++q) {
           float lx, ly;
           apply(ks, st, q, lx, ly);
+          if (MODE == kModeDField) {
+            lx *= g4(w4[q2], q);
+            ly *= g4(w4[q2], q);
+          }
           vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
           vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
           if (has_src) {
@@ -276,28 +326,46 @@ __global__ void __launch_bounds__(kThreads, 3)
       shift(wx);
       shift(wy);
     }
-    __syncthreads();  // stage k & 1 is free for the loads of tile k + 2
+    release(done, k, [&] { issue(k + 2); });
   }
 }
 
 // ----------------------------------------------------------------- adjoint
+// Stage (SCALAR): halo box of lam^{m+1}, own box of lam^{m+2}, halo box of
+// u^m.  Stage (DFIELD): halo boxes of lam^{m+1}, u^m and D; lam^{m+2} is read
+// into registers straight from global memory before the wait (keeps two
+// CTAs per SM within shared memory).
+template <int MODE>
+struct AdjLayout {
+  static constexpr int kLam = 0;
+  static constexpr int kPrev = kHaloFloats;  // SCALAR only
+  static constexpr int kU = (MODE == kModeScalar) ? kHaloFloats + kOwnFloats : kHaloFloats;
+  static constexpr int kD = kU + kHaloFloats;  // DFIELD only
+  static constexpr int kEnd = (MODE == kModeScalar) ? kU + kHaloFloats : kD + kBH * kBW;
+  static constexpr int kStage = (kEnd + 31) / 32 * 32;  // 128-byte multiple
+};
+
+template <int MODE>
 __global__ void __launch_bounds__(kThreads, 2)
     tma_adj_kernel(const AdjStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap u_map,
-                   int tiles_x, int tiles_y, int has_u, int* err) {
+                   const __grid_constant__ CUtensorMap d_map, int tiles_x, int tiles_y, int has_u, int* err) {
+  using L = AdjLayout<MODE>;
   extern __shared__ float sm_raw[];
   float* sm = aligned128(sm_raw);
-  constexpr int kStage = 2 * kHaloFloats + kOwnFloats;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * kStage);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * L::kStage);
   __shared__ double red[kThreads / 32][6];
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
   const int ntiles = a.S * tiles_x * tiles_y;
-  const uint32_t bytes = (uint32_t)(kHaloFloats + kOwnFloats + (has_u ? kHaloFloats : 0)) * 4u;
+  const uint32_t bytes =
+      (uint32_t)(kHaloFloats + (MODE == kModeScalar ? kOwnFloats : kBH * kBW) + (has_u ? kHaloFloats : 0)) * 4u;
+  __shared__ int done[2];
   if (tid == 0) {
     bar_init(&bar[0]);
     bar_init(&bar[1]);
+    done[0] = done[1] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -307,31 +375,55 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) return;
     const TileId id = tile_of(t, tiles_x, tiles_y);
-    float* st = sm + (k & 1) * kStage;
+    float* st = sm + (k & 1) * L::kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
-    tma_load3(st, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
-    tma_load3(st + kHaloFloats, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
-    if (has_u) tma_load3(st + kHaloFloats + kOwnFloats, &u_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+    tma_load3(st + L::kLam, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+    if (MODE == kModeScalar)
+      tma_load3(st + L::kPrev, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
+    else
+      tma_load2(st + L::kD, &d_map, id.y0 - 4, id.x0 - 1, &bar[k & 1]);
+    if (has_u) tma_load3(st + L::kU, &u_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
   };
-  if (tid == 0) issue(0);
+  if (tid == 0) {
+    issue(0);
+    issue(1);
+  }
   const int qc = tid & 15, rg = tid >> 4;
   const int j = 4 * qc;
-  // imaging sums: FP32 over a thread's 8 cells of a tile, accumulated over
-  // tiles as FP32 pairs (TwoSum), FP64 across threads and launches
+  const bool inject = a.frame >= 0 && a.record == kRecordReceivers;
+  // imaging sums (SCALAR): FP32 over a thread's 8 cells of a tile,
+  // accumulated over tiles as FP32 pairs (TwoSum), FP64 across threads and
+  // launches
   float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    if (tid == 0) issue(k + 1);
-    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
     const TileId id = tile_of(t, tiles_x, tiles_y);
-    float* hb = sm + (k & 1) * kStage;
-    float* pb = hb + kHaloFloats;
-    const float* ub = pb + kOwnFloats;
-    // adjoint source at receiver cells: subtract it from this tile's copy of
-    // lam^{m+2} (lam^m = ... - lam^{m+2} + ... + g)
-    if (a.frame >= 0 && a.record == kRecordReceivers) {
+    const int gj = id.y0 + j;
+    const int r0 = 2 * rg;
+    // receivers in this tile (uniform over the CTA): the injection and its
+    // barriers only run where the per-call table says there are some
+    const bool tile_inject = inject && (a.tile_flags == nullptr || a.tile_flags[t] != 0);
+    float4 pv[2][2];  // DFIELD: lam^{m+2} of rows r0, r0 + 1 (x, y)
+    if (MODE == kModeDField) {
+#pragma unroll
+      for (int q2 = 0; q2 < 2; ++q2) {
+        const int gi = id.x0 + r0 + q2;
+        const size_t o = (size_t)id.shot * 2 * N + (size_t)gi * ny + gj;
+        const bool in = gi < nx && gj < ny;
+        pv[q2][0] = in ? *reinterpret_cast<const float4*>(a.prev + o) : make_float4(0.f, 0.f, 0.f, 0.f);
+        pv[q2][1] = in ? *reinterpret_cast<const float4*>(a.prev + N + o) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
+    float* hb = sm + (k & 1) * L::kStage;
+    float* pb = hb + L::kPrev;
+    const float* ub = hb + L::kU;
+    const float* db = hb + L::kD;
+    // adjoint source at receiver cells (SCALAR): subtract it from this
+    // tile's copy of lam^{m+2} (lam^m = ... - lam^{m+2} + ... + g)
+    if (MODE == kModeScalar && tile_inject) {
       for (int rr = tid; rr < a.nrec; rr += kThreads) {
         const int32_t idx = a.rec_idx[(size_t)id.shot * a.nrec + rr];
         if (idx < 0 || (size_t)idx >= N) continue;
@@ -345,13 +437,25 @@ __global__ void __launch_bounds__(kThreads, 2)
       __syncthreads();
     }
     float* out = a.out + (size_t)id.shot * 2 * N;
-    const int gj = id.y0 + j;
+    // lam windows for the stencils: weighted by 1 - D in DFIELD (A^T lam =
+    // A0((1 - D) lam)); the centre value itself stays unweighted
+    auto lam_win = [&](int r, float wx_[6], float wy_[6]) {
+      win(hb, r, j, wx_);
+      win(hb + kBH * kBW, r, j, wy_);
+      if (MODE == kModeDField) {
+        float dw[6];
+        win(db, r, j, dw);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+          const float w = 1.f - dw[c];
+          wx_[c] = w * wx_[c];
+          wy_[c] = w * wy_[c];
+        }
+      }
+    };
     float wx[3][6], wy[3][6], vx_[3][6], vy_[3][6];
-    const int r0 = 2 * rg;
-    win(hb, r0, j, wx[0]);
-    win(hb + kBH * kBW, r0, j, wy[0]);
-    win(hb, r0 + 1, j, wx[1]);
-    win(hb + kBH * kBW, r0 + 1, j, wy[1]);
+    lam_win(r0, wx[0], wy[0]);
+    lam_win(r0 + 1, wx[1], wy[1]);
     if (has_u) {
       win(ub, r0, j, vx_[0]);
       win(ub + kBH * kBW, r0, j, vy_[0]);
@@ -362,24 +466,32 @@ __global__ void __launch_bounds__(kThreads, 2)
 #pragma unroll
     for (int q2 = 0; q2 < 2; ++q2) {
       const int r = r0 + q2;
-      win(hb, r + 2, j, wx[2]);
-      win(hb + kBH * kBW, r + 2, j, wy[2]);
+      lam_win(r + 2, wx[2], wy[2]);
       Sums4 st;
       sums4(wx, wy, st);
       const int gi = id.x0 + r;
       const bool in = gi < nx && gj < ny;
+      // unweighted lam^{m+1} at the 4 cells
+      const float4 c1x = *reinterpret_cast<const float4*>(hb + (r + 1) * kBW + j + 4);
+      const float4 c1y = *reinterpret_cast<const float4*>(hb + kBH * kBW + (r + 1) * kBW + j + 4);
+      const size_t o = (size_t)gi * ny + gj;
       if (in) {
-        const float4 pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
-        const float4 pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+        float4 pvx, pvy;
+        if (MODE == kModeScalar) {
+          pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
+          pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+        } else {
+          pvx = pv[q2][0];
+          pvy = pv[q2][1];
+        }
         float vx[4], vy[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           float lx, ly;
           apply(ks, st, q, lx, ly);
-          vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
-          vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
+          vx[q] = (2.f * g4(c1x, q) - g4(pvx, q)) + lx;
+          vy[q] = (2.f * g4(c1y, q) - g4(pvy, q)) + ly;
         }
-        const size_t o = (size_t)gi * ny + gj;
         if (a.frame >= 0 && a.record == kRecordFields) {
           const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * N + o;
           const float4 gx = *reinterpret_cast<const float4*>(a.g_x + go);
@@ -399,15 +511,28 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (in) {
           Sums4 su;
           sums4(vx_, vy_, su);
+          if (MODE == kModeScalar) {
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float l1x = st.cx[q], l1y = st.cy[q];
-            acc[0] += l1x * su.xx_x[q];
-            acc[1] += l1y * su.yy_y[q];
-            acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
-            acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
-            acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
-            acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
+            for (int q = 0; q < 4; ++q) {
+              const float l1x = g4(c1x, q), l1y = g4(c1y, q);
+              acc[0] += l1x * su.xx_x[q];
+              acc[1] += l1y * su.yy_y[q];
+              acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
+              acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
+              acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
+              acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
+            }
+          } else {
+            float* ga = a.gacc + (size_t)id.shot * N + o;
+            float4 g = *reinterpret_cast<const float4*>(ga);
+            float gv[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              float Lx, Ly;
+              apply(ks, su, q, Lx, Ly);
+              gv[q] += g4(c1x, q) * Lx + g4(c1y, q) * Ly;
+            }
+            *reinterpret_cast<float4*>(ga) = make_float4(gv[0], gv[1], gv[2], gv[3]);
           }
         }
         shift(vx_);
@@ -416,16 +541,34 @@ __global__ void __launch_bounds__(kThreads, 2)
       shift(wx);
       shift(wy);
     }
+    if (MODE == kModeScalar) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {  // TwoSum(hi, acc)
-      const float s = hi[q] + acc[q];
-      const float bp = s - hi[q];
-      lo[q] += (hi[q] - (s - bp)) + (acc[q] - bp);
-      hi[q] = s;
+      for (int q = 0; q < 6; ++q) {  // TwoSum(hi, acc)
+        const float s = hi[q] + acc[q];
+        const float bp = s - hi[q];
+        lo[q] += (hi[q] - (s - bp)) + (acc[q] - bp);
+        hi[q] = s;
+      }
     }
-    __syncthreads();  // stage k & 1 is free for the loads of tile k + 2
+    if (MODE == kModeDField && tile_inject) {
+      // adjoint source at receiver cells, added to the stored lam^m (several
+      // receivers may share a cell); the block's own stores are visible
+      // after the barrier
+      __syncthreads();
+      for (int rr = tid; rr < a.nrec; rr += kThreads) {
+        const int32_t idx = a.rec_idx[(size_t)id.shot * a.nrec + rr];
+        if (idx < 0 || (size_t)idx >= N) continue;
+        const int gi = idx / ny, gjj = idx - gi * ny;
+        if (gi >= id.x0 && gi < id.x0 + kTX && gjj >= id.y0 && gjj < id.y0 + kTY) {
+          const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * a.nrec + rr;
+          atomicAdd(out + idx, gs * a.g_x[go]);
+          atomicAdd(out + N + idx, gs * a.g_y[go]);
+        }
+      }
+    }
+    release(done, k, [&] { issue(k + 2); });
   }
-  if (!has_u) return;
+  if (MODE != kModeScalar || !has_u) return;
   const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
@@ -454,6 +597,19 @@ __global__ void wait_selftest_kernel(int* status) {
 }
 
 __device__ int g_selftest_status;
+
+// Receiver table of the tiled adjoint: flags[(shot, tile)] = 1 where the
+// shot has a receiver in the tile.
+__global__ void tile_flags_kernel(const int32_t* __restrict__ rec_idx, int S, int nrec, int nx, int ny,
+                                  int tiles_x, int tiles_y, uint8_t* __restrict__ flags) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= S * nrec) return;
+  const int s = e / nrec;
+  const int32_t idx = rec_idx[e];
+  if (idx < 0 || (int64_t)idx >= (int64_t)nx * ny) return;  // ignored, as in the kernels
+  const int gi = idx / ny, gj = idx - gi * ny;
+  flags[(size_t)s * tiles_x * tiles_y + (size_t)(gi / kTX) * tiles_y + gj / kTY] = 1;
+}
 
 // ----------------------------------------------------------------- host
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -495,16 +651,37 @@ int num_sms() {
   return n;
 }
 
+// Tensor map over the degradation plane [nx][ny]: dims (ny, nx).
+bool make_map2(CUtensorMap* m, const float* base, int nx, int ny, int bw, int bh) {
+  auto fn = encode_fn();
+  if (fn == nullptr || base == nullptr) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)ny, (cuuint64_t)nx};
+  const cuuint64_t strides[1] = {(cuuint64_t)ny * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 constexpr size_t kFwdSmem = 2 * (size_t)(kHaloFloats + kOwnFloats) * 4 + 16 + 128;
-constexpr size_t kAdjSmem = 2 * (size_t)(2 * kHaloFloats + kOwnFloats) * 4 + 16 + 128;
+template <int MODE>
+constexpr size_t adj_smem() {
+  return 2 * (size_t)AdjLayout<MODE>::kStage * 4 + 16 + 128;
+}
 
 cudaError_t set_smem() {
   static std::once_flag once;
   static cudaError_t result = cudaSuccess;
   std::call_once(once, [] {
-    result = cudaFuncSetAttribute(tma_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-    if (result == cudaSuccess)
-      result = cudaFuncSetAttribute(tma_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAdjSmem);
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e[4] = {
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar>, at, (int)kFwdSmem),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField>, at, (int)kFwdSmem),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar>, at, (int)adj_smem<kModeScalar>()),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeDField>, at, (int)adj_smem<kModeDField>())};
+    for (cudaError_t x : e)
+      if (x != cudaSuccess) result = x;
   });
   return result;
 }
@@ -528,10 +705,21 @@ cudaError_t wait_selftest(int* status_host, cudaStream_t st) {
   return cudaStreamSynchronize(st);
 }
 
+cudaError_t launch_tile_flags(const int32_t* rec_idx, int S, int nrec, int nx, int ny, uint8_t* flags,
+                              cudaStream_t st) {
+  const int tiles_x = (nx + kTX - 1) / kTX, tiles_y = (ny + kTY - 1) / kTY;
+  cudaError_t e = cudaMemsetAsync(flags, 0, tma_tiles(nx, ny, S), st);
+  if (e != cudaSuccess) return e;
+  const int n = S * nrec;
+  return tracked_launch(kProfOther, st, [&] {
+    tile_flags_kernel<<<(n + 255) / 256, 256, 0, st>>>(rec_idx, S, nrec, nx, ny, tiles_x, tiles_y, flags);
+  });
+}
+
 bool tma_eligible(int mode, int nx, int ny, int S) {
   (void)nx;
   (void)S;
-  return mode == kModeScalar && ny % 4 == 0 && encode_fn() != nullptr;
+  return (mode == kModeScalar || mode == kModeDField) && ny % 4 == 0 && encode_fn() != nullptr;
 }
 
 size_t tma_tiles(int nx, int ny, int S) {
@@ -542,15 +730,16 @@ namespace {
 inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 }  // namespace
 
-// Steps the tiled kernel cannot take (u^i == 0 at the first step, buffers
-// not on 16-byte boundaries) run on the first per-step kernel instead.
-cudaError_t launch_tma_fwd(const FwdStep& a, int* err, cudaStream_t st) {
-  const bool ok = a.cur != nullptr && a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) &&
-                  al16(a.copy0) && al16(a.copy1) && (a.frame < 0 || (al16(a.hist_x) && al16(a.hist_y)));
+// Steps the tiled kernels cannot take (u^i == 0 at the first step, buffers
+// not on 16-byte boundaries) run on the first per-step kernels instead.
+cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st) {
+  const bool ok = (mode == kModeScalar || (mode == kModeDField && al16(a.field))) && a.cur != nullptr &&
+                  a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) && al16(a.copy0) &&
+                  al16(a.copy1) && (a.frame < 0 || (al16(a.hist_x) && al16(a.hist_y)));
   CUtensorMap cur_map, prev_map;
   if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
       !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, a.S, kTY, kTX))
-    return launch_fwd_step(kModeScalar, a, st);
+    return launch_fwd_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
@@ -558,21 +747,26 @@ cudaError_t launch_tma_fwd(const FwdStep& a, int* err, cudaStream_t st) {
   int grid = num_sms() * 3;
   if (grid > ntiles) grid = ntiles;
   const double cells = (double)a.S * a.nx * a.ny;
+  const int hp = a.prev ? 1 : 0;
   return tracked_launch(kProfForward, st, [&] {
-    tma_fwd_kernel<<<grid, kThreads, kFwdSmem, st>>>(a, cur_map, prev_map, tiles_x, tiles_y,
-                                                     a.prev ? 1 : 0, err);
-  }, cells * alg_bytes_forward(kModeScalar));
+    if (mode == kModeScalar)
+      tma_fwd_kernel<kModeScalar><<<grid, kThreads, kFwdSmem, st>>>(a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+    else
+      tma_fwd_kernel<kModeDField><<<grid, kThreads, kFwdSmem, st>>>(a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+  }, cells * alg_bytes_forward(mode));
 }
 
-cudaError_t launch_tma_adj(const AdjStep& a, int* err, cudaStream_t st) {
-  const bool ok = a.ny % 4 == 0 && a.cur != nullptr && a.prev != nullptr && al16(a.cur) &&
-                  al16(a.prev) && al16(a.out) && al16(a.u) &&
-                  (a.frame < 0 || a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
-  CUtensorMap cur_map, prev_map, u_map;
+cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st) {
+  const bool dfield = mode == kModeDField;
+  const bool ok = (mode == kModeScalar || (dfield && al16(a.field) && al16(a.gacc))) && a.ny % 4 == 0 &&
+                  a.cur != nullptr && a.prev != nullptr && al16(a.cur) && al16(a.prev) && al16(a.out) &&
+                  al16(a.u) && (a.frame < 0 || a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
+  CUtensorMap cur_map, prev_map, u_map, d_map;
   if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
       !make_map(&prev_map, a.prev, a.nx, a.ny, a.S, kTY, kTX) ||
-      !make_map(&u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, kBW, kBH))
-    return launch_adj_step(kModeScalar, a, st);
+      !make_map(&u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
+      !make_map2(&d_map, dfield ? a.field : a.cur, a.nx, a.ny, kBW, kBH))
+    return launch_adj_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
@@ -580,10 +774,15 @@ cudaError_t launch_tma_adj(const AdjStep& a, int* err, cudaStream_t st) {
   int grid = num_sms() * 2;
   if (grid > ntiles) grid = ntiles;
   const double cells = (double)a.S * a.nx * a.ny;
+  const int hu = a.u ? 1 : 0;
   return tracked_launch(kProfAdjoint, st, [&] {
-    tma_adj_kernel<<<grid, kThreads, kAdjSmem, st>>>(a, cur_map, prev_map, u_map, tiles_x, tiles_y,
-                                                     a.u ? 1 : 0, err);
-  }, cells * alg_bytes_adjoint(kModeScalar));
+    if (!dfield)
+      tma_adj_kernel<kModeScalar><<<grid, kThreads, adj_smem<kModeScalar>(), st>>>(
+          a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+    else
+      tma_adj_kernel<kModeDField><<<grid, kThreads, adj_smem<kModeDField>(), st>>>(
+          a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+  }, cells * alg_bytes_adjoint(mode));
 }
 
 }  // namespace ernn

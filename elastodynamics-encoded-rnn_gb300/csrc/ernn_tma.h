@@ -6,15 +6,19 @@
 
 namespace ernn {
 
-// Scalar constants and ny % 4 == 0 (rows of 16-byte multiples for the copy
-// engine), and the driver exposes the tensor-map encoder.
+// Scalar constants or a degradation map, ny % 4 == 0 (rows of 16-byte
+// multiples for the copy engine), and the driver exposes the tensor-map
+// encoder.
 bool tma_eligible(int mode, int nx, int ny, int S);
 // Number of 64 x 32 tiles of one step over all shots.
 size_t tma_tiles(int nx, int ny, int S);
-// Same contract as launch_fwd_step / launch_adj_step (scalar mode); `err` is
-// the call's device error word.
-cudaError_t launch_tma_fwd(const FwdStep& a, int* err, cudaStream_t st);
-cudaError_t launch_tma_adj(const AdjStep& a, int* err, cudaStream_t st);
+// Same contract as launch_fwd_step / launch_adj_step (SCALAR or DFIELD
+// mode); `err` is the call's device error word.
+cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st);
+cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st);
+// Per-call receiver table of the tiled adjoint (tma_tiles bytes at `flags`).
+cudaError_t launch_tile_flags(const int32_t* rec_idx, int S, int nrec, int nx, int ny, uint8_t* flags,
+                              cudaStream_t st);
 // Runs one bounded wait that cannot complete and copies the error word it
 // records into *status_host; synchronises `st`.
 cudaError_t wait_selftest(int* status_host, cudaStream_t st);

@@ -27,7 +27,7 @@ import numpy as np
 import torch
 
 from . import materials, sources
-from .propagate import Geometry, propagate
+from .propagate import Geometry, check_device_status, propagate
 
 H, DT, RHO = 1e-4, 5e-9, 1560.0
 C_ORTHO = materials.orthotropic_xz(130e9, 12e9, 6e9, 5.5e9)  # C11, C33, C13, C55 (GPa), C15 = C35 = 0
@@ -323,7 +323,7 @@ class MultiInversion:
                 lk = trace_misfit(ux, uy, inv.obs[0], inv.obs[1])
                 lk.backward()
             losses.append(lk)
-        for s in self.streams:
+        for s in self.streams[:len(self.invs)]:  # the streams that got work (joined a capture)
             main.wait_stream(s)
         self.opt.step()
         return torch.stack([l.detach() for l in losses]).sum()
@@ -337,6 +337,7 @@ class MultiInversion:
                 self._eager_step()
         torch.cuda.current_stream(self.device).wait_stream(side)
         torch.cuda.synchronize(self.device)
+        check_device_status()
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.loss = self._eager_step()

@@ -177,6 +177,8 @@ class _DeviceStatus:
         self.pending.append((fn, buf, ev))
 
     def poll(self, wait: bool = False) -> None:
+        if not self.pending or torch.cuda.is_current_stream_capturing():
+            return  # event queries are not allowed while a graph is being captured
         keep = []
         for fn, buf, ev in self.pending:
             if wait:

@@ -117,6 +117,12 @@ TILED_CASES = {
     "single_tile": dict(nx=32, ny=64, nt=60),
     "tiny": dict(nx=3, ny=4, nt=30, box=2),
     "many_tiles": dict(nx=130, ny=260, nt=50, S=2, record=O.RECORD_RECEIVERS, nrec=30),
+    "dfield_dense": dict(mode=O.MODE_DFIELD, nx=45, ny=76),
+    "dfield_receivers_multishot": dict(mode=O.MODE_DFIELD, nx=70, ny=132, record=O.RECORD_RECEIVERS,
+                                       S=3, nrec=40),
+    "dfield_duplicate_receivers": dict(mode=O.MODE_DFIELD, nx=40, ny=64, record=O.RECORD_RECEIVERS,
+                                       nrec=6, dup_receiver=True),
+    "dfield_x_force_tiny": dict(mode=O.MODE_DFIELD, nx=3, ny=4, nt=30, box=2, src_comp=0),
 }
 
 
@@ -140,11 +146,22 @@ def test_tiled_forward_matches_step_forward():
     assert rel(a[0], b[0]) <= 1e-5 and rel(a[1], b[1]) <= 1e-5, (rel(a[0], b[0]), rel(a[1], b[1]))
 
 
-def test_tiled_path_rejects_unsupported_problem():
-    case = random_case(nx=20, ny=18, nt=10)  # ny % 4 != 0
+@pytest.mark.parametrize("k", [1, 7, 1000])
+def test_tiled_dfield_checkpoint_interval(k):
+    case = random_case(mode=O.MODE_DFIELD, nx=40, ny=68, nt=90, S=2, record=O.RECORD_RECEIVERS)
     wx, wy = weights(case)
-    with pytest.raises(E._lib.ErnnError):
-        run_gpu(case, wx, wy, path=E.PATH_TILED)
+    ref = run_gpu(case, wx, wy, ckpt_k=None, path=E.PATH_TILED)
+    got = run_gpu(case, wx, wy, ckpt_k=k, path=E.PATH_TILED)
+    for x, y in zip(ref, got):
+        assert np.array_equal(x, y)
+
+
+def test_tiled_path_rejects_unsupported_problem():
+    for kw in (dict(nx=20, ny=18), dict(nx=20, ny=20, mode=O.MODE_FIELDS)):  # ny % 4, six planes
+        case = random_case(nt=10, **kw)
+        wx, wy = weights(case)
+        with pytest.raises(E._lib.ErnnError):
+            run_gpu(case, wx, wy, path=E.PATH_TILED)
 
 
 @pytest.mark.parametrize("path", [E.PATH_STEP, E.PATH_RESIDENT, E.PATH_TILED])
