@@ -14,18 +14,18 @@ Public surface:
       source signals and loads, in-plane rotation and stability, benchmark
       configurations.
 """
-from . import _lib, materials, sources
+from . import _lib, formats, materials, sources
 from ._lib import PATH_AUTO, PATH_RESIDENT, PATH_STEP, PATH_TILED
 from .propagate import (MODE_DFIELD, MODE_FIELDS, MODE_SCALAR, RECORD_FIELDS,
                         RECORD_RECEIVERS, ErnnPropagate, Geometry, check_device_status,
                         elastic_operator_with_force, propagate)
 from .simulators import (CFRPWaveSimulatorRicker, DegradationSimulator, ShotGatherSimulator,
-                         SpatiallyVaryingAnisotropicSimulator)
+                         SpatiallyVaryingAnisotropicSimulator, damage_loss, total_variation_2d)
 
 __all__ = [
     "CFRPWaveSimulatorRicker", "SpatiallyVaryingAnisotropicSimulator", "ShotGatherSimulator",
-    "DegradationSimulator", "ErnnPropagate", "Geometry", "propagate",
-    "elastic_operator_with_force", "sources", "materials", "MODE_SCALAR", "MODE_DFIELD",
+    "DegradationSimulator", "damage_loss", "total_variation_2d", "ErnnPropagate", "Geometry", "propagate",
+    "elastic_operator_with_force", "sources", "materials", "formats", "MODE_SCALAR", "MODE_DFIELD",
     "MODE_FIELDS", "RECORD_FIELDS", "RECORD_RECEIVERS", "PATH_AUTO", "PATH_STEP",
     "PATH_RESIDENT", "PATH_TILED", "check_device_status", "load_library",
 ]

@@ -283,3 +283,29 @@ class DegradationSimulator(nn.Module):
 
     def forward(self):
         return propagate(self.C0, self.rho, self.geom, D=self.D)
+
+
+def total_variation_2d(field: torch.Tensor) -> torch.Tensor:
+    """Sum of the absolute forward differences of a (batch, nx, ny) field along
+    both grid axes (Damage_inversion/Inversion_adam.py:179-195)."""
+    return (torch.sum(torch.abs(field[:, 1:, :] - field[:, :-1, :])) +
+            torch.sum(torch.abs(field[:, :, 1:] - field[:, :, :-1])))
+
+
+def damage_loss(sim: SpatiallyVaryingAnisotropicSimulator, pred_ux, pred_uy, target_ux, target_uy,
+                secondary_time_stride: int = 1, lambda_tv: float = 0.0):
+    """The damage inversion's objective, as its inverter computes it
+    (Damage_inversion/Inversion_adam.py:420-422, 441-463): every
+    `secondary_time_stride`-th frame of the (1, nt_out, nx, ny) histories,
+    5:1 weighted mean squared errors of u_x and u_y, plus lambda_tv times the
+    total variation of the six constant fields of `sim`.  Targets are the
+    full-rate histories.  Returns (total, data, tv)."""
+    ts = secondary_time_stride
+    px, py = pred_ux[:, ::ts], pred_uy[:, ::ts]
+    tx, ty = target_ux[:, ::ts], target_uy[:, ::ts]
+    data = 5 * torch.mean((px - tx) ** 2) + torch.mean((py - ty) ** 2)
+    tv = 0.0
+    if lambda_tv > 0:
+        C = sim.get_material_params()[:6]
+        tv = lambda_tv * sum(total_variation_2d(c) for c in C)
+    return data + tv, data, tv

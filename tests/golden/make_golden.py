@@ -133,7 +133,7 @@ def operator_case(P, Dm, dtype, nx=19, ny=16, nsq=17, seed=3):
         torch.set_default_dtype(torch.float32)
 
 
-def damage_case(Dm, dtype, domain=(20, 20), nt=120, stride=5, ts=2, seed=7):
+def damage_case(Dm, dtype, domain=(20, 20), nt=120, stride=5, ts=2, seed=7, lambda_tv=0.0):
     torch.set_default_dtype(dtype)
     try:
         base = dict(C11_init=130.74e9, C22_init=11.50e9, C12_init=10.49e9, C16_init=30.67e9,
@@ -152,9 +152,9 @@ def damage_case(Dm, dtype, domain=(20, 20), nt=120, stride=5, ts=2, seed=7):
                 p = getattr(sim, n)
                 p.add_(0.08 * torch.randn(p.shape, generator=g))
         inv = Dm.SpatiallyVaryingParameterInverter(sim, tx, ty, secondary_time_stride=ts,
-                                                   lambda_tv=0.0)
+                                                   lambda_tv=lambda_tv)
         ux, uy = sim(save_all_steps=False)
-        loss, _, _ = inv.compute_loss(ux, uy)
+        loss, loss_data, loss_tv = inv.compute_loss(ux, uy)
         loss.backward()
         C = sim.get_material_params()
         names = ["log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66"]
@@ -164,6 +164,7 @@ def damage_case(Dm, dtype, domain=(20, 20), nt=120, stride=5, ts=2, seed=7):
             rho=float(sim.rho), C_fields=np.stack([d(c[0]) for c in C[:6]]),
             gauss=d(sim.gaussian_dist), signal=d(sim.source_signal)[0],
             hist_ux=d(ux), hist_uy=d(uy), target_ux=d(tx), target_uy=d(ty), loss=float(loss),
+            loss_data=float(loss_data), loss_tv=float(loss_tv), lambda_tv=lambda_tv,
             grad_log=np.stack([d(getattr(sim, n).grad[0]) for n in names]))
     finally:
         torch.set_default_dtype(torch.float32)
@@ -177,6 +178,9 @@ def main():
         np.savez_compressed(os.path.join(OUT, f"operator_{tag}.npz"), **operator_case(P, Dm, dtype))
         np.savez_compressed(os.path.join(OUT, f"param_inversion_{tag}.npz"), **param_case(P, dtype))
         np.savez_compressed(os.path.join(OUT, f"damage_inversion_{tag}.npz"), **damage_case(Dm, dtype))
+        # the reference run's regularisation weight (Damage_inversion/Inversion_adam.py:827)
+        np.savez_compressed(os.path.join(OUT, f"damage_inversion_tv_{tag}.npz"),
+                            **damage_case(Dm, dtype, lambda_tv=1e-21))
     print("wrote fixtures to", OUT)
 
 

@@ -293,6 +293,30 @@ def test_dropin_damage_simulator_vs_reference_golden():
     assert rel(got, g["grad_log"]) <= GRAD_TOL
 
 
+def test_dropin_damage_loss_with_tv_vs_reference_golden():
+    # the reference run's objective: 5:1 weighted misfit on every ts-th frame
+    # plus lambda_tv = 1e-21 times the total variation of the six fields
+    g = np.load(os.path.join(GOLDEN, "damage_inversion_tv_f64.npz"))
+    n = int(g["nx"])
+    sim = E.SpatiallyVaryingAnisotropicSimulator((n, n), float(g["h"]), float(g["dt"]), int(g["nt"]),
+                                                 int(g["stride"]), source_f0=4e6, source_t0=2.5e-7,
+                                                 source_amplitude=1e10, total_time=int(g["nt"]) * float(g["dt"]),
+                                                 rho_known=float(g["rho"]), gaussian_param=5e6).to(DEV)
+    names = ("log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66")
+    with torch.no_grad():
+        for t, name in enumerate(names):
+            getattr(sim, name).copy_(torch.log(torch.tensor(g["C_fields"][t], dtype=torch.float64))[None].float())
+    ux, uy = sim(save_all_steps=False)
+    tx = torch.tensor(g["target_ux"], dtype=torch.float32, device=DEV)
+    ty = torch.tensor(g["target_uy"], dtype=torch.float32, device=DEV)
+    total, data, tv = E.damage_loss(sim, ux, uy, tx, ty, int(g["ts"]), float(g["lambda_tv"]))
+    assert abs(float(data) - float(g["loss_data"])) <= 1e-4 * float(g["loss_data"])
+    assert abs(float(tv) - float(g["loss_tv"])) <= 1e-5 * float(g["loss_tv"])
+    total.backward()
+    got = np.stack([getattr(sim, nm).grad[0].cpu().numpy() for nm in names])
+    assert rel(got, g["grad_log"]) <= GRAD_TOL, rel(got, g["grad_log"])
+
+
 def test_damage_simulator_rejects_non_square_like_reference():
     sim = E.SpatiallyVaryingAnisotropicSimulator((12, 10), 1e-4, 5e-9, 10, 5).to(DEV)
     with pytest.raises(RuntimeError):
@@ -372,3 +396,19 @@ def test_device_status_word_is_clear_after_calls(path):
     E.check_device_status()
     assert status.pending == []
     assert E._lib.load().ernn_last_path() == path
+
+
+@pytest.mark.parametrize("path", [E.PATH_STEP, E.PATH_RESIDENT, E.PATH_TILED])
+def test_receiver_traces_equal_gathered_dense_history(path):
+    # same seed: identical sources; the receiver mode records frame k = u^{k*stride+1}
+    # at the receiver cells, exactly the dense history gathered there
+    dense = random_case(nx=40, ny=64, nt=61, stride=3, S=2)
+    recs = random_case(nx=40, ny=64, nt=61, stride=3, S=2, record=O.RECORD_RECEIVERS, nrec=12)
+    rho = torch.tensor(dense.rho, dtype=torch.float32, device=DEV)
+    C = torch.tensor(dense.C, dtype=torch.float32, device=DEV)
+    with torch.no_grad():
+        hx, hy = E.propagate(C, rho, to_geometry(dense, path=path))
+        tx, ty = E.propagate(C, rho, to_geometry(recs, path=path))
+    rec_idx = torch.as_tensor(recs.rec_idx, dtype=torch.int32, device=DEV)
+    gx, gy = E.formats.traces_from_history(hx, hy, rec_idx)
+    assert torch.equal(gx, tx) and torch.equal(gy, ty)
