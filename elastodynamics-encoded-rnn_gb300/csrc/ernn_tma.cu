@@ -96,8 +96,11 @@ __device__ __forceinline__ void release(int* done, int k, F&& refill) {
 
 // TMA destinations start on 128-byte boundaries: the dynamic shared block is
 // allocated 128 bytes longer and its start rounded up.
+// (pointer arithmetic on the __shared__ array, so the compiler keeps the
+// shared state space and emits shared-memory loads)
 __device__ __forceinline__ float* aligned128(float* p) {
-  return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 127) & ~static_cast<uintptr_t>(127));
+  const uint32_t a = s32(p);
+  return p + ((((a + 127u) & ~127u) - a) >> 2);
 }
 
 __device__ __forceinline__ void fence_async() {
@@ -279,31 +282,38 @@ __global__ void __launch_bounds__(kThreads, 3)
       Sums4 st;
       sums4(wx, wy, st);
       const int gi = id.x0 + r;
-      if (gi < nx && gj < ny) {
-        float4 pvx = make_float4(0.f, 0.f, 0.f, 0.f), pvy = pvx;
-        if (has_prev) {
-          pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
-          pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+      // computed for every cell of the tile (the boxes are zero outside the
+      // grid); only the stores are guarded
+      float4 pvx = make_float4(0.f, 0.f, 0.f, 0.f), pvy = pvx;
+      if (has_prev) {
+        pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
+        pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+      }
+      float vx[4], vy[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float lx, ly;
+        apply(ks, st, q, lx, ly);
+        if (MODE == kModeDField) {
+          lx *= g4(w4[q2], q);
+          ly *= g4(w4[q2], q);
         }
-        float vx[4], vy[4];
+        vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
+        vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
+      }
+      // source box: rows and columns of this thread's 4 cells inside it
+      const int sa = gi - ox;
+      if (has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          float lx, ly;
-          apply(ks, st, q, lx, ly);
-          if (MODE == kModeDField) {
-            lx *= g4(w4[q2], q);
-            ly *= g4(w4[q2], q);
-          }
-          vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
-          vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
-          if (has_src) {
-            const int sa = gi - ox, sb = gj + q - oy;
-            if (sa >= 0 && sa < a.bx && sb >= 0 && sb < a.by) {
-              const float f = amp * a.src_map[((size_t)id.shot * a.bx + sa) * a.by + sb];
-              if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
-            }
+          const int sb = gj + q - oy;
+          if ((unsigned)sb < (unsigned)a.by) {
+            const float f = amp * a.src_map[((size_t)id.shot * a.bx + sa) * a.by + sb];
+            if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
           }
         }
+      }
+      if (gi < nx && gj < ny) {
         const float4 nvx = make_float4(vx[0], vx[1], vx[2], vx[3]);
         const float4 nvy = make_float4(vy[0], vy[1], vy[2], vy[3]);
         const size_t o = (size_t)gi * ny + gj;
@@ -471,27 +481,42 @@ __global__ void __launch_bounds__(kThreads, 2)
       sums4(wx, wy, st);
       const int gi = id.x0 + r;
       const bool in = gi < nx && gj < ny;
-      // unweighted lam^{m+1} at the 4 cells
-      const float4 c1x = *reinterpret_cast<const float4*>(hb + (r + 1) * kBW + j + 4);
-      const float4 c1y = *reinterpret_cast<const float4*>(hb + kBH * kBW + (r + 1) * kBW + j + 4);
-      const size_t o = (size_t)gi * ny + gj;
-      if (in) {
-        float4 pvx, pvy;
-        if (MODE == kModeScalar) {
-          pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
-          pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
-        } else {
-          pvx = pv[q2][0];
-          pvy = pv[q2][1];
-        }
-        float vx[4], vy[4];
+      // unweighted lam^{m+1} at the 4 cells (zero outside the grid, so the
+      // imaging products of those cells vanish without a guard)
+      float c1x[4], c1y[4];
+      if (MODE == kModeScalar) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          float lx, ly;
-          apply(ks, st, q, lx, ly);
-          vx[q] = (2.f * g4(c1x, q) - g4(pvx, q)) + lx;
-          vy[q] = (2.f * g4(c1y, q) - g4(pvy, q)) + ly;
+          c1x[q] = st.cx[q];
+          c1y[q] = st.cy[q];
         }
+      } else {
+        const float4 cx4 = *reinterpret_cast<const float4*>(hb + (r + 1) * kBW + j + 4);
+        const float4 cy4 = *reinterpret_cast<const float4*>(hb + kBH * kBW + (r + 1) * kBW + j + 4);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          c1x[q] = g4(cx4, q);
+          c1y[q] = g4(cy4, q);
+        }
+      }
+      const size_t o = (size_t)gi * ny + gj;
+      float4 pvx, pvy;
+      if (MODE == kModeScalar) {
+        pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
+        pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+      } else {
+        pvx = pv[q2][0];
+        pvy = pv[q2][1];
+      }
+      float vx[4], vy[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float lx, ly;
+        apply(ks, st, q, lx, ly);
+        vx[q] = (2.f * c1x[q] - g4(pvx, q)) + lx;
+        vy[q] = (2.f * c1y[q] - g4(pvy, q)) + ly;
+      }
+      if (in) {
         if (a.frame >= 0 && a.record == kRecordFields) {
           const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * N + o;
           const float4 gx = *reinterpret_cast<const float4*>(a.g_x + go);
@@ -508,32 +533,30 @@ __global__ void __launch_bounds__(kThreads, 2)
       if (has_u) {
         win(ub, r + 2, j, vx_[2]);
         win(ub + kBH * kBW, r + 2, j, vy_[2]);
-        if (in) {
-          Sums4 su;
-          sums4(vx_, vy_, su);
-          if (MODE == kModeScalar) {
+        Sums4 su;
+        sums4(vx_, vy_, su);
+        if (MODE == kModeScalar) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const float l1x = g4(c1x, q), l1y = g4(c1y, q);
-              acc[0] += l1x * su.xx_x[q];
-              acc[1] += l1y * su.yy_y[q];
-              acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
-              acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
-              acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
-              acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
-            }
-          } else {
-            float* ga = a.gacc + (size_t)id.shot * N + o;
-            float4 g = *reinterpret_cast<const float4*>(ga);
-            float gv[4] = {g.x, g.y, g.z, g.w};
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              float Lx, Ly;
-              apply(ks, su, q, Lx, Ly);
-              gv[q] += g4(c1x, q) * Lx + g4(c1y, q) * Ly;
-            }
-            *reinterpret_cast<float4*>(ga) = make_float4(gv[0], gv[1], gv[2], gv[3]);
+          for (int q = 0; q < 4; ++q) {
+            const float l1x = c1x[q], l1y = c1y[q];
+            acc[0] += l1x * su.xx_x[q];
+            acc[1] += l1y * su.yy_y[q];
+            acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
+            acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
+            acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
+            acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
           }
+        } else if (in) {
+          float* ga = a.gacc + (size_t)id.shot * N + o;
+          float4 g = *reinterpret_cast<const float4*>(ga);
+          float gv[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            float Lx, Ly;
+            apply(ks, su, q, Lx, Ly);
+            gv[q] += c1x[q] * Lx + c1y[q] * Ly;
+          }
+          *reinterpret_cast<float4*>(ga) = make_float4(gv[0], gv[1], gv[2], gv[3]);
         }
         shift(vx_);
         shift(vy_);
