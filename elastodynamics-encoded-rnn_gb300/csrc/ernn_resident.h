@@ -9,7 +9,7 @@
 
 namespace ernn {
 
-constexpr int kResThreads = 256;  // threads per CTA (each owns 4 x 4-cell items)
+constexpr int kResThreads = 256;  // threads per CTA (each owns 4 x 4-cell items; 512 measured slower)
 constexpr int kResMaxRec = 1024;  // receivers one CTA can own
 
 struct ResCommon {

@@ -4,6 +4,8 @@ Run in a container that has the reference checked out (default path below, or
 pass it as the first argument).  The reference is imported unmodified:
   * Parameter_inversion/Inversion_adam.py is imported as a module with stub
     modules for matplotlib and h5py (absent here, unused on this path);
+  * Parameter_inversion/FEM_generate_data.py likewise (its solver runs on the
+    CPU here; plots are stubbed);
   * Damage_inversion/Inversion_adam.py selects a GPU at import time
     (Inversion_adam.py:36-43), so only its definitions are extracted with `ast`
     and executed with `device` bound to the CPU.
@@ -31,7 +33,7 @@ sys.dont_write_bytecode = True
 
 
 def _stub_plotting():
-    for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.ticker", "mpl_toolkits",
+    for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.ticker", "matplotlib.colors", "mpl_toolkits",
                  "mpl_toolkits.axes_grid1", "h5py"]:
         sys.modules.setdefault(name, mock.MagicMock(name=name))
 
@@ -170,6 +172,59 @@ def damage_case(Dm, dtype, domain=(20, 20), nt=120, stride=5, ts=2, seed=7, lamb
         torch.set_default_dtype(torch.float32)
 
 
+def load_fem_module():
+    _stub_plotting()
+    path = os.path.join(REF, "Parameter_inversion", "FEM_generate_data.py")
+    spec = importlib.util.spec_from_file_location("ref_fem_generate", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    # the solver draws two figures on its way; they are not part of the path
+    mod.plot_gaussian_distribution_func = lambda *a, **k: None
+    mod.plot_ricker_wavelet = lambda *a, **k: None
+    return mod
+
+
+FEM_CASES = {
+    # CFL below 0.5: the requested dt is kept
+    "fem": dict(nx=21, ny=21, Lx=0.02, Ly=0.02, nt=201, t_total=10e-6, source_amplitude=1e10,
+                source_f0=500e3, source_t0=2e-6, gaussian_param=5e5, C11=130.74e9, C22=11.50e9,
+                C12=10.49e9, C16=30.67e9, C26=3.75e9, C66=14.77e9, rho=1610.0,
+                source_position=(0.0, 0.0)),
+    # CFL above 0.5 and an off-centre source: the generator shortens dt
+    "fem_cfl": dict(nx=17, ny=13, Lx=0.016, Ly=0.012, nt=61, t_total=6e-6, source_amplitude=1e10,
+                    source_f0=500e3, source_t0=2e-6, gaussian_param=5e5, C11=130.74e9,
+                    C22=11.50e9, C12=10.49e9, C16=30.67e9, C26=3.75e9, C66=14.77e9, rho=1610.0,
+                    source_position=(0.002, -0.001)),
+}
+
+
+def fem_case(F, kw):
+    """The reference FEM generator run on the CPU in float32 (it moves
+    everything to float32 tensors itself); plotting is stubbed and its output
+    folder goes to a temporary directory."""
+    import tempfile
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        try:
+            x, y, t, ux, uy, tot, mask, src_idx, nodes, elements, info = \
+                F.solve_2d_anisotropic_wave_fem_ricker_fixed(device=torch.device("cpu"), **kw)
+        finally:
+            os.chdir(cwd)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    gauss = F.gaussian_point_load(X, Y, kw["source_position"][0], kw["source_position"][1],
+                                  kw["gaussian_param"])
+    sig = np.array([F.ricker_wavelet(tn, kw["source_f0"], kw["source_t0"], kw["source_amplitude"])
+                    for tn in t])
+    return dict(nx=kw["nx"], ny=kw["ny"], nt=len(t), dt=float(t[1] - t[0]), t=t, x=x, y=y,
+                dx=kw["Lx"] / (kw["nx"] - 1), dy=kw["Ly"] / (kw["ny"] - 1), rho=kw["rho"],
+                C=np.array([kw[k] for k in ("C11", "C22", "C12", "C16", "C26", "C66")]),
+                load=gauss.astype(np.float32), signal=sig.astype(np.float32),
+                ux=ux.astype(np.float32), uy=uy.astype(np.float32), elements=elements,
+                requested=np.array([kw["nt"], kw["t_total"]]),
+                **{f"arg_{k}": np.asarray(v) for k, v in kw.items()})
+
+
 def main():
     torch.manual_seed(0)
     P = load_param_module()
@@ -181,6 +236,10 @@ def main():
         # the reference run's regularisation weight (Damage_inversion/Inversion_adam.py:827)
         np.savez_compressed(os.path.join(OUT, f"damage_inversion_tv_{tag}.npz"),
                             **damage_case(Dm, dtype, lambda_tv=1e-21))
+    F = load_fem_module()
+    torch.set_default_dtype(torch.float32)
+    for name, kw in FEM_CASES.items():
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **fem_case(F, kw))
     print("wrote fixtures to", OUT)
 
 
