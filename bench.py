@@ -432,11 +432,106 @@ def run_multi(args, dist):
     }
 
 
+FEM301 = dict(nx=301, ny=301, Lx=0.4, Ly=0.4, nt=2001, t_total=60e-6, source_amplitude=1e10,
+              source_f0=100e3, source_t0=10e-6, gaussian_param=5e6, C11=130.74e9, C22=11.50e9,
+              C12=10.49e9, C16=30.67e9, C26=3.75e9, C66=14.77e9, rho=1610.0,
+              source_position=(0.0, 0.0))
+
+
+def run_fem(args, dist):
+    """fem301: the FEM data generator's own configuration (301^2 nodes, 2001
+    levels, frames every 5 levels); a step is one generator run."""
+    import ernn_gb300 as E
+    from ernn_gb300 import fem as EF
+
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    lib = E.load_library()
+    c = dict(FEM301)
+    x, y, el, bnd, dx, dy = EF.create_structured_triangular_mesh(c["nx"], c["ny"], c["Lx"], c["Ly"])
+    t, dt, nt = EF._time_axis(c["nt"] if args.nt is None else args.nt, c["t_total"], dx, dy,
+                              c["C11"], c["C22"], c["C66"], c["rho"])
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    load = EF.gaussian_point_load(X, Y, 0.0, 0.0, c["gaussian_param"]).astype(np.float32)
+    sig = EF.ricker_wavelet(t, c["source_f0"], c["source_t0"], c["source_amplitude"]).astype(np.float32)
+    C = tuple(c[k] for k in ("C11", "C22", "C12", "C16", "C26", "C66"))
+    nx, ny, stride = c["nx"], c["ny"], 5
+    load_d = torch.tensor(load, device=dev)
+    sig_d = torch.tensor(sig, device=dev)
+    run = lambda ld, sg: EF.fem_frames(nx, ny, nt, dx, dy, dt, c["rho"], C, ld, sg, stride=stride, device=dev)
+    for _ in range(max(args.warmup, 0)):
+        run(load_d, sig_d)
+    torch.cuda.synchronize()
+    if args.plain:
+        for _ in range(args.steps):
+            run(load_d, sig_d)
+        torch.cuda.synchronize()
+        return None
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    clocks = Clocks(dev.index)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    n0 = lib.ernn_launch_count()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record()
+        run(load_d, sig_d)
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = (lib.ernn_launch_count() - n0) / args.steps
+    ms = dist.max(sum(a.elapsed_time(b) for a, b in ev) / args.steps)
+    node_steps = nx * ny * (nt - 2)
+    value = dist.world * node_steps / (ms * 1e-3) / 1e9
+    # e2e: load and time factors from pinned host memory in, every frame out
+    load_h, sig_h = torch.tensor(load).pin_memory(), torch.tensor(sig).pin_memory()
+    nt_out = (nt + stride - 1) // stride
+    out_h = torch.empty((2, nt_out, nx, ny), dtype=torch.float32).pin_memory()
+    e2e = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        e2e[k][0].record()
+        fx, fy = run(load_h.to(dev, non_blocking=True), sig_h.to(dev, non_blocking=True))
+        out_h[0].copy_(fx, non_blocking=True)
+        out_h[1].copy_(fy, non_blocking=True)
+        e2e[k][1].record()
+    torch.cuda.synchronize()
+    e2e_ms = dist.max(sum(a.elapsed_time(b) for a, b in e2e) / args.steps)
+    rec = {
+        "metric": "Gnode-steps/s (FEM data generator time loop)", "value": round(value, 4),
+        "unit": "Gnode-steps/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (the generator's own source and material)",
+        "config": {"workload": f"fem301: {nx}x{ny} nodes, {nt} levels (dt {dt:.3e} s), frames every {stride}",
+                   "l2": "flushed between timed runs (256 MiB write)"},
+        "e2e": {"value": round(dist.world * node_steps / (e2e_ms * 1e-3) / 1e9, 4), "unit": "Gnode-steps/s",
+                "h2d_bytes_per_step": load.nbytes + sig.nbytes, "d2h_bytes_per_step": out_h.numel() * 4,
+                "ms_per_step": round(e2e_ms, 3)},
+        "gpu_launches": int(launches * args.steps), "clocks": clk,
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        from oracle import fem as OF
+        ns = 60
+        t0 = time.perf_counter()
+        OF.fem_forward(nx, ny, ns, dx, dy, dt, c["rho"], C, load, sig[:ns], stride=stride, precision="f32")
+        cpu_s = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": round(nx * ny * (ns - 2) / cpu_s / 1e9, 6), "unit": "Gnode-steps/s",
+                               "cores": 1, "kind": "port",
+                               "sample": f"fem301 grid, {ns} of {nt} levels, C restatement of the generator loop"}
+    return rec
+
+
 def run_reference(args, dist):
     """The reference path restated op for op in PyTorch (oracle/torch_ref.py),
     on the host cores with all threads; bounded sample per step."""
     if dist.rank != 0:
         return None
+    if args.workload in ("fem301", "multi64"):
+        return run_reference_other(args)
     import ernn_gb300.harness as Hn
     w = Hn.WORKLOADS[args.workload]()
     nts = args.cpu_sample_steps
@@ -466,6 +561,43 @@ def run_reference(args, dist):
     if torch.cuda.is_available():
         rec["gpu_autograd"] = gpu_autograd(args, w)
     return rec
+
+
+def run_reference_other(args):
+    """Reference arm of the non-default workloads: the C restatement of the
+    generator loop (fem301), or the restated reference path looped over the
+    instances' bounded samples is not provided (multi64)."""
+    if args.workload == "multi64":
+        return {"impl": "reference", "unavailable": "multi64 has no reference arm here; the default "
+                "workload's arm times the reference path"}
+    from ernn_gb300 import fem as EF
+    from oracle import fem as OF
+    c = dict(FEM301)
+    x, y, el, bnd, dx, dy = EF.create_structured_triangular_mesh(c["nx"], c["ny"], c["Lx"], c["Ly"])
+    t, dt, nt = EF._time_axis(c["nt"], c["t_total"], dx, dy, c["C11"], c["C22"], c["C66"], c["rho"])
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    load = EF.gaussian_point_load(X, Y, 0.0, 0.0, c["gaussian_param"]).astype(np.float32)
+    sig = EF.ricker_wavelet(t, c["source_f0"], c["source_t0"], c["source_amplitude"]).astype(np.float32)
+    C = tuple(c[k] for k in ("C11", "C22", "C12", "C16", "C26", "C66"))
+    ns = 60
+    vals = []
+    for k in range(max(args.warmup, 0) + args.steps):
+        t0 = time.perf_counter()
+        OF.fem_forward(c["nx"], c["ny"], ns, dx, dy, dt, c["rho"], C, load, sig[:ns], stride=5,
+                       precision="f32")
+        if k >= args.warmup:
+            vals.append(c["nx"] * c["ny"] * (ns - 2) / (time.perf_counter() - t0) / 1e9)
+    v = statistics.median(vals)
+    sample = f"fem301 grid, {ns} of {nt} levels, C restatement of the generator loop, 1 thread"
+    return {"impl": "reference", "metric": "Gnode-steps/s (FEM data generator time loop)",
+            "value": round(v, 6), "unit": "Gnode-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(c["nx"] * c["ny"] * (nt - 2) / (v * 1e9) * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": "fem301"},
+            "cpu_baseline": {"value": round(v, 6), "unit": "Gnode-steps/s", "cores": 1, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(v, 6), "unit": "Gnode-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
 
 
 def gpu_autograd(args, w, iters=3):
@@ -518,6 +650,8 @@ def main():
             rec = run_reference(args, dist)
         elif args.workload == "multi64":
             rec = run_multi(args, dist)
+        elif args.workload == "fem301":
+            rec = run_fem(args, dist)
         else:
             rec = run_ernn(args, dist)
         if rec is not None and dist.rank == 0:

@@ -38,6 +38,14 @@ class ErnnInputs(ctypes.Structure):
                 ("C", "D", "rho", "src_signal", "src_map", "src_origin", "rec_idx")]
 
 
+class ErnnFemProblem(ctypes.Structure):
+    """Mirror of struct ErnnFemProblem (include/ernn.h)."""
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nt", ctypes.c_int32),
+                ("stride", ctypes.c_int32), ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+                ("dt", ctypes.c_double), ("rho", ctypes.c_double), ("C", ctypes.c_double * 6),
+                ("out_scale", ctypes.c_double)]
+
+
 # name -> (restype, argtypes); the complete exported surface of include/ernn.h
 _P = ctypes.c_void_p
 SIGNATURES = {
@@ -56,6 +64,9 @@ SIGNATURES = {
                                     _P]),
     "ernn_forward_static": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
                                            _P, _P, _P]),
+    "ernn_fem_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(ErnnFemProblem)]),
+    "ernn_fem_forward": (ctypes.c_int, [ctypes.POINTER(ErnnFemProblem), _P, _P, _P, _P, _P, _P,
+                                        ctypes.c_size_t, _P]),
     "ernn_launch_count": (ctypes.c_uint64, []),
     "ernn_last_path": (ctypes.c_int32, []),
     "ernn_device_status": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.c_void_p, ctypes.c_int,

@@ -44,10 +44,13 @@ def _is_hdf5(path: str) -> bool:
         return f.read(8) == b"\x89HDF\r\n\x1a\n"
 
 
-def save_wavefields(path: str, ux, uy, x, y, t, source_info: dict | None = None) -> str:
+def save_wavefields(path: str, ux, uy, x, y, t, source_info: dict | None = None,
+                    extra: dict | None = None) -> str:
     """Write (nt_ds, nx, ny) fields in the generator's layout.  HDF5 when
     h5py is present and the name does not end in `.npz`, else `.npz` (the
-    suffix is added when missing).  Returns the path written."""
+    suffix is added when missing).  `extra` maps further dataset paths
+    ("damage_mask", "damage_info/region_0/size", ...) to values, as the
+    damaged-plate generator writes them.  Returns the path written."""
     ux = np.asarray(ux, dtype=np.float32)
     uy = np.asarray(uy, dtype=np.float32)
     if ux.ndim != 3 or ux.shape != uy.shape:
@@ -63,6 +66,8 @@ def save_wavefields(path: str, ux, uy, x, y, t, source_info: dict | None = None)
             g = f.create_group("source_info")
             for k, v in info.items():
                 g.create_dataset(k, data=v if np.isscalar(v) else np.asarray(v))
+            for k, v in (extra or {}).items():
+                f.create_dataset(k, data=v if np.isscalar(v) else np.asarray(v))
         return path
     if not path.endswith(".npz"):
         path = path + ".npz"
@@ -70,6 +75,8 @@ def save_wavefields(path: str, ux, uy, x, y, t, source_info: dict | None = None)
               "y": np.asarray(y, dtype=np.float32), "t": np.asarray(t, dtype=np.float32)}
     for k, v in info.items():
         arrays[f"source_info/{k}"] = np.asarray(v)
+    for k, v in (extra or {}).items():
+        arrays[k] = np.asarray(v)
     np.savez(path, **arrays)
     return path
 

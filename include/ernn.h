@@ -174,6 +174,40 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
 int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, float* out_uy,
                         void* stream);
 
+/* ---------------------------------------------------------------------------
+ * FEM data generator (the step before the ERNN path): the explicit
+ * finite-element time loop that produces the reference's training
+ * wavefields, solve_2d_anisotropic_wave_fem_ricker_fixed
+ * (Parameter_inversion/FEM_generate_data.py:196-590) — structured
+ * checkerboard triangular mesh, lumped mass, constant-strain elements with
+ * three Gauss points, central differences, edges fixed at zero, frames scaled
+ * by out_scale (0.7 there).  The host keeps the generator's dt / nt choice
+ * (its CFL adjustment) and computes the nodal load and the time factors. */
+typedef struct ErnnFemProblem {
+  int32_t nx, ny;   /* nodes along x and y */
+  int32_t nt;       /* time levels 0 .. nt-1 (u^0 = u^1 = 0) */
+  int32_t stride;   /* frame k holds level k*stride; nt_out = ceil(nt / stride) */
+  double dx, dy;    /* node spacing (Lx / (nx-1), Ly / (ny-1)) */
+  double dt, rho;
+  double C[6];      /* C11, C22, C12, C16, C26, C66 */
+  double out_scale; /* factor applied to the frames */
+} ErnnFemProblem;
+
+/* Device workspace of ernn_fem_forward: three time levels of two components. */
+size_t ernn_fem_workspace_bytes(const ErnnFemProblem* p);
+
+/* load: (nx, ny) nodal Gaussian (y fastest), signal: (nt) time factors,
+ * C_fields: NULL (the constants of p->C everywhere) or 6 planes (nx, ny) of
+ * per-node constants, each element taking those of the node nearest its
+ * centroid (the damaged-plate generator, Damage_inversion/FEM_generate_data.py:
+ * 1002-1017); frames_x / frames_y: (nt_out, nx, ny) outputs; all device
+ * memory, enqueued on `stream`.  Replaces the time loop of
+ * Parameter_inversion/FEM_generate_data.py:474-499 (Damage_inversion/...:1093-1117)
+ * and the frame extraction of :519-526 / :926-930. */
+int ernn_fem_forward(const ErnnFemProblem* p, const float* load, const float* signal,
+                     const float* C_fields, float* frames_x, float* frames_y, void* workspace,
+                     size_t workspace_bytes, void* stream);
+
 /* Number of kernels this library has launched since it was loaded. (host call)
  * Diagnostic; no counterpart in the reference. */
 uint64_t ernn_launch_count(void);

@@ -22,9 +22,10 @@ class _FemProblem(ctypes.Structure):
 
 
 def fem_forward(nx, ny, nt, dx, dy, dt, rho, C, load, signal, stride=1, out_scale=0.7,
-                precision="f64"):
+                precision="f64", C_fields=None):
     """Frames (nt_out, nx, ny) of both components, frame k = out_scale * u^{k*stride}.
-    `load` is the nodal Gaussian as an (nx, ny) array, `signal` the (nt,) time factors."""
+    `load` is the nodal Gaussian as an (nx, ny) array, `signal` the (nt,) time
+    factors, `C_fields` None or (6, nx, ny) per-node constants (damaged plate)."""
     real = np.float32 if precision == "f32" else np.float64
     p = _FemProblem(nx, ny, nt, stride, dx, dy, dt, rho, (ctypes.c_double * 6)(*[float(c) for c in C]),
                     out_scale)
@@ -35,8 +36,10 @@ def fem_forward(nx, ny, nt, dx, dy, dt, rho, C, load, signal, stride=1, out_scal
     fy = np.zeros((nt_out, nx, ny), dtype=real)
     fn = getattr(_lib(), f"oracle_fem_forward_{precision}")
     fn.restype = ctypes.c_int
-    fn.argtypes = [ctypes.POINTER(_FemProblem)] + [ctypes.c_void_p] * 4
+    cf = None if C_fields is None else np.ascontiguousarray(C_fields, dtype=real)
+    fn.argtypes = [ctypes.POINTER(_FemProblem)] + [ctypes.c_void_p] * 5
     rc = fn(ctypes.byref(p), node_load.ctypes.data_as(ctypes.c_void_p), sig.ctypes.data_as(ctypes.c_void_p),
+            None if cf is None else cf.ctypes.data_as(ctypes.c_void_p),
             fx.ctypes.data_as(ctypes.c_void_p), fy.ctypes.data_as(ctypes.c_void_p))
     if rc != 0:
         raise RuntimeError(f"oracle_fem_forward failed ({rc})")

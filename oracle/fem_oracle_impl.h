@@ -4,10 +4,12 @@
  *
  * load:   (nx * ny) nodal Gaussian, node id j*nx + i (FEM_generate_data.py:308, `.T.flatten()`)
  * signal: (nt) Ricker time factors (:461-463)
+ * Cf:     NULL (p->C everywhere) or 6 planes (nx, ny) of per-node constants
+ *         (the damaged-plate generator, Damage_inversion/FEM_generate_data.py)
  * frames_x/y: (nt_out, nx, ny), nt_out = ceil(nt / stride)
  */
 int FN(oracle_fem_forward)(const OracleFemProblem* p, const REAL* load, const REAL* signal,
-                           REAL* frames_x, REAL* frames_y) {
+                           const REAL* Cf, REAL* frames_x, REAL* frames_y) {
   if (!p || p->nx < 2 || p->ny < 2 || p->nt < 1 || p->stride < 1) return FEM_ERR_INVALID;
   const int nx = p->nx, ny = p->ny, nt = p->nt;
   const size_t nn = (size_t)nx * ny;
@@ -22,9 +24,11 @@ int FN(oracle_fem_forward)(const OracleFemProblem* p, const REAL* load, const RE
   REAL* bx = (REAL*)malloc(ne * 3 * sizeof(REAL)); /* dN/dx per element node */
   REAL* by = (REAL*)malloc(ne * 3 * sizeof(REAL));
   REAL* fac = (REAL*)malloc(ne * sizeof(REAL));     /* |det J| per element */
+  REAL* ce = (REAL*)malloc(ne * 6 * sizeof(REAL));  /* constants per element */
   char* bnd = (char*)calloc(nn, 1);
-  if (!el || !M || !ux || !uy || !fx || !fy || !bx || !by || !fac || !bnd) {
+  if (!el || !M || !ux || !uy || !fx || !fy || !bx || !by || !fac || !bnd || !ce) {
     free(el); free(M); free(ux); free(uy); free(fx); free(fy); free(bx); free(by); free(fac); free(bnd);
+    free(ce);
     return FEM_ERR_ALLOC;
   }
   /* mesh (:150-168) */
@@ -63,9 +67,21 @@ int FN(oracle_fem_forward)(const OracleFemProblem* p, const REAL* load, const RE
       by[3 * e + a] = r01 * (REAL)dxi[a] + r11 * (REAL)deta[a];
     }
     fac[e] = (REAL)fabs(det);
+    /* constants: uniform, or those of the grid node nearest the element's
+     * centroid (argmin |x - mean(x)|, argmin |y - mean(y)|;
+     * Damage_inversion/FEM_generate_data.py:1002-1017) */
+    if (Cf == NULL) {
+      for (int c = 0; c < 6; ++c) ce[6 * e + c] = (REAL)p->C[c];
+    } else {
+      const double mx = (xc[0] + xc[1] + xc[2]) / 3.0, my = (yc[0] + yc[1] + yc[2]) / 3.0;
+      int bi = 0, bj = 0;
+      for (int i = 1; i < nx; ++i)
+        if (fabs(i * p->dx - mx) < fabs(bi * p->dx - mx)) bi = i;
+      for (int j = 1; j < ny; ++j)
+        if (fabs(j * p->dy - my) < fabs(bj * p->dy - my)) bj = j;
+      for (int c = 0; c < 6; ++c) ce[6 * e + c] = Cf[(size_t)c * nn + (size_t)bi * ny + bj];
+    }
   }
-  const REAL C11 = (REAL)p->C[0], C22 = (REAL)p->C[1], C12 = (REAL)p->C[2];
-  const REAL C16 = (REAL)p->C[3], C26 = (REAL)p->C[4], C66 = (REAL)p->C[5];
   const REAL w = (REAL)(1.0 / 6.0);
   const REAL dt2 = (REAL)(p->dt * p->dt);
   const REAL rho_inv = (REAL)(1.0 / p->rho);
@@ -93,6 +109,8 @@ int FN(oracle_fem_forward)(const OracleFemProblem* p, const REAL* load, const RE
           eyy += gy[a] * cy[t[a]];
           gxy += gy[a] * cx[t[a]] + gx[a] * cy[t[a]];
         }
+        const REAL* k6 = ce + 6 * e;
+        const REAL C11 = k6[0], C22 = k6[1], C12 = k6[2], C16 = k6[3], C26 = k6[4], C66 = k6[5];
         const REAL sxx = C11 * exx + C12 * eyy + C16 * gxy;
         const REAL syy = C12 * exx + C22 * eyy + C26 * gxy;
         const REAL txy = C16 * exx + C26 * eyy + C66 * gxy;
@@ -130,5 +148,6 @@ int FN(oracle_fem_forward)(const OracleFemProblem* p, const REAL* load, const RE
     }
   }
   free(el); free(M); free(ux); free(uy); free(fx); free(fy); free(bx); free(by); free(fac); free(bnd);
+  free(ce);
   return 0;
 }

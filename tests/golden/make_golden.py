@@ -33,7 +33,8 @@ sys.dont_write_bytecode = True
 
 
 def _stub_plotting():
-    for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.ticker", "matplotlib.colors", "mpl_toolkits",
+    for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.ticker", "matplotlib.colors",
+                 "matplotlib.patches", "matplotlib.collections", "mpl_toolkits",
                  "mpl_toolkits.axes_grid1", "h5py"]:
         sys.modules.setdefault(name, mock.MagicMock(name=name))
 
@@ -172,15 +173,16 @@ def damage_case(Dm, dtype, domain=(20, 20), nt=120, stride=5, ts=2, seed=7, lamb
         torch.set_default_dtype(torch.float32)
 
 
-def load_fem_module():
+def load_fem_module(folder="Parameter_inversion"):
     _stub_plotting()
-    path = os.path.join(REF, "Parameter_inversion", "FEM_generate_data.py")
-    spec = importlib.util.spec_from_file_location("ref_fem_generate", path)
+    path = os.path.join(REF, folder, "FEM_generate_data.py")
+    spec = importlib.util.spec_from_file_location(f"ref_fem_generate_{folder}", path)
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    # the solver draws two figures on its way; they are not part of the path
-    mod.plot_gaussian_distribution_func = lambda *a, **k: None
-    mod.plot_ricker_wavelet = lambda *a, **k: None
+    # the solvers draw figures on their way; they are not part of the path
+    for name in dir(mod):
+        if name.startswith(("plot_", "visualize_")):
+            setattr(mod, name, lambda *a, **k: None)
     return mod
 
 
@@ -196,6 +198,11 @@ FEM_CASES = {
                     C22=11.50e9, C12=10.49e9, C16=30.67e9, C26=3.75e9, C66=14.77e9, rho=1610.0,
                     source_position=(0.002, -0.001)),
 }
+
+
+DAMAGE_FEM = dict(FEM_CASES["fem"], damage_configs=[
+    {"type": "circle", "center": (0.004, 0.003), "size": 0.003, "reduction_factor": 0.5},
+    {"type": "square", "center": (-0.005, -0.004), "size": 0.002, "reduction_factor": 0.7}])
 
 
 def fem_case(F, kw):
@@ -216,7 +223,16 @@ def fem_case(F, kw):
                                   kw["gaussian_param"])
     sig = np.array([F.ricker_wavelet(tn, kw["source_f0"], kw["source_t0"], kw["source_amplitude"])
                     for tn in t])
-    return dict(nx=kw["nx"], ny=kw["ny"], nt=len(t), dt=float(t[1] - t[0]), t=t, x=x, y=y,
+    extra = {}
+    if "damage_mask" in info:
+        cfg = kw["damage_configs"]
+        extra = dict(damage_mask=info["damage_mask"],
+                     damage_types=np.array([c["type"] for c in cfg]),
+                     damage_centers=np.array([c["center"] for c in cfg], dtype=np.float64),
+                     damage_sizes=np.array([c["size"] for c in cfg], dtype=np.float64),
+                     damage_factors=np.array([c["reduction_factor"] for c in cfg], dtype=np.float64))
+        kw = {k: v for k, v in kw.items() if k != "damage_configs"}
+    return dict(nx=kw["nx"], ny=kw["ny"], nt=len(t), dt=float(t[1] - t[0]), t=t, x=x, y=y, **extra,
                 dx=kw["Lx"] / (kw["nx"] - 1), dy=kw["Ly"] / (kw["ny"] - 1), rho=kw["rho"],
                 C=np.array([kw[k] for k in ("C11", "C22", "C12", "C16", "C26", "C66")]),
                 load=gauss.astype(np.float32), signal=sig.astype(np.float32),
@@ -240,6 +256,8 @@ def main():
     torch.set_default_dtype(torch.float32)
     for name, kw in FEM_CASES.items():
         np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **fem_case(F, kw))
+    FD = load_fem_module("Damage_inversion")
+    np.savez_compressed(os.path.join(OUT, "fem_damage.npz"), **fem_case(FD, DAMAGE_FEM))
     print("wrote fixtures to", OUT)
 
 
