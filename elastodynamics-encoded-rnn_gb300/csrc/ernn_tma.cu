@@ -341,22 +341,29 @@ __global__ void __launch_bounds__(kThreads, 3)
 }
 
 // ----------------------------------------------------------------- adjoint
-// Stage (SCALAR): halo box of lam^{m+1}, own box of lam^{m+2}, halo box of
-// u^m.  Stage (DFIELD): halo boxes of lam^{m+1}, u^m and D; lam^{m+2} is read
-// into registers straight from global memory before the wait (keeps two
-// CTAs per SM within shared memory).
+// Stage (SCALAR): halo box of lam^{m+1}, own boxes of lam^{m+2} and u^m
+// (u^m enters only through its own cells).  The six
+// imaging sums sum_cells lam . (dA/dC_k u) are evaluated in the transposed
+// form sum_cells u . (dA/dC_k lam): the second differences with zero ghosts
+// are symmetric operators, so both forms are the same sum over the grid, and
+// the stencils of lam^{m+1} are the ones the update already computed.
+// Stage (DFIELD): halo boxes of lam^{m+1}, u^m and D (its imaging is per
+// cell, so u's stencils are needed); lam^{m+2} is read into registers
+// before the wait (keeps two CTAs per SM within shared memory).
 template <int MODE>
 struct AdjLayout {
   static constexpr int kLam = 0;
   static constexpr int kPrev = kHaloFloats;  // SCALAR only
-  static constexpr int kU = (MODE == kModeScalar) ? kHaloFloats + kOwnFloats : kHaloFloats;
+  // u^m: own box after lam^{m+2} (SCALAR), halo box (DFIELD)
+  static constexpr int kU = (MODE == kModeScalar) ? kPrev + kOwnFloats : kHaloFloats;
   static constexpr int kD = kU + kHaloFloats;  // DFIELD only
-  static constexpr int kEnd = (MODE == kModeScalar) ? kU + kHaloFloats : kD + kBH * kBW;
+  static constexpr int kEnd = (MODE == kModeScalar) ? kU + kOwnFloats : kD + kBH * kBW;
   static constexpr int kStage = (kEnd + 31) / 32 * 32;  // 128-byte multiple
+  static constexpr int kCtasPerSm = 2;
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     tma_adj_kernel(const AdjStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap u_map,
                    const __grid_constant__ CUtensorMap d_map, int tiles_x, int tiles_y, int has_u, int* err) {
@@ -369,8 +376,9 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
   const int ntiles = a.S * tiles_x * tiles_y;
-  const uint32_t bytes =
-      (uint32_t)(kHaloFloats + (MODE == kModeScalar ? kOwnFloats : kBH * kBW) + (has_u ? kHaloFloats : 0)) * 4u;
+  const uint32_t bytes = (uint32_t)(MODE == kModeScalar
+                                        ? kHaloFloats + kOwnFloats + (has_u ? kOwnFloats : 0)
+                                        : kHaloFloats + kBH * kBW + (has_u ? kHaloFloats : 0)) * 4u;
   __shared__ int done[2];
   if (tid == 0) {
     bar_init(&bar[0]);
@@ -393,7 +401,10 @@ __global__ void __launch_bounds__(kThreads, 2)
       tma_load3(st + L::kPrev, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
     else
       tma_load2(st + L::kD, &d_map, id.y0 - 4, id.x0 - 1, &bar[k & 1]);
-    if (has_u) tma_load3(st + L::kU, &u_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+    if (has_u) {
+      if (MODE == kModeScalar) tma_load3(st + L::kU, &u_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
+      else tma_load3(st + L::kU, &u_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+    }
   };
   if (tid == 0) {
     issue(0);
@@ -466,7 +477,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     float wx[3][6], wy[3][6], vx_[3][6], vy_[3][6];
     lam_win(r0, wx[0], wy[0]);
     lam_win(r0 + 1, wx[1], wy[1]);
-    if (has_u) {
+    if (MODE == kModeDField && has_u) {
       win(ub, r0, j, vx_[0]);
       win(ub + kBH * kBW, r0, j, vy_[0]);
       win(ub, r0 + 1, j, vx_[1]);
@@ -530,23 +541,27 @@ __global__ void __launch_bounds__(kThreads, 2)
         *reinterpret_cast<float4*>(out + o) = make_float4(vx[0], vx[1], vx[2], vx[3]);
         *reinterpret_cast<float4*>(out + N + o) = make_float4(vy[0], vy[1], vy[2], vy[3]);
       }
-      if (has_u) {
+      if (MODE == kModeScalar && has_u) {
+        // transposed imaging: u^m at the cell times the stencils of lam^{m+1}
+        const float4 u4x = *reinterpret_cast<const float4*>(ub + r * kTY + j);
+        const float4 u4y = *reinterpret_cast<const float4*>(ub + kTX * kTY + r * kTY + j);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float ux = g4(u4x, q), uy = g4(u4y, q);
+          acc[0] += ux * st.xx_x[q];
+          acc[1] += uy * st.yy_y[q];
+          acc[2] += uy * st.xy_x[q] + ux * st.xy_y[q];
+          acc[3] += ux * (0.5f * st.xy_x[q] + st.xx_y[q]) + uy * st.xx_x[q];
+          acc[4] += uy * (st.yy_x[q] + 0.5f * st.xy_y[q]) + ux * st.yy_y[q];
+          acc[5] += ux * st.yy_x[q] + uy * st.xx_y[q];
+        }
+      }
+      if (MODE == kModeDField && has_u) {
         win(ub, r + 2, j, vx_[2]);
         win(ub + kBH * kBW, r + 2, j, vy_[2]);
         Sums4 su;
         sums4(vx_, vy_, su);
-        if (MODE == kModeScalar) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float l1x = c1x[q], l1y = c1y[q];
-            acc[0] += l1x * su.xx_x[q];
-            acc[1] += l1y * su.yy_y[q];
-            acc[2] += l1x * su.xy_y[q] + l1y * su.xy_x[q];
-            acc[3] += l1x * (0.5f * su.xy_x[q] + su.xx_y[q]) + l1y * su.xx_x[q];
-            acc[4] += l1x * su.yy_y[q] + l1y * (su.yy_x[q] + 0.5f * su.xy_y[q]);
-            acc[5] += l1x * su.yy_x[q] + l1y * su.xx_y[q];
-          }
-        } else if (in) {
+        if (in) {
           float* ga = a.gacc + (size_t)id.shot * N + o;
           float4 g = *reinterpret_cast<const float4*>(ga);
           float gv[4] = {g.x, g.y, g.z, g.w};
@@ -787,14 +802,14 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
   CUtensorMap cur_map, prev_map, u_map, d_map;
   if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
       !make_map(&prev_map, a.prev, a.nx, a.ny, a.S, kTY, kTX) ||
-      !make_map(&u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
+      !make_map(&u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, dfield ? kBW : kTY, dfield ? kBH : kTX) ||
       !make_map2(&d_map, dfield ? a.field : a.cur, a.nx, a.ny, kBW, kBH))
     return launch_adj_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.S * tiles_x * tiles_y;
-  int grid = num_sms() * 2;
+  int grid = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm : AdjLayout<kModeScalar>::kCtasPerSm);
   if (grid > ntiles) grid = ntiles;
   const double cells = (double)a.S * a.nx * a.ny;
   const int hu = a.u ? 1 : 0;
