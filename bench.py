@@ -42,7 +42,7 @@ FLUSH_BYTES = 256 * 1024 * 1024
 PATHS = {"auto": 0, "step": 1, "resident": 2, "tiled": 3}
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -58,7 +58,7 @@ def parse():
                     help="kernel path of the library (auto picks per problem)")
     ap.add_argument("--plain", action="store_true",
                     help="only run warmup + steps iterations (no timing, no JSON): a profiling target")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def make_workload(args):
