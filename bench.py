@@ -39,7 +39,7 @@ L2_BYTES = 129 * 1024 * 1024
 FLUSH_BYTES = 256 * 1024 * 1024
 
 
-PATHS = {"auto": 0, "step": 1, "resident": 2, "tiled": 3}
+PATHS = {"auto": 0, "step": 1, "resident": 2, "tiled": 3, "tuned": -1}
 
 
 def parse(argv=None):
@@ -68,7 +68,7 @@ def make_workload(args):
         w.nt = args.nt
     if args.ckpt is not None:
         w.ckpt_k = args.ckpt
-    w.path = PATHS[args.path]
+    w.path = max(PATHS[args.path], 0)
     return w
 
 
@@ -221,6 +221,14 @@ def run_ernn(args, dist):
     lib = E.load_library()
     w = make_workload(args)
     inv = Hn.make_inversion(w, dev)
+    tuned = None
+    if args.path == "tuned":  # measured path and checkpoint interval (ernn_gb300.autotune)
+        from ernn_gb300 import autotune
+        damage = isinstance(inv, Hn.DamageInversion)
+        C = inv.C0 if damage else inv.params()
+        D = inv.D.detach() if damage else None
+        tuned = autotune.tune(inv.geom, C.detach(), inv.rho, D=D)
+        inv.geom.path, inv.geom.ckpt_k = tuned
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(max(args.warmup, 0)):
         inv.step()
@@ -335,6 +343,7 @@ def run_ernn(args, dist):
                                f"ckpt every {inv.geom.ckpt_k} steps",
                    "cell_steps_per_iter": w.cell_steps,
                    "kernel_path": {0: "auto", 1: "step", 2: "resident", 3: "tiled"}[int(lib.ernn_last_path())],
+                   "path_choice": "measured (autotune)" if tuned else args.path,
                    "l2": "flushed between timed iterations (256 MiB write)",
                    "parallelism": f"replicas x{dist.world}"},
         "e2e": {"value": round(dist.world * w.cell_steps / (e2e_ms * 1e-3) / 1e9, 4),

@@ -14,7 +14,7 @@ Public surface:
       source signals and loads, in-plane rotation and stability, benchmark
       configurations.
 """
-from . import _lib, fem, formats, materials, sources
+from . import _lib, autotune, fem, formats, materials, sources
 from ._lib import PATH_AUTO, PATH_RESIDENT, PATH_STEP, PATH_TILED
 from .propagate import (MODE_DFIELD, MODE_FIELDS, MODE_SCALAR, RECORD_FIELDS,
                         RECORD_RECEIVERS, ErnnPropagate, Geometry, check_device_status,
@@ -25,7 +25,7 @@ from .simulators import (CFRPWaveSimulatorRicker, DegradationSimulator, ShotGath
 __all__ = [
     "CFRPWaveSimulatorRicker", "SpatiallyVaryingAnisotropicSimulator", "ShotGatherSimulator",
     "DegradationSimulator", "damage_loss", "total_variation_2d", "ErnnPropagate", "Geometry", "propagate",
-    "elastic_operator_with_force", "sources", "materials", "formats", "fem", "MODE_SCALAR", "MODE_DFIELD",
+    "elastic_operator_with_force", "sources", "materials", "formats", "fem", "autotune", "MODE_SCALAR", "MODE_DFIELD",
     "MODE_FIELDS", "RECORD_FIELDS", "RECORD_RECEIVERS", "PATH_AUTO", "PATH_STEP",
     "PATH_RESIDENT", "PATH_TILED", "check_device_status", "load_library",
 ]

@@ -13,6 +13,7 @@ from . import _build
 MODE_SCALAR, MODE_DFIELD, MODE_FIELDS = 0, 1, 2
 RECORD_FIELDS, RECORD_RECEIVERS = 0, 1
 PATH_AUTO, PATH_STEP, PATH_RESIDENT, PATH_TILED = 0, 1, 2, 3
+FLAG_SHOT_CONSTANTS = 1
 
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "workspace too small", 3: "CUDA runtime error",
@@ -27,7 +28,7 @@ class ErnnProblem(ctypes.Structure):
         ("nt", ctypes.c_int32), ("stride", ctypes.c_int32), ("mode", ctypes.c_int32),
         ("record", ctypes.c_int32), ("nrec", ctypes.c_int32), ("src_comp", ctypes.c_int32),
         ("src_bx", ctypes.c_int32), ("src_by", ctypes.c_int32), ("ckpt_k", ctypes.c_int32),
-        ("path", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("path", ctypes.c_int32), ("flags", ctypes.c_int32),
         ("h", ctypes.c_double), ("dt", ctypes.c_double),
     ]
 

@@ -24,6 +24,7 @@ inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 // Workspace plan of one problem.
 struct Plan {
   int S, nx, ny, nt, k, nseg, nt_out, nblocks, npart, kres;
+  int ncoef;  // coefficient blocks: nshots with ERNN_FLAG_SHOT_CONSTANTS, else 1
   bool store_all;
   size_t N, state_bytes;
   // tape
@@ -43,8 +44,9 @@ Plan make_plan(const ErnnProblem& p) {
   pl.state_bytes = align_up((size_t)p.nshots * 2 * pl.N * sizeof(float));
   const dim3 g = step_grid(p.nx, p.ny, p.nshots);
   pl.nblocks = (int)(g.x * g.y * g.z);
+  pl.ncoef = (p.flags & ERNN_FLAG_SHOT_CONSTANTS) ? p.nshots : 1;
   size_t off = 0;
-  pl.t_coef = off; off += align_up(sizeof(Coef));
+  pl.t_coef = off; off += align_up((size_t)pl.ncoef * sizeof(Coef));
   pl.t_A = off; off += pl.state_bytes;
   pl.t_B = off; off += pl.state_bytes;
   pl.t_total_notape = off;
@@ -53,7 +55,7 @@ Plan make_plan(const ErnnProblem& p) {
   else off += (size_t)(pl.nseg - 1) * 2 * pl.state_bytes;          // (u^{jk}, u^{jk-1})
   pl.t_total_tape = off;
   off = 0;
-  pl.s_coef = off; off += align_up(sizeof(Coef));
+  pl.s_coef = off; off += align_up((size_t)pl.ncoef * sizeof(Coef));
   pl.s_LA = off; off += pl.state_bytes;
   pl.s_LB = off; off += pl.state_bytes;
   // two recompute segments: the cluster-resident path recomputes segment j-1
@@ -66,9 +68,11 @@ Plan make_plan(const ErnnProblem& p) {
   if (p.mode == kModeDField) off += align_up((size_t)p.nshots * pl.N * sizeof(float));
   if (p.mode == kModeFields) off += align_up((size_t)p.nshots * 6 * pl.N * sizeof(float));
   pl.s_part = off;
-  // partial-sum rows: per-step path one per block; resident path one per
-  // imaging CTA (at most 8 clusters of 16 per shot)
+  // partial-sum rows: plain per-step path one per block; resident path one
+  // per imaging CTA (at most 8 clusters of 16 per shot); tiled path one per
+  // CTA, kTiledRowsPerShot per shot with per-shot constants
   pl.npart = pl.nblocks > p.nshots * 16 * 8 ? pl.nblocks : p.nshots * 16 * 8;
+  if (pl.ncoef > 1 && pl.npart < p.nshots * kTiledRowsPerShot) pl.npart = p.nshots * kTiledRowsPerShot;
   if (p.mode == kModeScalar) off += align_up((size_t)pl.npart * 8 * sizeof(double));
   // receiver table of the tiled adjoint: one byte per (shot, 64 x 32 tile)
   pl.s_tflags = off;
@@ -88,8 +92,9 @@ int validate(const ErnnProblem* p) {
   if (p->record == kRecordReceivers && p->nrec < 1) return ERNN_ERR_INVALID;
   if (p->src_comp != 0 && p->src_comp != 1) return ERNN_ERR_INVALID;
   if (p->src_bx < 0 || p->src_by < 0) return ERNN_ERR_INVALID;
-  if (p->path < ERNN_PATH_AUTO || p->path > ERNN_PATH_TILED || p->reserved != 0)
-    return ERNN_ERR_INVALID;
+  if (p->path < ERNN_PATH_AUTO || p->path > ERNN_PATH_TILED) return ERNN_ERR_INVALID;
+  if ((p->flags & ~ERNN_FLAG_SHOT_CONSTANTS) != 0) return ERNN_ERR_INVALID;
+  if ((p->flags & ERNN_FLAG_SHOT_CONSTANTS) && p->mode != kModeScalar) return ERNN_ERR_INVALID;
   if (!(p->h > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->h) || !std::isfinite(p->dt))
     return ERNN_ERR_INVALID;
   return ERNN_OK;
@@ -119,6 +124,7 @@ FwdStep base_fwd(const ErnnProblem& p, const ErnnInputs& in, const Coef* coef, i
   a.nx = p.nx; a.ny = p.ny; a.S = p.nshots; a.nt = p.nt;
   a.frame = -1; a.gframe = -1; a.nt_out = nt_out;
   a.coef = coef;
+  a.coef_stride = (p.flags & ERNN_FLAG_SHOT_CONSTANTS) ? 1 : 0;
   a.field = (p.mode == kModeFields) ? in.C : in.D;
   a.src_signal = in.src_signal;
   a.src_map = in.src_map;
@@ -163,6 +169,7 @@ bool pick_resident(const ErnnProblem& p, const ErnnInputs& in, Coef* coef, ResCo
   rc.nx = p.nx; rc.ny = p.ny; rc.S = p.nshots; rc.nt = p.nt; rc.stride = p.stride;
   rc.nt_out = (p.nt + p.stride - 1) / p.stride;
   rc.coef = coef;
+  rc.coef_stride = (p.flags & ERNN_FLAG_SHOT_CONSTANTS) ? 1 : 0;
   rc.src_signal = in.src_signal; rc.src_map = in.src_map; rc.src_origin = in.src_origin;
   rc.bx = p.src_bx; rc.by = p.src_by; rc.src_comp = p.src_comp;
   rc.rec_idx = (p.record == kRecordReceivers) ? in.rec_idx : nullptr;
@@ -359,7 +366,7 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
   if (tape_bytes < (with_tape ? pl.t_total_tape : pl.t_total_notape)) return ERNN_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
   Coef* coef = reinterpret_cast<Coef*>(at(tape, pl.t_coef));
-  ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st));
+  ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st, pl.ncoef));
 
   if (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT) {
     ResCommon res;
@@ -435,10 +442,10 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   void* tape = const_cast<void*>(tape_c);  // read only below
 
   Coef* coef = reinterpret_cast<Coef*>(at(scratch, pl.s_coef));
-  ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st));
+  ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st, pl.ncoef));
   const size_t gcount = (size_t)p->nshots * pl.nt_out *
                         (p->record == kRecordFields ? pl.N : (size_t)p->nrec);
-  ERNN_CUDA(launch_gscale(g_ux, g_uy, gcount, coef, st));
+  ERNN_CUDA(launch_gscale(g_ux, g_uy, gcount, coef, st, pl.ncoef));
   float* LA = fat(scratch, pl.s_LA);
   float* LB = fat(scratch, pl.s_LB);
   ERNN_CUDA(cudaMemsetAsync(LA, 0, 2 * pl.state_bytes, st));  // LA and LB are adjacent
@@ -454,7 +461,10 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
       int img_rows = 0;
       if ((rc = resident_adjoint(*p, pl, res, g_ux, g_uy, tape, scratch, partials, &img_rows, st)))
         return rc;
-      ERNN_CUDA(launch_finalize_scalar(partials, img_rows, coef, grad_C, st));
+      // imaging rows are grouped by shot
+      if (pl.ncoef > 1) ERNN_CUDA(launch_finalize_scalar(partials, img_rows / p->nshots, coef, grad_C, st,
+                                                         p->nshots, 1));
+      else ERNN_CUDA(launch_finalize_scalar(partials, img_rows, coef, grad_C, st));
       return ERNN_OK;
     }
     if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;
@@ -478,6 +488,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   b.field = (p->mode == kModeFields) ? in->C : in->D;
   b.g_x = g_ux; b.g_y = g_uy;
   b.nt_out = pl.nt_out; b.record = p->record; b.nrec = p->nrec; b.rec_idx = in->rec_idx;
+  b.coef_stride = pl.ncoef > 1 ? 1 : 0;
   b.partials = partials;
   b.gacc = gacc;
   b.tile_flags = nullptr;
@@ -487,6 +498,18 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     b.tile_flags = flags;
   }
 
+  // per-shot gradients need one row layout for the whole call: the tiled
+  // kernel only if every step takes it (same buffers every step)
+  if (tiled && pl.ncoef > 1) {
+    AdjStep probe = b;
+    probe.out = LA; probe.cur = LB; probe.prev = LA;
+    probe.u = pl.store_all ? stored(1) : seg(0);
+    if (!tma_adj_would_run(p->mode, probe)) {
+      tiled = 0;
+      g_last_path.store(ERNN_PATH_STEP, std::memory_order_relaxed);
+    }
+  }
+  const bool tiled_adj = tiled != 0;
   auto adj_step = [&](int m, const float* um) -> int {
     const int idx = p->nt - m;
     b.m = m;
@@ -520,7 +543,12 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
         if ((rc = adj_step(m, seg(m - 1 - i0)))) return rc;
     }
   }
-  if (p->mode == kModeScalar) {
+  if (p->mode == kModeScalar && pl.ncoef > 1) {
+    // per-shot gradients: the tiled kernel keeps kTiledRowsPerShot rows per
+    // shot, the plain kernel one row per block (blocks of a shot contiguous)
+    const int rows = tiled_adj ? kTiledRowsPerShot : pl.nblocks / p->nshots;
+    ERNN_CUDA(launch_finalize_scalar(partials, rows, coef, grad_C, st, p->nshots, 1));
+  } else if (p->mode == kModeScalar) {
     ERNN_CUDA(launch_finalize_scalar(partials, pl.nblocks, coef, grad_C, st));
   } else {
     ERNN_CUDA(launch_finalize_fields(p->mode, gacc, p->nshots, (int)pl.N, coef, grad_field, st));

@@ -96,11 +96,15 @@ cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>
 // Coefficients.  The constants arrive as float32 device scalars (the
 // reference's clamped exp(log C) tensors); C12 + C66 is formed in float32 as
 // the reference forms it from float32 tensors (Inversion_adam.py:88).
+// One block per coefficient block: block b reads C[6b..6b+5] and rho[b]
+// (one block, or one per shot with per-shot constants).
 __global__ void coef_kernel(int mode, const float* __restrict__ C, const float* __restrict__ rho,
                             double h, double dt, Coef* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (threadIdx.x != 0) return;
+  const int b = blockIdx.x;
+  C += 6 * b;
   Coef c;
-  const double r = (double)rho[0];
+  const double r = (double)rho[b];
   const double q = dt * dt / (r * h * h);
   c.k11 = c.k22 = c.kq12 = c.k16 = c.k26 = c.k66 = c.k16h = c.k26h = 0.f;
   if (mode != kModeFields) {
@@ -123,7 +127,7 @@ __global__ void coef_kernel(int mode, const float* __restrict__ C, const float* 
   c.gmax_bits = 0u;
   c.err = 0;
   c.pad2 = 0.0;
-  *out = c;
+  out[b] = c;
 }
 
 // Scalar-constant operator on a staged tile, Lq of ernn_common.cuh.
@@ -219,7 +223,7 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
   }
   __syncthreads();
 
-  const Coef* K = a.coef;
+  const Coef* K = a.coef + (size_t)s * a.coef_stride;
   const float amp = a.src_signal[(size_t)s * a.nt + a.i] * K->kappa;
   const bool has_src = a.bx > 0 && a.by > 0;
   const int ox = has_src ? a.src_origin[2 * s] : 0, oy = has_src ? a.src_origin[2 * s + 1] : 0;
@@ -288,7 +292,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   const size_t N = (size_t)nx * ny;
   const float* cur = a.cur + (size_t)s * 2 * N;
   const float* um = a.u ? a.u + (size_t)s * 2 * N : nullptr;
-  const Coef* K = a.coef;
+  const Coef* K = a.coef + (size_t)s * a.coef_stride;
   const float q = K->q;
 
   // Stage lam^{m+1} (weighted as A^T needs it) and u^m with a one-cell halo.
@@ -484,22 +488,29 @@ __global__ void gmax_kernel(const float* __restrict__ gx, const float* __restric
 
 // Power-of-two scale that brings max |g| into [1, 2): keeps the adjoint
 // field away from FP32 denormals; undone exactly in FP64 at the end.
-__global__ void gscale_kernel(Coef* coef) {
+__global__ void gscale_kernel(Coef* coef, int ncoef) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const uint32_t bits = coef->gmax_bits;
   int e = (int)((bits >> 23) & 0xffu) - 127;  // unbiased exponent of max |g|
   if (bits == 0u || e > 126) e = 0;           // zero, inf or nan: no scaling
   if (e < -126) e = -126;
-  coef->gscale = __uint_as_float((uint32_t)(127 - e) << 23);                   // 2^-e
-  coef->inv_gscale = __longlong_as_double((long long)(1023 + e) << 52);        // 2^e
+  for (int b = 0; b < ncoef; ++b) {            // one scale for every shot's block
+    coef[b].gscale = __uint_as_float((uint32_t)(127 - e) << 23);               // 2^-e
+    coef[b].inv_gscale = __longlong_as_double((long long)(1023 + e) << 52);    // 2^e
+  }
 }
 
 // Deterministic FP64 sum of the per-block partials, then the chain from the
-// six imaging sums to dL/dC.
+// six imaging sums to dL/dC.  Block s of the grid finalises gradient s from
+// rows [s * rows, (s + 1) * rows) with coefficient block s * coef_stride
+// (one gradient, or one per shot with per-shot constants).
 __global__ void finalize_scalar_kernel(const double* __restrict__ partials, int nblocks,
-                                       const Coef* coef, double* __restrict__ grad) {
+                                       const Coef* coef, int coef_stride, double* __restrict__ grad) {
   __shared__ double sh[6][256];
   const int tid = threadIdx.x;
+  partials += (size_t)blockIdx.x * nblocks * 8;
+  coef += (size_t)blockIdx.x * coef_stride;
+  grad += 6 * (size_t)blockIdx.x;
   for (int t = 0; t < 6; ++t) {
     double v = 0.0;
     for (int b = tid; b < nblocks; b += 256) v += partials[(size_t)b * 8 + t];
@@ -604,8 +615,8 @@ static int small_grid(size_t n, int threads) {
 }
 
 cudaError_t launch_coef(int mode, const float* C, const float* rho, double h, double dt,
-                        Coef* coef, cudaStream_t st) {
-  return tracked(kProfOther, st, [&] { coef_kernel<<<1, 32, 0, st>>>(mode, C, rho, h, dt, coef); });
+                        Coef* coef, cudaStream_t st, int ncoef) {
+  return tracked(kProfOther, st, [&] { coef_kernel<<<ncoef, 32, 0, st>>>(mode, C, rho, h, dt, coef); });
 }
 
 cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st) {
@@ -642,18 +653,18 @@ cudaError_t launch_gather(const float* state, int nx, int ny, int S, const int32
 }
 
 cudaError_t launch_gscale(const float* gx, const float* gy, size_t n, Coef* coef,
-                          cudaStream_t st) {
+                          cudaStream_t st, int ncoef) {
   cudaError_t e = tracked(kProfOther, st, [&] {
     gmax_kernel<<<small_grid(n, 256), 256, 0, st>>>(gx, gy, n, coef);
   });
   if (e != cudaSuccess) return e;
-  return tracked(kProfOther, st, [&] { gscale_kernel<<<1, 32, 0, st>>>(coef); });
+  return tracked(kProfOther, st, [&] { gscale_kernel<<<1, 32, 0, st>>>(coef, ncoef); });
 }
 
 cudaError_t launch_finalize_scalar(const double* partials, int nblocks, const Coef* coef,
-                                   double* grad_C, cudaStream_t st) {
+                                   double* grad_C, cudaStream_t st, int ngrad, int coef_stride) {
   return tracked(kProfOther, st, [&] {
-    finalize_scalar_kernel<<<1, 256, 0, st>>>(partials, nblocks, coef, grad_C);
+    finalize_scalar_kernel<<<ngrad, 256, 0, st>>>(partials, nblocks, coef, coef_stride, grad_C);
   });
 }
 

@@ -30,6 +30,7 @@ struct FwdStep {
   float* tr_x;
   float* tr_y;
   const Coef* coef;
+  int coef_stride;     // 0: one coefficient block; 1: one per shot (coef + shot)
   const float* field;  // FIELDS: 6 planes of C; DFIELD: D plane
   const float* src_signal;
   const float* src_map;
@@ -47,12 +48,13 @@ struct AdjStep {
   float* out;         // lam^m (may alias prev)
   const float* u;     // u^m, nullptr when the imaging term vanishes (m == nt)
   const Coef* coef;
+  int coef_stride;    // 0: one coefficient block; 1: one per shot (coef + shot)
   const float* field;
   const float* g_x;   // adjoint source bases (S, nt_out, N or nrec)
   const float* g_y;
   int frame, nt_out, record, nrec;
   const int32_t* rec_idx;
-  double* partials;   // SCALAR: [block][8] FP64 running sums
+  double* partials;   // SCALAR: [row][8] FP64 running sums (rows: see the kernels)
   float* gacc;        // DFIELD: [S][N]; FIELDS: [S][6][N] running sums
   // tiled kernels: non-zero for the 64 x 32 tiles (shot-major) holding a
   // receiver, or nullptr (every tile scans the receivers)
@@ -61,17 +63,20 @@ struct AdjStep {
 
 dim3 step_grid(int nx, int ny, int S);
 
+// ncoef coefficient blocks from C[6 ncoef] and rho[ncoef].
 cudaError_t launch_coef(int mode, const float* C, const float* rho, double h, double dt,
-                        Coef* coef, cudaStream_t st);
+                        Coef* coef, cudaStream_t st, int ncoef = 1);
 cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st);
 cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st);
 cudaError_t launch_gather(const float* state, int nx, int ny, int S, const int32_t* rec_idx,
                           int nrec, int frame, int nt_out, float* tr_x, float* tr_y,
                           cudaStream_t st);
 cudaError_t launch_gscale(const float* gx, const float* gy, size_t n, Coef* coef,
-                          cudaStream_t st);
+                          cudaStream_t st, int ncoef = 1);
+// ngrad gradients of 6: gradient s sums partial rows [s nblocks, (s+1) nblocks).
 cudaError_t launch_finalize_scalar(const double* partials, int nblocks, const Coef* coef,
-                                   double* grad_C, cudaStream_t st);
+                                   double* grad_C, cudaStream_t st, int ngrad = 1,
+                                   int coef_stride = 0);
 cudaError_t launch_finalize_fields(int mode, const float* gacc, int S, int N,
                                    const Coef* coef, float* grad_field, cudaStream_t st);
 cudaError_t launch_operator(int S, int nx, int ny, int mode, double h, const float* C,

@@ -437,19 +437,19 @@ __device__ __forceinline__ void block_reduce6(const double v6[6], double* __rest
   }
 }
 
-// IMG role: items (shot, n, row group, column quad) spread over all IMG CTAs;
-// products summed in FP32 over an item's 16 cells, in FP64 from there on.
-__device__ void imaging_role(const ResCommon& c, const ResImg& g, int cta, int ncta) {
+// IMG role: the items (n, row group, column quad) of one shot spread over
+// that shot's IMG CTAs; products summed in FP32 over an item's 16 cells, in
+// FP64 from there on; one partial row per CTA, rows grouped by shot.
+__device__ void imaging_role(const ResCommon& c, const ResImg& g, int shot, int cta, int ncta) {
   const size_t N = (size_t)c.nx * c.ny;
   const int ngr = (c.nx + 3) / 4, ncq = c.ny / 4;
   const int nn = g.n_hi - g.n_lo + 1;
   const long long per_n = (long long)ngr * ncq;
-  const long long total = (long long)c.S * nn * per_n;
+  const long long total = (long long)nn * per_n;
   double acc64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (long long it = (long long)cta * kResThreads + threadIdx.x; it < total;
        it += (long long)ncta * kResThreads) {
-    const int shot = (int)(it / ((long long)nn * per_n));
-    const long long r = it - (long long)shot * nn * per_n;
+    const long long r = it;
     const int dn = (int)(r / per_n);
     const int rem = (int)(r - (long long)dn * per_n);
     const int gi = rem / ncq, qc = rem - gi * ncq;
@@ -459,7 +459,7 @@ __device__ void imaging_role(const ResCommon& c, const ResImg& g, int cta, int n
 #pragma unroll
     for (int t = 0; t < 6; ++t) acc64[t] += (double)acc[t];
   }
-  block_reduce6(acc64, g.partials + (size_t)cta * 8);
+  block_reduce6(acc64, g.partials + ((size_t)shot * ncta + cta) * 8);
 }
 
 // ---------------------------------------------------------------- kernel
@@ -469,11 +469,10 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
                                                                    const ResRoles roles) {
   const int z = (int)blockIdx.z;
   if (roles.z_img >= 0 && z >= roles.z_img) {
-    // IMG role: no cluster features, no shared state
-    const int cta = ((z - roles.z_img) * (int)gridDim.y + (int)blockIdx.y) * (int)gridDim.x +
-                    (int)blockIdx.x;
-    const int ncta = (roles.n_img_z * (int)gridDim.y) * (int)gridDim.x;
-    imaging_role(c, g, cta, ncta);
+    // IMG role: no cluster features, no shared state; blockIdx.y is the shot
+    const int cta = (z - roles.z_img) * (int)gridDim.x + (int)blockIdx.x;
+    const int ncta = roles.n_img_z * (int)gridDim.x;
+    imaging_role(c, g, (int)blockIdx.y, cta, ncta);
     return;
   }
   extern __shared__ __align__(128) float smem[];
@@ -497,9 +496,9 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   int* rec_count = rec_list + 2 * kResMaxRec;
   uint64_t* bar = reinterpret_cast<uint64_t*>(rec_count + 4);  // [3], 8-byte aligned
 
-  const KSr ks{c.coef->k11, c.coef->k22, c.coef->kq12, c.coef->k16,
-               c.coef->k26, c.coef->k66, c.coef->k16h, c.coef->k26h};
-  const float kappa = c.coef->kappa;
+  const Coef* K = c.coef + (size_t)shot * c.coef_stride;
+  const KSr ks{K->k11, K->k22, K->kq12, K->k16, K->k26, K->k66, K->k16h, K->k26h};
+  const float kappa = K->kappa;
   const size_t shot_off = (size_t)shot * 2 * N;
 
   // -------- initial state: zero the levels and the load, then load
@@ -640,7 +639,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     }
   } else {
     // ================================================================ LAM role
-    const float gs = c.coef->gscale;
+    const float gs = c.coef->gscale;  // one scale for every shot
     // residuals of the receivers this thread injects (entries tid + h * kResThreads),
     // loaded one recording step ahead
     constexpr int kRecPerThread = (kResMaxRec + kResThreads - 1) / kResThreads;

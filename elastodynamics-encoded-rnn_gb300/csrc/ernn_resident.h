@@ -16,6 +16,7 @@ struct ResCommon {
   int nx, ny, S, nt, stride, nt_out;
   int R, CL;              // rows per CTA, CTAs per cluster (one cluster per shot and role)
   const Coef* coef;
+  int coef_stride;        // 0: one coefficient block; 1: one per shot (coef + shot)
   const float* src_signal;
   const float* src_map;
   const int32_t* src_origin;
@@ -60,7 +61,7 @@ struct ResImg {
   const float* lbuf;
   const float* ubuf;
   size_t state_stride;
-  double* partials;        // [IMG CTAs][8]
+  double* partials;        // [shot][IMG CTAs of the shot][8]
 };
 
 // blockIdx.z of each role (-1: absent); IMG occupies n_img_z planes from z_img.

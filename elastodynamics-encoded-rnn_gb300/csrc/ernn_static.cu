@@ -69,10 +69,11 @@ extern "C" int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, f
   if ((size_t)p->src_bx * p->src_by > 0 && (in->src_map == nullptr || in->src_origin == nullptr))
     return ERNN_ERR_INVALID;
   if (p->record == kRecordReceivers && in->rec_idx == nullptr) return ERNN_ERR_INVALID;
-  // coefficient block, then two state levels of nshots x 2 x nx x ny floats
+  // coefficient block(s), then two state levels of nshots x 2 x nx x ny floats
   const size_t N = (size_t)p->nx * p->ny;
   const size_t state_bytes = align_static((size_t)p->nshots * 2 * N * sizeof(float));
-  const size_t coef_bytes = align_static(sizeof(Coef));
+  const int ncoef = (p->flags & ERNN_FLAG_SHOT_CONSTANTS) ? p->nshots : 1;
+  const size_t coef_bytes = align_static((size_t)ncoef * sizeof(Coef));
   if (coef_bytes + 2 * state_bytes > kStaticScratchBytes) return ERNN_ERR_WORKSPACE;
 
   void* base = nullptr;
@@ -82,7 +83,7 @@ extern "C" int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, f
   float* A = reinterpret_cast<float*>(b + coef_bytes);
   float* B = reinterpret_cast<float*>(b + coef_bytes + state_bytes);
   cudaStream_t st = (cudaStream_t)stream;
-  if (launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st) != cudaSuccess) return ERNN_ERR_CUDA;
+  if (launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st, ncoef) != cudaSuccess) return ERNN_ERR_CUDA;
 
   const int nt_out = (p->nt + p->stride - 1) / p->stride;
   const bool receivers = (p->record == kRecordReceivers);
@@ -91,6 +92,7 @@ extern "C" int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, f
   a.nx = p->nx; a.ny = p->ny; a.S = p->nshots; a.nt = p->nt;
   a.nt_out = nt_out;
   a.coef = coef;
+  a.coef_stride = ncoef > 1 ? 1 : 0;
   a.field = (p->mode == kModeFields) ? in->C : in->D;
   a.src_signal = in->src_signal;
   a.src_map = in->src_map;

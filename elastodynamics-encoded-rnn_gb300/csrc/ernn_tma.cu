@@ -227,8 +227,6 @@ __global__ void __launch_bounds__(kThreads, 3)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  const Coefs ks = coefs(a.coef);
-  const float kappa = a.coef->kappa;
   const bool has_src = a.bx > 0 && a.by > 0;
   auto issue = [&](int k) {  // loads of this CTA's k-th tile into stage k & 1
     const int t = blockIdx.x + k * gridDim.x;
@@ -250,8 +248,11 @@ __global__ void __launch_bounds__(kThreads, 3)
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
     const TileId id = tile_of(t, tiles_x, tiles_y);
-    // per-tile scalars, loaded before the wait
-    const float amp = a.src_signal[(size_t)id.shot * a.nt + a.i] * kappa;
+    // per-tile scalars, loaded before the wait (coefficients per shot with
+    // per-shot constants)
+    const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
+    const Coefs ks = coefs(K);
+    const float amp = a.src_signal[(size_t)id.shot * a.nt + a.i] * K->kappa;
     const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
     const int gj = id.y0 + j;
     const int r0 = 2 * rg;  // tile rows r0, r0 + 1 -> box rows r0 + 1, r0 + 2
@@ -387,8 +388,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  const Coefs ks = coefs(a.coef);
-  const float gs = a.coef->gscale;
+  const float gs = a.coef->gscale;  // one scale for every shot
   auto issue = [&](int k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) return;
@@ -415,12 +415,40 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   const bool inject = a.frame >= 0 && a.record == kRecordReceivers;
   // imaging sums (SCALAR): FP32 over a thread's 8 cells of a tile,
   // accumulated over tiles as FP32 pairs (TwoSum), FP64 across threads and
-  // launches
+  // launches.  Partial row: blockIdx.x; with per-shot constants
+  // shot * kTiledRowsPerShot + blockIdx.x, flushed when the CTA's strided
+  // tile list moves on to the next shot (shots never recur: t increases).
   float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const bool per_shot = a.coef_stride != 0;
+  int acc_shot = -1;
+  auto flush = [&](int shot) {  // CTA-uniform: every warp calls it at the same point
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      double v = (double)hi[q] + (double)lo[q];
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if (lane == 0) red[warp][q] = v;
+      hi[q] = 0.f;
+      lo[q] = 0.f;
+    }
+    __syncthreads();
+    if (tid < 6) {
+      double v = 0.0;
+      for (int w = 0; w < kThreads / 32; ++w) v += red[w][tid];
+      const size_t row = per_shot ? (size_t)shot * kTiledRowsPerShot + blockIdx.x : blockIdx.x;
+      a.partials[row * 8 + tid] += v;
+    }
+    __syncthreads();  // red is free again
+  };
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
     const TileId id = tile_of(t, tiles_x, tiles_y);
+    if (MODE == kModeScalar && per_shot && has_u && id.shot != acc_shot) {
+      if (acc_shot >= 0) flush(acc_shot);
+      acc_shot = id.shot;
+    }
+    const Coefs ks = coefs(a.coef + (size_t)id.shot * a.coef_stride);
     const int gj = id.y0 + j;
     const int r0 = 2 * rg;
     // receivers in this tile (uniform over the CTA): the injection and its
@@ -607,19 +635,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     release(done, k, [&] { issue(k + 2); });
   }
   if (MODE != kModeScalar || !has_u) return;
-  const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-  for (int q = 0; q < 6; ++q) {
-    double v = (double)hi[q] + (double)lo[q];
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (lane == 0) red[warp][q] = v;
-  }
-  __syncthreads();
-  if (tid < 6) {
-    double v = 0.0;
-    for (int w = 0; w < kThreads / 32; ++w) v += red[w][tid];
-    a.partials[(size_t)blockIdx.x * 8 + tid] += v;
-  }
+  flush(per_shot ? acc_shot : 0);
 }
 
 // ------------------------------------------------------ wait self-test
@@ -794,23 +810,36 @@ cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st
   }, cells * alg_bytes_forward(mode));
 }
 
-cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st) {
+namespace {
+bool adj_maps(int mode, const AdjStep& a, CUtensorMap* cur_map, CUtensorMap* prev_map, CUtensorMap* u_map,
+              CUtensorMap* d_map) {
   const bool dfield = mode == kModeDField;
   const bool ok = (mode == kModeScalar || (dfield && al16(a.field) && al16(a.gacc))) && a.ny % 4 == 0 &&
                   a.cur != nullptr && a.prev != nullptr && al16(a.cur) && al16(a.prev) && al16(a.out) &&
-                  al16(a.u) && (a.frame < 0 || a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
+                  al16(a.u) && (a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
+  return ok && make_map(cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) &&
+         make_map(prev_map, a.prev, a.nx, a.ny, a.S, kTY, kTX) &&
+         make_map(u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, dfield ? kBW : kTY, dfield ? kBH : kTX) &&
+         make_map2(d_map, dfield ? a.field : a.cur, a.nx, a.ny, kBW, kBH);
+}
+}  // namespace
+
+bool tma_adj_would_run(int mode, const AdjStep& a) {
+  CUtensorMap m[4];
+  return adj_maps(mode, a, &m[0], &m[1], &m[2], &m[3]);
+}
+
+cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st) {
+  const bool dfield = mode == kModeDField;
   CUtensorMap cur_map, prev_map, u_map, d_map;
-  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
-      !make_map(&prev_map, a.prev, a.nx, a.ny, a.S, kTY, kTX) ||
-      !make_map(&u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, dfield ? kBW : kTY, dfield ? kBH : kTX) ||
-      !make_map2(&d_map, dfield ? a.field : a.cur, a.nx, a.ny, kBW, kBH))
-    return launch_adj_step(mode, a, st);
+  if (!adj_maps(mode, a, &cur_map, &prev_map, &u_map, &d_map)) return launch_adj_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.S * tiles_x * tiles_y;
   int grid = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm : AdjLayout<kModeScalar>::kCtasPerSm);
   if (grid > ntiles) grid = ntiles;
+  if (grid > kTiledRowsPerShot) grid = kTiledRowsPerShot;
   const double cells = (double)a.S * a.nx * a.ny;
   const int hu = a.u ? 1 : 0;
   return tracked_launch(kProfAdjoint, st, [&] {

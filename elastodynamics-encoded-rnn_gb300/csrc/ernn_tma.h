@@ -10,12 +10,19 @@ namespace ernn {
 // multiples for the copy engine), and the driver exposes the tensor-map
 // encoder.
 bool tma_eligible(int mode, int nx, int ny, int S);
+// Partial-sum rows reserved per shot by the tiled adjoint with per-shot
+// constants (its grid never exceeds this many CTAs).
+constexpr int kTiledRowsPerShot = 1024;
 // Number of 64 x 32 tiles of one step over all shots.
 size_t tma_tiles(int nx, int ny, int S);
 // Same contract as launch_fwd_step / launch_adj_step (SCALAR or DFIELD
 // mode); `err` is the call's device error word.
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st);
 cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st);
+// Whether launch_tma_adj takes the tiled kernel for steps shaped like `a`
+// (buffers on 16-byte boundaries, tensor maps encodable) rather than falling
+// back to the plain kernel.
+bool tma_adj_would_run(int mode, const AdjStep& a);
 // Per-call receiver table of the tiled adjoint (tma_tiles bytes at `flags`).
 cudaError_t launch_tile_flags(const int32_t* rec_idx, int S, int nrec, int nx, int ny, uint8_t* flags,
                               cudaStream_t st);

@@ -285,26 +285,77 @@ def multi_instances(n=64, seed=0, sides=None):
     return out
 
 
+class _InstanceGroup:
+    """Instances of one grid size, step count and acquisition geometry, run as
+    the shots of one propagation with per-shot constants: each keeps its own
+    constants, density, observations and gradient."""
+
+    def __init__(self, invs, device, budget_fraction):
+        from .propagate import choose_ckpt_k
+        from ._lib import FLAG_SHOT_CONSTANTS
+        self.invs = invs
+        g0 = invs[0].geom
+        S = len(invs)
+        rep = lambda t: t.repeat((S,) + (1,) * (t.dim() - 1)).contiguous()
+        self.geom = Geometry(nx=g0.nx, ny=g0.ny, nt=g0.nt, h=g0.h, dt=g0.dt,
+                             src_signal=rep(g0.src_signal), src_map=rep(g0.src_map),
+                             src_origin=rep(g0.src_origin), stride=g0.stride, src_comp=g0.src_comp,
+                             rec_idx=rep(g0.rec_idx), path=g0.path)
+        self.geom.ckpt_k = choose_ckpt_k(self.geom, 0, device, budget_fraction=budget_fraction,
+                                         flags=FLAG_SHOT_CONSTANTS if S > 1 else 0)
+        self.obs = [torch.cat([inv.obs[c] for inv in invs]).contiguous() for c in (0, 1)]
+        self.rho = torch.full((S,), RHO, dtype=torch.float32, device=device)
+
+    def loss(self):
+        if len(self.invs) == 1:
+            ux, uy = propagate(self.invs[0].params(), self.rho[0], self.geom)
+            return trace_misfit(ux, uy, self.obs[0], self.obs[1])
+        C = torch.stack([inv.params() for inv in self.invs])
+        ux, uy = propagate(C, self.rho, self.geom)
+        # the sum of each instance's own misfit
+        return sum(trace_misfit(ux[s:s + 1], uy[s:s + 1], self.obs[0][s:s + 1], self.obs[1][s:s + 1])
+                   for s in range(len(self.invs)))
+
+
 class MultiInversion:
     """Many independent scalar-constant inversions advanced as one iteration:
-    each instance's forward, misfit and hand adjoint run on one of `nstreams`
-    CUDA streams, one Adam step updates every instance, and the whole iteration
-    is captured once in a CUDA graph and replayed (`step`)."""
+    instances with the same grid size and step count run together as the
+    shots of one propagation with per-shot constants (their own constants,
+    densities and gradients), the groups on `nstreams` CUDA streams, one Adam
+    step updates every instance, and the whole iteration is captured once in
+    a CUDA graph and replayed (`step`).  group=False runs every instance on
+    its own."""
 
-    def __init__(self, ws, device, lr=1e-2, seed=0, nstreams=8, graph=True):
-        from .propagate import choose_ckpt_k
+    def __init__(self, ws, device, lr=1e-2, seed=0, nstreams=8, graph=True, group=True):
         self.ws = ws
         self.device = device
-        self.invs = []
-        for k, w in enumerate(ws):
-            inv = Inversion(w, device, lr=lr, seed=seed + k)
-            # fix the checkpoint interval now (the choice queries free memory)
-            inv.geom.ckpt_k = choose_ckpt_k(inv.geom, 0, device, budget_fraction=0.4 / len(ws))
-            self.invs.append(inv)
+        self.invs = [Inversion(w, device, lr=lr, seed=seed + k) for k, w in enumerate(ws)]
+        keyed = {}
+        for k, (w, inv) in enumerate(zip(ws, self.invs)):
+            key = (w.nx, w.ny, inv.geom.nt, w.stride, tuple(w.src_cells), tuple(w.rec_cells), w.f0,
+                   w.amplitude, w.gaussian_param, w.path) if group else k
+            keyed.setdefault(key, []).append(inv)
+        # largest work first: the longest groups start earliest on the streams
+        members = sorted(keyed.values(), key=lambda g: -sum(i.w.cell_steps for i in g))
+        self.groups = [_InstanceGroup(g, device, 0.4 * len(g) / len(ws)) for g in members]
+        # groups large enough for the tiled kernels (which fill the GPU on
+        # their own) run one after another on the first stream; the smaller
+        # ones share the remaining streams and overlap with them
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
+        big = lambda g: g.geom.nshots * -(-g.geom.nx // 32) * -(-g.geom.ny // 64) >= 4 * sms
+        nsmall = max(1, nstreams - 1)
+        small = 0
+        self.stream_of = []
+        for g in self.groups:
+            if big(g) or nstreams == 1:
+                self.stream_of.append(0)
+            else:
+                self.stream_of.append(1 + small % nsmall)
+                small += 1
         params = [inv.params.theta for inv in self.invs]
         self.opt = torch.optim.Adam(params, lr=lr, capturable=graph)
         self.streams = [torch.cuda.Stream(device) for _ in range(nstreams)]
-        self.obs = [o for inv in self.invs for o in inv.obs]
+        self.obs = [o for g in self.groups for o in g.obs]
         self.cell_steps = sum(w.cell_steps for w in ws)
         self.graph = None
         self.loss = None
@@ -315,16 +366,17 @@ class MultiInversion:
         self.opt.zero_grad(set_to_none=False)
         main = torch.cuda.current_stream(self.device)
         losses = []
-        for k, inv in enumerate(self.invs):
-            s = self.streams[k % len(self.streams)]
-            s.wait_stream(main)
+        used = sorted(set(self.stream_of))
+        for k in used:
+            self.streams[k].wait_stream(main)
+        for k, grp in enumerate(self.groups):
+            s = self.streams[self.stream_of[k]]
             with torch.cuda.stream(s):
-                ux, uy = propagate(inv.params(), inv.rho, inv.geom)
-                lk = trace_misfit(ux, uy, inv.obs[0], inv.obs[1])
+                lk = grp.loss()
                 lk.backward()
             losses.append(lk)
-        for s in self.streams[:len(self.invs)]:  # the streams that got work (joined a capture)
-            main.wait_stream(s)
+        for k in used:  # the streams that got work (joined a capture)
+            main.wait_stream(self.streams[k])
         self.opt.step()
         return torch.stack([l.detach() for l in losses]).sum()
 

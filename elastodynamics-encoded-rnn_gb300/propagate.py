@@ -69,13 +69,13 @@ class Geometry:
     def record(self) -> int:
         return RECORD_FIELDS if self.rec_idx is None else RECORD_RECEIVERS
 
-    def problem(self, mode: int) -> _lib.ErnnProblem:
+    def problem(self, mode: int, flags: int = 0) -> _lib.ErnnProblem:
         nrec = 0 if self.rec_idx is None else int(self.rec_idx.shape[1])
         k = self.ckpt_k if self.ckpt_k is not None else self.nt
         return _lib.ErnnProblem(self.nshots, self.nx, self.ny, self.nt, self.stride, mode,
                                 self.record, nrec, self.src_comp, int(self.src_map.shape[1]),
-                                int(self.src_map.shape[2]), int(max(1, k)), int(self.path), 0,
-                                float(self.h), float(self.dt))
+                                int(self.src_map.shape[2]), int(max(1, k)), int(self.path),
+                                int(flags), float(self.h), float(self.dt))
 
     def out_shape(self):
         if self.rec_idx is None:
@@ -111,7 +111,7 @@ class Geometry:
         self._checked = True
 
 
-def choose_ckpt_k(geom: Geometry, mode: int, device, budget_fraction: float = 0.4) -> int:
+def choose_ckpt_k(geom: Geometry, mode: int, device, budget_fraction: float = 0.4, flags: int = 0) -> int:
     """Checkpoint interval for a problem: keep every state when the tape fits in
     `budget_fraction` of the free device memory (no recomputation), otherwise the
     largest interval whose checkpoints plus recompute segment fit, starting from
@@ -122,7 +122,7 @@ def choose_ckpt_k(geom: Geometry, mode: int, device, budget_fraction: float = 0.
     nt = geom.nt
 
     def need(k):
-        p = geom.problem(mode)
+        p = geom.problem(mode, flags)
         p.ckpt_k = k
         return lib.ernn_tape_bytes(ctypes.byref(p), 1) + lib.ernn_adjoint_scratch_bytes(ctypes.byref(p))
 
@@ -206,35 +206,45 @@ def check_device_status() -> None:
 class ErnnPropagate(torch.autograd.Function):
     """(C, D, rho) -> (out_ux, out_uy) through the fused CUDA time loop.
 
-    C:   (6,) scalar constants (SCALAR, or C0 of DFIELD) or (6, nx, ny) planes (FIELDS).
+    C:   (6,) scalar constants (SCALAR, or C0 of DFIELD), (S, 6) per-shot
+         constants (SCALAR: independent media advancing together, with rho (S,)),
+         or (6, nx, ny) planes (FIELDS).
     D:   (nx, ny) degradation map or None.
-    rho: 0-dim density.
+    rho: 0-dim density, or (S,) with per-shot constants.
     Returns the dense history (S, nt_out, nx, ny) per component, or receiver
     traces (S, nt_out, R), frame k holding u^{k*stride+1}.
-    Gradients: dL/dC (FP64 reduction, returned as float32) in SCALAR mode,
-    dL/dC(x) in FIELDS mode, dL/dD(x) in DFIELD mode (C0 gets none).
+    Gradients: dL/dC (FP64 reduction, returned as float32; (S, 6) with
+    per-shot constants) in SCALAR mode, dL/dC(x) in FIELDS mode, dL/dD(x) in
+    DFIELD mode (C0 gets none).
     """
 
     @staticmethod
     def forward(ctx, C, D, rho, geom: Geometry, keep_tape: bool = True):
         _require_cuda(C, D, rho)
         dev = C.device
-        mode = _mode_of(C, D)
+        per_shot = D is None and C.dim() == 2 and C.shape[-1] == 6
+        mode = MODE_SCALAR if per_shot else _mode_of(C, D)
+        flags = _lib.FLAG_SHOT_CONSTANTS if per_shot else 0
         C = C.detach().to(torch.float32).contiguous()
         D = None if D is None else D.detach().to(torch.float32).contiguous()
-        rho = rho.detach().to(torch.float32).reshape(1).contiguous()
-        if mode == MODE_FIELDS and tuple(C.shape) != (6, geom.nx, geom.ny):
+        rho = rho.detach().to(torch.float32).reshape(-1).contiguous()
+        if per_shot:
+            if tuple(C.shape) != (geom.nshots, 6) or tuple(rho.shape) != (geom.nshots,):
+                raise ValueError("per-shot constants must be (S, 6) with rho (S,)")
+        elif mode == MODE_FIELDS and tuple(C.shape) != (6, geom.nx, geom.ny):
             raise ValueError("per-cell constants must be (6, nx, ny)")
-        if mode != MODE_FIELDS and tuple(C.shape) != (6,):
+        elif mode != MODE_FIELDS and tuple(C.shape) != (6,):
             raise ValueError("scalar constants must be (6,)")
+        if not per_shot and rho.numel() != 1:
+            raise ValueError("rho must be a scalar")
         if D is not None and tuple(D.shape) != (geom.nx, geom.ny):
             raise ValueError("D must be (nx, ny)")
         geom.check(dev)
         _STATUS.poll()
         lib = _lib.load()
         if geom.ckpt_k is None:
-            geom.ckpt_k = choose_ckpt_k(geom, mode, dev)
-        prob = geom.problem(mode)
+            geom.ckpt_k = choose_ckpt_k(geom, mode, dev, flags=flags)
+        prob = geom.problem(mode, flags)
         want_grad = bool(keep_tape and (ctx.needs_input_grad[0] or ctx.needs_input_grad[1]))
         tape_bytes = lib.ernn_tape_bytes(ctypes.byref(prob), int(want_grad))
         with torch.cuda.device(dev):
@@ -249,6 +259,7 @@ class ErnnPropagate(torch.autograd.Function):
             _STATUS.enqueue("ernn_forward", prob, tape, 0)
         ctx.geom = geom
         ctx.mode = mode
+        ctx.flags = flags
         ctx.tape = tape if want_grad else None
         ctx.save_for_backward(C, D, rho)
         return out_ux, out_uy
@@ -264,11 +275,12 @@ class ErnnPropagate(torch.autograd.Function):
         g_ux = torch.zeros(shape, device=dev) if g_ux is None else g_ux.to(torch.float32).contiguous()
         g_uy = torch.zeros(shape, device=dev) if g_uy is None else g_uy.to(torch.float32).contiguous()
         lib = _lib.load()
-        prob = geom.problem(mode)
+        prob = geom.problem(mode, ctx.flags)
         scratch_bytes = lib.ernn_adjoint_scratch_bytes(ctypes.byref(prob))
         with torch.cuda.device(dev):
             scratch = torch.empty(scratch_bytes, dtype=torch.uint8, device=dev)
-            grad_C64 = torch.empty(6, dtype=torch.float64, device=dev) if mode == MODE_SCALAR else None
+            grad_C64 = torch.empty(tuple(C.shape), dtype=torch.float64, device=dev) \
+                if mode == MODE_SCALAR else None
             if mode == MODE_FIELDS:
                 grad_field = torch.empty((6, geom.nx, geom.ny), dtype=torch.float32, device=dev)
             elif mode == MODE_DFIELD:

@@ -67,6 +67,14 @@ enum {
                              ny % 4 == 0); ERNN_ERR_UNSUPPORTED otherwise */
 };
 
+/* Problem flags. */
+enum {
+  /* SCALAR mode: every shot has its own constants and density — C is
+   * nshots x 6, rho nshots, grad_C nshots x 6 — so independent inversions
+   * of one grid size and step count advance in the same launches */
+  ERNN_FLAG_SHOT_CONSTANTS = 1
+};
+
 /* One propagation problem.  Plain data; identical layout in C, C++, ctypes. */
 typedef struct ErnnProblem {
   int32_t nshots;   /* independent shots sharing the medium (batched) */
@@ -80,16 +88,17 @@ typedef struct ErnnProblem {
   int32_t src_bx, src_by; /* source map box size in cells */
   int32_t ckpt_k;   /* checkpoint interval in steps; >= nt keeps every state */
   int32_t path;     /* ERNN_PATH_*: which kernels run the time loop */
-  int32_t reserved; /* must be 0 */
+  int32_t flags;    /* ERNN_FLAG_* bits; others must be 0 */
   double h;         /* grid spacing [m] */
   double dt;        /* time step [s] */
 } ErnnProblem;
 
 /* Inputs shared by the forward and the adjoint (all device pointers). */
 typedef struct ErnnInputs {
-  const float* C;            /* SCALAR, DFIELD: 6 floats; FIELDS: 6 planes of nx*ny */
+  const float* C;            /* SCALAR, DFIELD: 6 floats (nshots x 6 with
+                                ERNN_FLAG_SHOT_CONSTANTS); FIELDS: 6 planes of nx*ny */
   const float* D;            /* DFIELD: nx*ny; otherwise NULL */
-  const float* rho;          /* 1 float, density [kg/m^3] */
+  const float* rho;          /* 1 float (nshots with ERNN_FLAG_SHOT_CONSTANTS), density [kg/m^3] */
   const float* src_signal;   /* nshots*nt: force amplitude of step i */
   const float* src_map;      /* nshots*src_bx*src_by: spatial load inside the box */
   const int32_t* src_origin; /* nshots*2: (x0, y0) of each shot's box; may lie partly outside */
@@ -149,7 +158,8 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
  * g_ux, g_uy: dL/d(out_ux, out_uy), same shapes as the forward outputs.
  * tape: the tape of the matching ernn_forward(with_tape = 1) call.
  * scratch: ernn_adjoint_scratch_bytes(p) bytes.
- * grad_C: SCALAR: 6 doubles dL/dC (FP64 reduction over cells, steps, shots);
+ * grad_C: SCALAR: 6 doubles dL/dC (FP64 reduction over cells, steps, shots),
+ *         nshots x 6 with ERNN_FLAG_SHOT_CONSTANTS (each shot's own constants);
  *         other modes: may be NULL.
  * grad_field: FIELDS: 6 planes dL/dC_ij(x) (float); DFIELD: nx*ny dL/dD(x);
  *             SCALAR: may be NULL. */
@@ -164,7 +174,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
  * inputs, outputs and results as ernn_forward(with_tape = 0) on the per-step
  * kernels; the two-level wavefield lives in an 8 MiB file-scope device array
  * that every GPU loading the library keeps until exit.  Problems needing
- * more than that (256 B + 2 x nshots x 2 x nx x ny x 4 B, each rounded up to
+ * more than that (the coefficient blocks, 64 B each, + 2 x nshots x 2 x nx x ny x 4 B, each rounded up to
  * 256 B) are rejected with ERNN_ERR_WORKSPACE.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that device
  * current: make it before any stream capture; `stream` must belong to the

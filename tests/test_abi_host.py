@@ -46,7 +46,7 @@ def test_version_and_error_strings():
 
 def _problem(**kw):
     base = dict(nshots=2, nx=64, ny=48, nt=100, stride=5, mode=0, record=1, nrec=8, src_comp=1,
-                src_bx=9, src_by=9, ckpt_k=10, path=0, reserved=0, h=1e-4, dt=5e-9)
+                src_bx=9, src_by=9, ckpt_k=10, path=0, flags=0, h=1e-4, dt=5e-9)
     base.update(kw)
     return E._lib.ErnnProblem(*[base[f] for f, _ in E._lib.ErnnProblem._fields_])
 
@@ -56,7 +56,7 @@ def test_validation_rejects_bad_problems():
     assert lib.ernn_validate(ctypes.byref(_problem())) == 0
     bad = [dict(nx=0), dict(nt=0), dict(stride=0), dict(mode=3), dict(record=2),
            dict(nrec=0), dict(src_comp=2), dict(h=0.0), dict(dt=-1.0), dict(ckpt_k=0),
-           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=4), dict(path=-1), dict(reserved=1)]
+           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=4), dict(path=-1), dict(flags=2), dict(flags=1, mode=1)]
     for kw in bad:
         assert lib.ernn_validate(ctypes.byref(_problem(**kw))) == 1, kw
     assert lib.ernn_validate(None) == 1

@@ -40,3 +40,21 @@ def test_graph_captured_iteration_matches_eager():
     assert abs(loss_g - loss_e) <= 1e-6 * abs(loss_e), (loss_g, loss_e)
     assert rel(grad_g, grad_e) <= 1e-6, rel(grad_g, grad_e)
     Hn.check_device_status()
+
+
+def test_grouped_instances_match_separate_runs():
+    # two instances of one size run as the shots of one call with per-shot
+    # constants; their losses and gradients equal those of separate calls
+    def ws():
+        out = Hn.multi_instances(n=3, sides=[192, 192, 256])
+        for w in out:
+            w.nt = 150
+        return out
+    g = Hn.MultiInversion(ws(), DEV, graph=False, group=True)
+    e = Hn.MultiInversion(ws(), DEV, graph=False, group=False)
+    assert len(g.groups) == 2 and len(e.groups) == 3
+    lg, le = float(g.step()), float(e.step())
+    assert abs(lg - le) <= 1e-6 * abs(le), (lg, le)
+    gg = g.gradient().detach().cpu().numpy().astype(np.float64)
+    ge = e.gradient().detach().cpu().numpy().astype(np.float64)
+    assert rel(gg, ge) <= 1e-5, rel(gg, ge)
