@@ -429,7 +429,9 @@ def run_multi(args, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded instances and observations)",
         "config": {"workload": f"multi64: 64 inversions, side {min(sides)}..{max(sides)}, nt = 5.2 side, "
-                               "one CUDA-graph-captured Adam iteration over all instances, 8 streams",
+                               f"one CUDA-graph-captured Adam iteration over all instances; "
+                               f"{len(inv.groups)} groups of equal instances, each one call with "
+                               f"per-shot constants, on 8 streams",
                    "cell_steps_per_iter": inv.cell_steps,
                    "l2": "flushed between timed iterations (256 MiB write)"},
         "e2e": {"value": round(dist.world * inv.cell_steps / (e2e_ms * 1e-3) / 1e9, 4),

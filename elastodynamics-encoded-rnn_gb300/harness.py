@@ -326,9 +326,13 @@ class MultiInversion:
     a CUDA graph and replayed (`step`).  group=False runs every instance on
     its own."""
 
-    def __init__(self, ws, device, lr=1e-2, seed=0, nstreams=8, graph=True, group=True):
+    def __init__(self, ws, device, lr=1e-2, seed=0, nstreams=8, graph=True, group=True, path=None,
+                 serial_big=False):
         self.ws = ws
         self.device = device
+        if path is not None:
+            for w in ws:
+                w.path = path
         self.invs = [Inversion(w, device, lr=lr, seed=seed + k) for k, w in enumerate(ws)]
         keyed = {}
         for k, (w, inv) in enumerate(zip(ws, self.invs)):
@@ -338,16 +342,18 @@ class MultiInversion:
         # largest work first: the longest groups start earliest on the streams
         members = sorted(keyed.values(), key=lambda g: -sum(i.w.cell_steps for i in g))
         self.groups = [_InstanceGroup(g, device, 0.4 * len(g) / len(ws)) for g in members]
-        # groups large enough for the tiled kernels (which fill the GPU on
-        # their own) run one after another on the first stream; the smaller
-        # ones share the remaining streams and overlap with them
+        # streams: round robin over the groups, or (serial_big) groups large
+        # enough for the tiled kernels one after another on the first stream
+        # and the smaller ones on the others
         sms = torch.cuda.get_device_properties(device).multi_processor_count
         big = lambda g: g.geom.nshots * -(-g.geom.nx // 32) * -(-g.geom.ny // 64) >= 4 * sms
         nsmall = max(1, nstreams - 1)
         small = 0
         self.stream_of = []
-        for g in self.groups:
-            if big(g) or nstreams == 1:
+        for k, g in enumerate(self.groups):
+            if not serial_big:
+                self.stream_of.append(k % nstreams)
+            elif big(g) or nstreams == 1:
                 self.stream_of.append(0)
             else:
                 self.stream_of.append(1 + small % nsmall)
