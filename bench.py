@@ -183,6 +183,10 @@ def cpu_sample(workload, nt_sample, iters=2):
     torch.set_num_threads(threads)
     w = Hn.WORKLOADS[workload]()
     dev = torch.device("cpu")
+    if w.extra.get("fields"):
+        t = fields_reference_iteration(w, nt_sample, dev, iters)
+        return (w.nx * w.ny * nt_sample / t / 1e9, threads,
+                f"{workload} grid, {nt_sample} of {w.nt} steps, six constant fields, best of {iters}")
     sig = torch.tensor(Hn.sources.hann_burst_signal(nt_sample, Hn.DT, w.f0, 5, w.amplitude),
                        dtype=torch.float32)[None].repeat(w.nshots, 1)
     pos = [Hn.sources.cell_position(i, j, w.nx, w.ny, Hn.H) for (i, j) in w.src_cells]
@@ -209,6 +213,47 @@ def cpu_sample(workload, nt_sample, iters=2):
     t = min(times)
     cells = w.nshots * w.nx * w.ny * nt_sample
     return cells / t / 1e9, threads, f"{workload} grid, {nt_sample} of {w.nt} steps, {w.nshots} shot(s), best of {iters}"
+
+
+def fields_reference_iteration(w, nt, dev, iters):
+    """The reference damage loop restated op for op (oracle/torch_ref.py on six
+    per-cell constant fields, autograd): forward with dense history every
+    `stride` steps, 5:1 misfit on every 2nd frame + TV, backward, Adam.
+    Returns the best time of `iters` iterations in seconds."""
+    import ernn_gb300.harness as Hn
+    from ernn_gb300 import sources as Src
+    from oracle import torch_ref
+    c = Hn.FIELDS301
+    h = c["L"] / (w.nx - 1)
+    dt = c["total_time"] / (c["nt"] - 1)
+    X, Y = Src.centered_grid(w.nx, w.ny, h, device=dev)
+    load = Src.gaussian_point_load(X, Y, 0.0, 0.0, c["gaussian_param"]).t()[None].contiguous()
+    tt = np.arange(nt) * dt
+    sig = torch.tensor(Src.ricker_wavelet(tt, c["f0"], c["t0"], c["amplitude"]), dtype=torch.float32,
+                       device=dev)[None]
+    logs = [torch.nn.Parameter(torch.full((1, w.nx, w.ny), float(np.log(v)), device=dev)) for v in c["C0"]]
+    rho = torch.tensor(c["rho"], device=dev)
+    opt = torch.optim.Adam(logs, lr=c["lr"])
+    with torch.no_grad():
+        tx, ty = torch_ref.propagate([torch.exp(p) for p in logs], rho, w.nx, w.ny, nt, h, dt, sig, load,
+                                     w.stride)
+    times = []
+    for _ in range(iters):
+        if dev.type == "cuda":
+            torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        opt.zero_grad()
+        C = [torch.exp(p) for p in logs]
+        px, py = torch_ref.propagate(C, rho, w.nx, w.ny, nt, h, dt, sig, load, w.stride)
+        loss = 5 * torch.mean((px[:, ::2] - tx[:, ::2]) ** 2) + torch.mean((py[:, ::2] - ty[:, ::2]) ** 2)
+        tv = sum(torch.sum(torch.abs(f[:, 1:] - f[:, :-1])) + torch.sum(torch.abs(f[:, :, 1:] - f[:, :, :-1]))
+                 for f in C)
+        (loss + c["lambda_tv"] * tv).backward()
+        opt.step()
+        if dev.type == "cuda":
+            torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    return min(times)
 
 
 # --------------------------------------------------------------------------
@@ -339,7 +384,8 @@ def run_ernn(args, dist):
         "dtype": "f32",
         "data": "synthetic (seeded tone-burst shots; observations = same forward at true constants + 0.5% noise)",
         "config": {"workload": f"{w.name}: {w.nx}x{w.ny} grid, {w.nt} steps, {w.nshots} shot(s), "
-                               f"{len(w.rec_cells)} receivers, {'D-field' if w.D_true is not None else 'scalar constants'}, "
+                               f"{len(w.rec_cells)} receivers, "
+                               f"{'six constant fields' if w.extra.get('fields') else 'D-field' if w.D_true is not None else 'scalar constants'}, "
                                f"ckpt every {inv.geom.ckpt_k} steps",
                    "cell_steps_per_iter": w.cell_steps,
                    "kernel_path": {0: "auto", 1: "step", 2: "resident", 3: "tiled"}[int(lib.ernn_last_path())],
@@ -570,7 +616,12 @@ def run_reference(args, dist):
                 "d2h_bytes_per_step": 0},
     }
     if torch.cuda.is_available():
-        rec["gpu_autograd"] = gpu_autograd(args, w)
+        if w.extra.get("fields"):
+            t = fields_reference_iteration(w, w.nt, torch.device("cuda", 0), 2)
+            rec["gpu_autograd"] = {"ms_per_iter": round(t * 1e3, 3),
+                                   "value": round(w.nx * w.ny * w.nt / t / 1e9, 5), "unit": "Gcell-steps/s"}
+        else:
+            rec["gpu_autograd"] = gpu_autograd(args, w)
     return rec
 
 

@@ -83,8 +83,17 @@ static cudaError_t tracked(int cls, cudaStream_t st, Fn&& fn, double alg_bytes =
   return cudaGetLastError();
 }
 
+// Tile height of the plain per-step kernels: 32 rows (4 per thread), or 8
+// rows (1 per thread) when a step has fewer than 512 tiles of 32 x 32 — four
+// times the warps for small grids, whose steps are latency bound.
+int step_rows(int nx, int ny, int S) {
+  const long long tiles32 = (long long)S * ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY);
+  return tiles32 < 512 ? 8 : TX;
+}
+
 dim3 step_grid(int nx, int ny, int S) {
-  return dim3((unsigned)((ny + TY - 1) / TY), (unsigned)((nx + TX - 1) / TX), (unsigned)S);
+  const int rows = step_rows(nx, ny, S);
+  return dim3((unsigned)((ny + TY - 1) / TY), (unsigned)((nx + rows - 1) / rows), (unsigned)S);
 }
 
 cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>& fn,
@@ -180,12 +189,13 @@ __device__ __forceinline__ void apply_ks(const KS& k, const Sten& s, float& lx, 
        k.k26h * s.xy_y;
 }
 
-// Stage rows x0-1 .. x0+TX and columns y0-1 .. y0+TY of both components of
+// Stage rows x0-1 .. x0+T and columns y0-1 .. y0+TY of both components of
 // a [comp][cell] state into shared memory, zero outside the grid.
+template <int T>
 __device__ __forceinline__ void stage_pair(float (*sx)[HY], float (*sy)[HY],
                                            const float* __restrict__ base, int nx, int ny,
                                            size_t N, int x0, int y0, int tid) {
-  for (int e = tid; e < HX * HY; e += NTHR) {
+  for (int e = tid; e < (T + 2) * HY; e += NTHR) {
     const int r = e / HY, c = e - r * HY;
     const int gi = x0 + r - 1, gj = y0 + c - 1;
     float vx = 0.f, vy = 0.f;
@@ -200,16 +210,17 @@ __device__ __forceinline__ void stage_pair(float (*sx)[HY], float (*sy)[HY],
 }
 
 // --------------------------------------------------------------------------
-template <int MODE>
+template <int MODE, int T>
 __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
-  __shared__ float sx[HX][HY];
-  __shared__ float sy[HX][HY];
+  constexpr int RPT_ = T / (NTHR / TY);  // rows per thread
+  __shared__ float sx[T + 2][HY];
+  __shared__ float sy[T + 2][HY];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TY + tx;
-  const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, s = blockIdx.z;
+  const int y0 = blockIdx.x * TY, x0 = blockIdx.y * T, s = blockIdx.z;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
   const float* cur = a.cur ? a.cur + (size_t)s * 2 * N : nullptr;
-  stage_pair(sx, sy, cur, nx, ny, N, x0, y0, tid);
+  stage_pair<T>(sx, sy, cur, nx, ny, N, x0, y0, tid);
 
   // Receiver gather of the input state u^i, folded into this launch.
   if (a.gframe >= 0 && blockIdx.x == 0 && blockIdx.y == 0) {
@@ -234,7 +245,7 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
   float* out = a.out + (size_t)s * 2 * N;
   const int gj = y0 + tx;
 #pragma unroll
-  for (int k = 0; k < RPT; ++k) {
+  for (int k = 0; k < RPT_; ++k) {
     const int r = ty + (NTHR / TY) * k;
     const int gi = x0 + r;
     if (gi >= nx || gj >= ny) continue;
@@ -280,14 +291,15 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
 }
 
 // --------------------------------------------------------------------------
-template <int MODE>
+template <int MODE, int T>
 __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   constexpr int NL = (MODE == kModeFields) ? 6 : 2;
-  __shared__ float sl[NL][HX][HY];
-  __shared__ float su[2][HX][HY];
+  constexpr int RPT_ = T / (NTHR / TY);  // rows per thread
+  __shared__ float sl[NL][T + 2][HY];
+  __shared__ float su[2][T + 2][HY];
   __shared__ double red[NTHR / 32][6];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TY + tx;
-  const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, s = blockIdx.z;
+  const int y0 = blockIdx.x * TY, x0 = blockIdx.y * T, s = blockIdx.z;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
   const float* cur = a.cur + (size_t)s * 2 * N;
@@ -296,7 +308,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   const float q = K->q;
 
   // Stage lam^{m+1} (weighted as A^T needs it) and u^m with a one-cell halo.
-  for (int e = tid; e < HX * HY; e += NTHR) {
+  for (int e = tid; e < (T + 2) * HY; e += NTHR) {
     const int r = e / HY, c = e - r * HY;
     const int gi = x0 + r - 1, gj = y0 + c - 1;
     const bool in = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
@@ -341,9 +353,9 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   float* out = a.out + (size_t)s * 2 * N;
   const int gj = y0 + tx;
   float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // this thread's cells, one step
-  float nvx[RPT], nvy[RPT];
+  float nvx[RPT_], nvy[RPT_];
 #pragma unroll
-  for (int k = 0; k < RPT; ++k) {
+  for (int k = 0; k < RPT_; ++k) {
     nvx[k] = 0.f;
     nvy[k] = 0.f;
     const int r = ty + (NTHR / TY) * k;
@@ -406,7 +418,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   if (inject) {
     __syncthreads();  // everyone is done reading su
 #pragma unroll
-    for (int k = 0; k < RPT; ++k) {
+    for (int k = 0; k < RPT_; ++k) {
       const int r = ty + (NTHR / TY) * k;
       su[0][r][tx] = nvx[k];
       su[1][r][tx] = nvy[k];
@@ -416,7 +428,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
       const int32_t idx = a.rec_idx[(size_t)s * a.nrec + rr];
       if (idx < 0 || (size_t)idx >= N) continue;  // out of range: ignored
       const int gi = idx / ny, gjj = idx - gi * ny;
-      if (gi >= x0 && gi < x0 + TX && gjj >= y0 && gjj < y0 + TY) {
+      if (gi >= x0 && gi < x0 + T && gjj >= y0 && gjj < y0 + TY) {
         const size_t go = ((size_t)s * a.nt_out + a.frame) * a.nrec + rr;
         atomicAdd(&su[0][gi - x0][gjj - y0], gs * a.g_x[go]);
         atomicAdd(&su[1][gi - x0][gjj - y0], gs * a.g_y[go]);
@@ -424,14 +436,14 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < RPT; ++k) {
+    for (int k = 0; k < RPT_; ++k) {
       const int r = ty + (NTHR / TY) * k;
       nvx[k] = su[0][r][tx];
       nvy[k] = su[1][r][tx];
     }
   }
 #pragma unroll
-  for (int k = 0; k < RPT; ++k) {
+  for (int k = 0; k < RPT_; ++k) {
     const int gi = x0 + ty + (NTHR / TY) * k;
     if (gi >= nx || gj >= ny) continue;
     const size_t o = (size_t)gi * ny + gj;
@@ -621,24 +633,44 @@ cudaError_t launch_coef(int mode, const float* C, const float* rho, double h, do
 
 cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st) {
   const dim3 grid = step_grid(a.nx, a.ny, a.S), block(TY, NTHR / TY);
+  const bool small = step_rows(a.nx, a.ny, a.S) != TX;
   const double cells = (double)a.S * a.nx * a.ny;
   return tracked(kProfForward, st, [&] {
     switch (mode) {
-      case kModeScalar: fwd_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
-      case kModeDField: fwd_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
-      default: fwd_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
+      case kModeScalar:
+        if (small) fwd_step_kernel<kModeScalar, 8><<<grid, block, 0, st>>>(a);
+        else fwd_step_kernel<kModeScalar, TX><<<grid, block, 0, st>>>(a);
+        break;
+      case kModeDField:
+        if (small) fwd_step_kernel<kModeDField, 8><<<grid, block, 0, st>>>(a);
+        else fwd_step_kernel<kModeDField, TX><<<grid, block, 0, st>>>(a);
+        break;
+      default:
+        if (small) fwd_step_kernel<kModeFields, 8><<<grid, block, 0, st>>>(a);
+        else fwd_step_kernel<kModeFields, TX><<<grid, block, 0, st>>>(a);
+        break;
     }
   }, cells * alg_bytes_forward(mode));
 }
 
 cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st) {
   const dim3 grid = step_grid(a.nx, a.ny, a.S), block(TY, NTHR / TY);
+  const bool small = step_rows(a.nx, a.ny, a.S) != TX;
   const double cells = (double)a.S * a.nx * a.ny;
   return tracked(kProfAdjoint, st, [&] {
     switch (mode) {
-      case kModeScalar: adj_step_kernel<kModeScalar><<<grid, block, 0, st>>>(a); break;
-      case kModeDField: adj_step_kernel<kModeDField><<<grid, block, 0, st>>>(a); break;
-      default: adj_step_kernel<kModeFields><<<grid, block, 0, st>>>(a); break;
+      case kModeScalar:
+        if (small) adj_step_kernel<kModeScalar, 8><<<grid, block, 0, st>>>(a);
+        else adj_step_kernel<kModeScalar, TX><<<grid, block, 0, st>>>(a);
+        break;
+      case kModeDField:
+        if (small) adj_step_kernel<kModeDField, 8><<<grid, block, 0, st>>>(a);
+        else adj_step_kernel<kModeDField, TX><<<grid, block, 0, st>>>(a);
+        break;
+      default:
+        if (small) adj_step_kernel<kModeFields, 8><<<grid, block, 0, st>>>(a);
+        else adj_step_kernel<kModeFields, TX><<<grid, block, 0, st>>>(a);
+        break;
     }
   }, cells * alg_bytes_adjoint(mode));
 }

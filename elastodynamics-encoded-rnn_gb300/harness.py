@@ -103,8 +103,25 @@ def damage512(ckpt_k=None, nt=3000):
                     ckpt_k=ckpt_k, D_true=damage_map(512, 512))
 
 
+# The damage loop of the reference (Damage_inversion/Inversion_adam.py:815-1000)
+# on its generator's grid: 301^2 nodes over 0.4 m, 4001 steps over 120 us,
+# history every 5 steps, loss on every 2nd frame with TV 1e-21, Adam lr 0.02
+# on the six log-constant fields; run through the drop-in
+# SpatiallyVaryingAnisotropicSimulator (six-field mode).
+FIELDS301 = dict(nx=301, L=0.4, nt=4001, total_time=120e-6, stride=5, ts=2, lambda_tv=1e-21,
+                 lr=0.02, C0=(130.74e9, 11.50e9, 10.49e9, 30.67e9, 3.75e9, 14.77e9), rho=1610.0,
+                 f0=100e3, t0=10e-6, amplitude=1e10, gaussian_param=5e6)
+
+
+def fields301():
+    c = FIELDS301
+    return Workload("fields301", c["nx"], c["nx"], c["nt"], np.asarray(c["C0"]), [(c["nx"] // 2, c["nx"] // 2)],
+                    [], stride=c["stride"], f0=c["f0"], amplitude=c["amplitude"],
+                    gaussian_param=c["gaussian_param"], extra={"fields": True})
+
+
 WORKLOADS = {"plate128": plate128, "rot256": rot256, "shots1024": shots1024,
-             "damage512": damage512}
+             "damage512": damage512, "fields301": fields301}
 
 
 def geometry(w: Workload, device, nt=None) -> Geometry:
@@ -253,8 +270,68 @@ class DamageInversion:
         return self.D.grad
 
 
+class FieldsInversion:
+    """One iteration of the reference's damage loop on the drop-in simulator:
+    six per-cell log-constant fields, the 5:1 misfit on every 2nd frame of the
+    dense history plus the TV term, Adam.  The observations are the forward
+    of the same simulator with the constants halved inside a 2 cm circle
+    (the damaged-plate generator's default region) plus 0.5 % noise."""
+
+    def __init__(self, w: Workload, device, lr=None, seed=0, nt=None):
+        from .simulators import SpatiallyVaryingAnisotropicSimulator, damage_loss
+        c = FIELDS301
+        self.w = w
+        self.device = device
+        nt = w.nt if nt is None else nt
+        h = c["L"] / (w.nx - 1)
+        C0 = dict(zip(("C11_init", "C22_init", "C12_init", "C16_init", "C26_init", "C66_init"), c["C0"]))
+        make = lambda: SpatiallyVaryingAnisotropicSimulator(
+            (w.nx, w.ny), h, c["total_time"] / (c["nt"] - 1), nt, w.stride, source_f0=c["f0"],
+            source_t0=c["t0"], source_amplitude=c["amplitude"], total_time=c["total_time"],
+            rho_known=c["rho"], gaussian_param=c["gaussian_param"], **C0).to(device)
+        self.loss_fn = damage_loss
+        true = make()
+        x = (torch.arange(w.nx, device=device) - (w.nx - 1) / 2) * h
+        X, Y = torch.meshgrid(x, x, indexing="ij")
+        damaged = (((X - 0.1) ** 2 + (Y - 0.1) ** 2).sqrt() <= 0.02)[None]
+        with torch.no_grad():
+            for n in ("log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66"):
+                getattr(true, n).add_(damaged * float(np.log(0.5)))
+            tx, ty = true()
+            g = torch.Generator(device=device).manual_seed(seed)
+            tx = tx + 0.005 * tx.std() * torch.randn(tx.shape, generator=g, device=device)
+            ty = ty + 0.005 * ty.std() * torch.randn(ty.shape, generator=g, device=device)
+        del true
+        self.sim = make()
+        self.obs = (tx.contiguous(), ty.contiguous())
+        self.opt = torch.optim.Adam(self.sim.parameters(), lr=c["lr"] if lr is None else lr)
+
+    @property
+    def geom(self):
+        return self.sim.geometry()
+
+    def step(self, obs=None):
+        obs = self.obs if obs is None else obs
+        self.opt.zero_grad(set_to_none=True)
+        ux, uy = self.sim()
+        loss, _, _ = self.loss_fn(self.sim, ux, uy, obs[0], obs[1], FIELDS301["ts"], FIELDS301["lambda_tv"])
+        loss.backward()
+        self.opt.step()
+        return loss
+
+    def forward_only(self):
+        with torch.no_grad():
+            return self.sim()
+
+    def gradient(self):
+        return torch.cat([p.grad.reshape(-1) for p in self.sim.parameters()])
+
+
 def make_inversion(w: Workload, device, **kw):
-    """The inversion iteration matching the workload (constants or degradation map)."""
+    """The inversion iteration matching the workload (constants, degradation
+    map, or six constant fields)."""
+    if w.extra.get("fields"):
+        return FieldsInversion(w, device, **kw)
     return DamageInversion(w, device, **kw) if w.D_true is not None else Inversion(w, device, **kw)
 
 

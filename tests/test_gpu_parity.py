@@ -70,6 +70,11 @@ CASES = {
     "x_force_stride_gt_nt": dict(src_comp=0, stride=200, nt=60),
     "duplicate_receivers": dict(record=O.RECORD_RECEIVERS, nrec=5, dup_receiver=True),
     "wide_multi_tile": dict(nx=70, ny=97, nt=80, S=2, stride=4),
+    # >= 512 tiles of 32 x 32: the 32-row tiles of the plain kernels (smaller
+    # problems take 8-row tiles)
+    "large_32row_tiles": dict(nx=512, ny=512, nt=18, S=2, stride=3, record=O.RECORD_RECEIVERS, nrec=20),
+    "large_32row_fields": dict(mode=O.MODE_FIELDS, nx=512, ny=520, nt=12, S=2, stride=2),
+    "large_32row_dfield": dict(mode=O.MODE_DFIELD, nx=520, ny=512, nt=12, S=2, record=O.RECORD_RECEIVERS),
 }
 
 
