@@ -56,6 +56,8 @@ def parse(argv=None):
     ap.add_argument("--ckpt", type=int, default=None, help="override the checkpoint interval")
     ap.add_argument("--path", choices=list(PATHS), default="auto",
                     help="kernel path of the library (auto picks per problem)")
+    ap.add_argument("--eager", action="store_true",
+                    help="launch every iteration from the host instead of replaying a CUDA graph")
     ap.add_argument("--plain", action="store_true",
                     help="only run warmup + steps iterations (no timing, no JSON): a profiling target")
     return ap.parse_args(argv)
@@ -274,6 +276,8 @@ def run_ernn(args, dist):
         D = inv.D.detach() if damage else None
         tuned = autotune.tune(inv.geom, C.detach(), inv.rho, D=D)
         inv.geom.path, inv.geom.ckpt_k = tuned
+    if not args.eager:  # the whole iteration as one CUDA graph, replayed per step
+        inv.capture()
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(max(args.warmup, 0)):
         inv.step()
@@ -341,9 +345,14 @@ def run_ernn(args, dist):
     torch.cuda.synchronize()
     fwd_ms = dist.max(sum(a.elapsed_time(b) for a, b in fev) / args.steps)
 
-    # ---- dominant kernel: per-launch device time from library events
+    # ---- dominant kernel: per-launch device time from library events (an
+    # eager iteration: a graph replay makes no library host calls)
     E._lib.profile(True)
-    inv.step()
+    n_eager = lib.ernn_launch_count()
+    inv.step_eager()
+    per_iter = lib.ernn_launch_count() - n_eager   # library kernels of one iteration
+    if inv.graph is not None:  # replays launch the captured kernels without host calls
+        launches = per_iter
     torch.cuda.synchronize()
     prof = E._lib.profile_read()
     E._lib.profile(False)
@@ -389,6 +398,7 @@ def run_ernn(args, dist):
                                f"ckpt every {inv.geom.ckpt_k} steps",
                    "cell_steps_per_iter": w.cell_steps,
                    "kernel_path": {0: "auto", 1: "step", 2: "resident", 3: "tiled"}[int(lib.ernn_last_path())],
+                   "launch": "one CUDA graph per iteration" if inv.graph is not None else "eager",
                    "path_choice": "measured (autotune)" if tuned else args.path,
                    "l2": "flushed between timed iterations (256 MiB write)",
                    "parallelism": f"replicas x{dist.world}"},

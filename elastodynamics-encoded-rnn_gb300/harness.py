@@ -200,21 +200,62 @@ def scales(C_true):
     return np.where(C > 0, C, 0.05 * C.max())
 
 
-class Inversion:
+class _GraphedIteration:
+    """CUDA-graph replay of an inversion iteration: `capture()` warms the
+    iteration up on a side stream (allocator pools, library caches, the
+    checkpoint choice), then records one iteration — the library's time
+    loops, the misfit, the adjoint and the optimiser step — as one graph;
+    `step(obs)` copies new observations into the captured input tensors and
+    replays it.  `step_eager()` runs the same iteration without the graph."""
+
+    graph = None
+    _loss = None
+
+    def capture(self):
+        dev = self.device
+        for group in self.opt.param_groups:  # optimiser state kept on the device
+            group["capturable"] = True
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                self.step_eager()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        check_device_status()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._loss = self.step_eager()
+        return self
+
+    def step(self, obs=None):
+        if obs is not None:
+            for dst, src in zip(self.obs, obs):
+                if dst.data_ptr() != src.data_ptr():
+                    dst.copy_(src, non_blocking=True)
+        if self.graph is None:
+            return self.step_eager()
+        self.graph.replay()
+        return self._loss
+
+
+class Inversion(_GraphedIteration):
     """One inversion iteration of the scalar-constant workloads."""
 
-    def __init__(self, w: Workload, device, lr=1e-2, seed=0, nt=None):
+    def __init__(self, w: Workload, device, lr=1e-2, seed=0, nt=None, graph=False):
         self.w = w
         self.device = device
         self.geom = geometry(w, device, nt)
         self.obs = observed(w, self.geom, device, seed=seed)
         self.rho = torch.tensor(RHO, device=device)
         self.params = NormalisedConstants(initial_guess(w, seed), scales(w.C_true)).to(device)
-        self.opt = torch.optim.Adam(self.params.parameters(), lr=lr)
+        self.opt = torch.optim.Adam(self.params.parameters(), lr=lr, capturable=graph)
+        if graph:
+            self.capture()
 
-    def step(self, obs=None):
-        obs = self.obs if obs is None else obs
-        self.opt.zero_grad(set_to_none=True)
+    def step_eager(self):
+        obs = self.obs
+        self.opt.zero_grad(set_to_none=False)
         ux, uy = propagate(self.params(), self.rho, self.geom)
         loss = trace_misfit(ux, uy, obs[0], obs[1])
         loss.backward()
@@ -237,11 +278,11 @@ class Inversion:
         return np.abs(C - T) / sc
 
 
-class DamageInversion:
+class DamageInversion(_GraphedIteration):
     """One inversion iteration of the degradation-map workload: D(x) trained by
     Adam with C(x) = (1 - D(x)) C0 (initial guess D = 0)."""
 
-    def __init__(self, w: Workload, device, lr=1e-2, seed=0, nt=None):
+    def __init__(self, w: Workload, device, lr=1e-2, seed=0, nt=None, graph=False):
         if w.D_true is None:
             raise ValueError("workload has no degradation map")
         self.w = w
@@ -251,11 +292,13 @@ class DamageInversion:
         self.rho = torch.tensor(RHO, device=device)
         self.C0 = torch.tensor(w.C_true, dtype=torch.float32, device=device)
         self.D = torch.nn.Parameter(torch.zeros((w.nx, w.ny), device=device))
-        self.opt = torch.optim.Adam([self.D], lr=lr)
+        self.opt = torch.optim.Adam([self.D], lr=lr, capturable=graph)
+        if graph:
+            self.capture()
 
-    def step(self, obs=None):
-        obs = self.obs if obs is None else obs
-        self.opt.zero_grad(set_to_none=True)
+    def step_eager(self):
+        obs = self.obs
+        self.opt.zero_grad(set_to_none=False)
         ux, uy = propagate(self.C0, self.rho, self.geom, D=self.D)
         loss = trace_misfit(ux, uy, obs[0], obs[1])
         loss.backward()
@@ -270,14 +313,14 @@ class DamageInversion:
         return self.D.grad
 
 
-class FieldsInversion:
+class FieldsInversion(_GraphedIteration):
     """One iteration of the reference's damage loop on the drop-in simulator:
     six per-cell log-constant fields, the 5:1 misfit on every 2nd frame of the
     dense history plus the TV term, Adam.  The observations are the forward
     of the same simulator with the constants halved inside a 2 cm circle
     (the damaged-plate generator's default region) plus 0.5 % noise."""
 
-    def __init__(self, w: Workload, device, lr=None, seed=0, nt=None):
+    def __init__(self, w: Workload, device, lr=None, seed=0, nt=None, graph=False):
         from .simulators import SpatiallyVaryingAnisotropicSimulator, damage_loss
         c = FIELDS301
         self.w = w
@@ -303,16 +346,21 @@ class FieldsInversion:
             ty = ty + 0.005 * ty.std() * torch.randn(ty.shape, generator=g, device=device)
         del true
         self.sim = make()
+        from .propagate import MODE_FIELDS, choose_ckpt_k
+        self.sim.ckpt_k = choose_ckpt_k(self.sim.geometry(), MODE_FIELDS, device)  # fixed before any capture
         self.obs = (tx.contiguous(), ty.contiguous())
-        self.opt = torch.optim.Adam(self.sim.parameters(), lr=c["lr"] if lr is None else lr)
+        self.opt = torch.optim.Adam(self.sim.parameters(), lr=c["lr"] if lr is None else lr,
+                                    capturable=graph)
+        if graph:
+            self.capture()
 
     @property
     def geom(self):
         return self.sim.geometry()
 
-    def step(self, obs=None):
-        obs = self.obs if obs is None else obs
-        self.opt.zero_grad(set_to_none=True)
+    def step_eager(self):
+        obs = self.obs
+        self.opt.zero_grad(set_to_none=False)
         ux, uy = self.sim()
         loss, _, _ = self.loss_fn(self.sim, ux, uy, obs[0], obs[1], FIELDS301["ts"], FIELDS301["lambda_tv"])
         loss.backward()

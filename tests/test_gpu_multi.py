@@ -58,3 +58,26 @@ def test_grouped_instances_match_separate_runs():
     gg = g.gradient().detach().cpu().numpy().astype(np.float64)
     ge = e.gradient().detach().cpu().numpy().astype(np.float64)
     assert rel(gg, ge) <= 1e-5, rel(gg, ge)
+
+
+@pytest.mark.parametrize("make", ["plate", "damage"])
+def test_graphed_iteration_matches_eager(make):
+    if make == "plate":
+        w = Hn.plate128()
+        w.nt = 300
+    else:
+        w = Hn.Workload("damage128", 128, 128, 200, Hn.C_ORTHO.copy(), Hn._top(2, 128, 128, margin=16),
+                        Hn._top(16, 128, 128), D_true=Hn.damage_map(128, 128))
+    g = Hn.make_inversion(w, DEV)
+    g.capture()
+    e = Hn.make_inversion(w, DEV)
+    param = (lambda inv: inv.params.theta) if make == "plate" else (lambda inv: inv.D)
+    with torch.no_grad():
+        param(e).copy_(param(g))
+    lg = float(g.step())                 # graph replay
+    le = float(e.step_eager())
+    assert abs(lg - le) <= 1e-6 * abs(le), (lg, le)
+    gg = g.gradient().detach().double().cpu().numpy()
+    ge = e.gradient().detach().double().cpu().numpy()
+    assert rel(gg, ge) <= 1e-6, rel(gg, ge)
+    Hn.check_device_status()
