@@ -434,7 +434,7 @@ def run_multi(args, dist):
     dev = torch.device("cuda", dist.local)
     torch.cuda.set_device(dev)
     lib = E.load_library()
-    ws = Hn.multi_instances(64 if args.nt is None else 64)
+    ws = Hn.multi_instances(64)
     t0 = time.perf_counter()
     inv = Hn.MultiInversion(ws, dev)
     setup_s = time.perf_counter() - t0

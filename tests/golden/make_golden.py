@@ -103,6 +103,31 @@ def param_case(P, dtype, domain=(24, 20), nt=150, stride=5, ts=2, ss=3):
         torch.set_default_dtype(torch.float32)
 
 
+def invert_case(P, domain=(24, 20), nt=150, stride=5, ts=2, ss=3, epochs=6, lr=1e-2):
+    """The reference's own inversion loop, CFRPParameterInverterRicker.invert
+    (Parameter_inversion/Inversion_adam.py:393-483), for a few Adam epochs in
+    float32: its loss and constants after every epoch."""
+    torch.set_default_dtype(torch.float32)
+    def make(C):
+        return P.CFRPWaveSimulatorRicker(
+            domain, H, DT, nt, stride, source_component="y", rho_known=RHO,
+            source_position=(0.0, 0.0),
+            C11_init=C["C11"], C22_init=C["C22"], C12_init=C["C12"],
+            C16_init=C["C16"], C26_init=C["C26"], C66_init=C["C66"], **SRC)
+    with torch.no_grad():
+        tx, ty = make(TRUE)()
+    sim = make(INIT)
+    inv = P.CFRPParameterInverterRicker(sim, tx, ty, secondary_time_stride=ts,
+                                        secondary_space_stride=ss)
+    inv.get_results = lambda *a, **k: None  # the summary printout is not part of the loop
+    inv.invert(max_epochs=epochs, lr=lr)
+    h = inv.history
+    return dict(nx=domain[0], ny=domain[1], nt=nt, stride=stride, ts=ts, ss=ss, h=H, dt=DT, rho=RHO,
+                epochs=epochs, lr=lr, target_ux=tx.double().numpy(), target_uy=ty.double().numpy(),
+                loss=np.array(h["loss"]),
+                params=np.array([h[k] for k in ("C11", "C22", "C12", "C16", "C26", "C66")]).T)
+
+
 def operator_case(P, Dm, dtype, nx=19, ny=16, nsq=17, seed=3):
     torch.set_default_dtype(dtype)
     try:
@@ -252,6 +277,7 @@ def main():
         # the reference run's regularisation weight (Damage_inversion/Inversion_adam.py:827)
         np.savez_compressed(os.path.join(OUT, f"damage_inversion_tv_{tag}.npz"),
                             **damage_case(Dm, dtype, lambda_tv=1e-21))
+    np.savez_compressed(os.path.join(OUT, "param_invert_f32.npz"), **invert_case(P))
     F = load_fem_module()
     torch.set_default_dtype(torch.float32)
     for name, kw in FEM_CASES.items():

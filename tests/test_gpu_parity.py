@@ -417,3 +417,30 @@ def test_receiver_traces_equal_gathered_dense_history(path):
     rec_idx = torch.as_tensor(recs.rec_idx, dtype=torch.int32, device=DEV)
     gx, gy = E.formats.traces_from_history(hx, hy, rec_idx)
     assert torch.equal(gx, tx) and torch.equal(gy, ty)
+
+
+def test_dropin_adam_trajectory_matches_reference_invert():
+    # the reference's own loop (CFRPParameterInverterRicker.invert, float32):
+    # zero_grad, forward, compute_loss, backward, Adam step, record — six
+    # epochs through the drop-in simulator give its losses and constants
+    g = np.load(os.path.join(GOLDEN, "param_invert_f32.npz"))
+    init = dict(C11_init=150e9, C22_init=75e9, C12_init=45e9, C16_init=11e9, C26_init=15e9,
+                C66_init=39e9)
+    sim = E.CFRPWaveSimulatorRicker((int(g["nx"]), int(g["ny"])), float(g["h"]), float(g["dt"]),
+                                    int(g["nt"]), int(g["stride"]), source_component="y",
+                                    source_f0=4e6, source_t0=2.5e-7, source_amplitude=1e10,
+                                    rho_known=float(g["rho"]), gaussian_param=5e6, **init).to(DEV)
+    tx = torch.tensor(g["target_ux"], dtype=torch.float32, device=DEV)
+    ty = torch.tensor(g["target_uy"], dtype=torch.float32, device=DEV)
+    opt = torch.optim.Adam(sim.parameters(), lr=float(g["lr"]), betas=(0.9, 0.999), eps=1e-8)
+    losses, params = [], []
+    for _ in range(int(g["epochs"])):
+        opt.zero_grad()
+        ux, uy = sim(save_all_steps=False)
+        loss = _reference_loss(ux, uy, tx, ty, int(g["ts"]), int(g["ss"]))
+        loss.backward()
+        opt.step()
+        losses.append(loss.item())
+        params.append(sim.get_current_params_values()[:6])
+    assert rel(np.array(losses), g["loss"]) <= 1e-4, (losses, g["loss"])
+    assert rel(np.array(params), g["params"]) <= 1e-6, (params, g["params"])
