@@ -74,9 +74,10 @@ Plan make_plan(const ErnnProblem& p) {
   pl.npart = pl.nblocks > p.nshots * 16 * 8 ? pl.nblocks : p.nshots * 16 * 8;
   if (pl.ncoef > 1 && pl.npart < p.nshots * kTiledRowsPerShot) pl.npart = p.nshots * kTiledRowsPerShot;
   if (p.mode == kModeScalar) off += align_up((size_t)pl.npart * 8 * sizeof(double));
-  // receiver table of the tiled adjoint: one byte per (shot, 64 x 32 tile)
+  // receiver table of the tiled adjoint: one byte per (shot, tile), sized for
+  // its smallest tiles (64 x 16)
   pl.s_tflags = off;
-  if (p.record == kRecordReceivers) off += align_up(tma_tiles(p.nx, p.ny, p.nshots));
+  if (p.record == kRecordReceivers) off += align_up(tma_tiles(p.nx, p.ny, p.nshots, 16));
   pl.s_total = off;
   return pl;
 }
@@ -494,7 +495,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   b.tile_flags = nullptr;
   if (tiled && p->record == kRecordReceivers) {
     uint8_t* flags = reinterpret_cast<uint8_t*>(at(scratch, pl.s_tflags));
-    ERNN_CUDA(launch_tile_flags(in->rec_idx, p->nshots, p->nrec, p->nx, p->ny, flags, st));
+    ERNN_CUDA(launch_tile_flags(p->mode, in->rec_idx, p->nshots, p->nrec, p->nx, p->ny, flags, st));
     b.tile_flags = flags;
   }
 

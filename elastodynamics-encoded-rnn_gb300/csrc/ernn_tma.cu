@@ -166,12 +166,13 @@ struct TileId {
   int shot, x0, y0;
 };
 
+template <int TR>  // tile rows
 __device__ __forceinline__ TileId tile_of(int t, int tiles_x, int tiles_y) {
   const int per_shot = tiles_x * tiles_y;
   TileId id;
   id.shot = t / per_shot;
   const int r = t - id.shot * per_shot;
-  id.x0 = (r / tiles_y) * kTX;
+  id.x0 = (r / tiles_y) * TR;
   id.y0 = (r % tiles_y) * kTY;
   return id;
 }
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(kThreads, 3)
   auto issue = [&](int k) {  // loads of this CTA's k-th tile into stage k & 1
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) return;
-    const TileId id = tile_of(t, tiles_x, tiles_y);
+    const TileId id = tile_of<kTX>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(kThreads, 3)
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = tile_of(t, tiles_x, tiles_y);
+    const TileId id = tile_of<kTX>(t, tiles_x, tiles_y);
     // per-tile scalars, loaded before the wait (coefficients per shot with
     // per-shot constants)
     const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
@@ -353,14 +354,21 @@ __global__ void __launch_bounds__(kThreads, 3)
 // before the wait (keeps two CTAs per SM within shared memory).
 template <int MODE>
 struct AdjLayout {
+  // SCALAR: 64 x 16 tiles, one row per thread (registers allow three CTAs
+  // per SM); DFIELD: 64 x 32 tiles, two rows per thread
+  static constexpr int kTR = (MODE == kModeScalar) ? 16 : 32;  // tile rows
+  static constexpr int kRT = kTR / 16;                         // rows per thread
+  static constexpr int kBHa = kTR + 2;                         // halo box rows
+  static constexpr int kHalo = 2 * kBHa * kBW;
+  static constexpr int kOwn = 2 * kTR * kTY;
   static constexpr int kLam = 0;
-  static constexpr int kPrev = kHaloFloats;  // SCALAR only
+  static constexpr int kPrev = kHalo;  // SCALAR only
   // u^m: own box after lam^{m+2} (SCALAR), halo box (DFIELD)
-  static constexpr int kU = (MODE == kModeScalar) ? kPrev + kOwnFloats : kHaloFloats;
-  static constexpr int kD = kU + kHaloFloats;  // DFIELD only
-  static constexpr int kEnd = (MODE == kModeScalar) ? kU + kOwnFloats : kD + kBH * kBW;
+  static constexpr int kU = (MODE == kModeScalar) ? kPrev + kOwn : kHalo;
+  static constexpr int kD = kU + kHalo;  // DFIELD only
+  static constexpr int kEnd = (MODE == kModeScalar) ? kU + kOwn : kD + kBHa * kBW;
   static constexpr int kStage = (kEnd + 31) / 32 * 32;  // 128-byte multiple
-  static constexpr int kCtasPerSm = 2;
+  static constexpr int kCtasPerSm = (MODE == kModeScalar) ? 3 : 2;
 };
 
 template <int MODE>
@@ -378,8 +386,8 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   const size_t N = (size_t)nx * ny;
   const int ntiles = a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(MODE == kModeScalar
-                                        ? kHaloFloats + kOwnFloats + (has_u ? kOwnFloats : 0)
-                                        : kHaloFloats + kBH * kBW + (has_u ? kHaloFloats : 0)) * 4u;
+                                        ? L::kHalo + L::kOwn + (has_u ? L::kOwn : 0)
+                                        : L::kHalo + L::kBHa * kBW + (has_u ? L::kHalo : 0)) * 4u;
   __shared__ int done[2];
   if (tid == 0) {
     bar_init(&bar[0]);
@@ -392,7 +400,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   auto issue = [&](int k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) return;
-    const TileId id = tile_of(t, tiles_x, tiles_y);
+    const TileId id = tile_of<L::kTR>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * L::kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
@@ -443,21 +451,21 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = tile_of(t, tiles_x, tiles_y);
+    const TileId id = tile_of<L::kTR>(t, tiles_x, tiles_y);
     if (MODE == kModeScalar && per_shot && has_u && id.shot != acc_shot) {
       if (acc_shot >= 0) flush(acc_shot);
       acc_shot = id.shot;
     }
     const Coefs ks = coefs(a.coef + (size_t)id.shot * a.coef_stride);
     const int gj = id.y0 + j;
-    const int r0 = 2 * rg;
+    const int r0 = L::kRT * rg;
     // receivers in this tile (uniform over the CTA): the injection and its
     // barriers only run where the per-call table says there are some
     const bool tile_inject = inject && (a.tile_flags == nullptr || a.tile_flags[t] != 0);
-    float4 pv[2][2];  // DFIELD: lam^{m+2} of rows r0, r0 + 1 (x, y)
+    float4 pv[L::kRT][2];  // DFIELD: lam^{m+2} of the thread's rows (x, y)
     if (MODE == kModeDField) {
 #pragma unroll
-      for (int q2 = 0; q2 < 2; ++q2) {
+      for (int q2 = 0; q2 < L::kRT; ++q2) {
         const int gi = id.x0 + r0 + q2;
         const size_t o = (size_t)id.shot * 2 * N + (size_t)gi * ny + gj;
         const bool in = gi < nx && gj < ny;
@@ -477,10 +485,10 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         const int32_t idx = a.rec_idx[(size_t)id.shot * a.nrec + rr];
         if (idx < 0 || (size_t)idx >= N) continue;
         const int gi = idx / ny, gjj = idx - gi * ny;
-        if (gi >= id.x0 && gi < id.x0 + kTX && gjj >= id.y0 && gjj < id.y0 + kTY) {
+        if (gi >= id.x0 && gi < id.x0 + L::kTR && gjj >= id.y0 && gjj < id.y0 + kTY) {
           const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * a.nrec + rr;
           atomicAdd(&pb[(gi - id.x0) * kTY + (gjj - id.y0)], -gs * a.g_x[go]);
-          atomicAdd(&pb[kTX * kTY + (gi - id.x0) * kTY + (gjj - id.y0)], -gs * a.g_y[go]);
+          atomicAdd(&pb[L::kTR * kTY + (gi - id.x0) * kTY + (gjj - id.y0)], -gs * a.g_y[go]);
         }
       }
       __syncthreads();
@@ -490,7 +498,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     // A0((1 - D) lam)); the centre value itself stays unweighted
     auto lam_win = [&](int r, float wx_[6], float wy_[6]) {
       win(hb, r, j, wx_);
-      win(hb + kBH * kBW, r, j, wy_);
+      win(hb + L::kBHa * kBW, r, j, wy_);
       if (MODE == kModeDField) {
         float dw[6];
         win(db, r, j, dw);
@@ -507,13 +515,13 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     lam_win(r0 + 1, wx[1], wy[1]);
     if (MODE == kModeDField && has_u) {
       win(ub, r0, j, vx_[0]);
-      win(ub + kBH * kBW, r0, j, vy_[0]);
+      win(ub + L::kBHa * kBW, r0, j, vy_[0]);
       win(ub, r0 + 1, j, vx_[1]);
-      win(ub + kBH * kBW, r0 + 1, j, vy_[1]);
+      win(ub + L::kBHa * kBW, r0 + 1, j, vy_[1]);
     }
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int q2 = 0; q2 < 2; ++q2) {
+    for (int q2 = 0; q2 < L::kRT; ++q2) {
       const int r = r0 + q2;
       lam_win(r + 2, wx[2], wy[2]);
       Sums4 st;
@@ -531,7 +539,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         }
       } else {
         const float4 cx4 = *reinterpret_cast<const float4*>(hb + (r + 1) * kBW + j + 4);
-        const float4 cy4 = *reinterpret_cast<const float4*>(hb + kBH * kBW + (r + 1) * kBW + j + 4);
+        const float4 cy4 = *reinterpret_cast<const float4*>(hb + L::kBHa * kBW + (r + 1) * kBW + j + 4);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           c1x[q] = g4(cx4, q);
@@ -542,7 +550,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       float4 pvx, pvy;
       if (MODE == kModeScalar) {
         pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
-        pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+        pvy = *reinterpret_cast<const float4*>(pb + L::kTR * kTY + r * kTY + j);
       } else {
         pvx = pv[q2][0];
         pvy = pv[q2][1];
@@ -572,7 +580,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       if (MODE == kModeScalar && has_u) {
         // transposed imaging: u^m at the cell times the stencils of lam^{m+1}
         const float4 u4x = *reinterpret_cast<const float4*>(ub + r * kTY + j);
-        const float4 u4y = *reinterpret_cast<const float4*>(ub + kTX * kTY + r * kTY + j);
+        const float4 u4y = *reinterpret_cast<const float4*>(ub + L::kTR * kTY + r * kTY + j);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const float ux = g4(u4x, q), uy = g4(u4y, q);
@@ -586,7 +594,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       }
       if (MODE == kModeDField && has_u) {
         win(ub, r + 2, j, vx_[2]);
-        win(ub + kBH * kBW, r + 2, j, vy_[2]);
+        win(ub + L::kBHa * kBW, r + 2, j, vy_[2]);
         Sums4 su;
         sums4(vx_, vy_, su);
         if (in) {
@@ -625,7 +633,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         const int32_t idx = a.rec_idx[(size_t)id.shot * a.nrec + rr];
         if (idx < 0 || (size_t)idx >= N) continue;
         const int gi = idx / ny, gjj = idx - gi * ny;
-        if (gi >= id.x0 && gi < id.x0 + kTX && gjj >= id.y0 && gjj < id.y0 + kTY) {
+        if (gi >= id.x0 && gi < id.x0 + L::kTR && gjj >= id.y0 && gjj < id.y0 + kTY) {
           const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * a.nrec + rr;
           atomicAdd(out + idx, gs * a.g_x[go]);
           atomicAdd(out + N + idx, gs * a.g_y[go]);
@@ -655,14 +663,14 @@ __device__ int g_selftest_status;
 // Receiver table of the tiled adjoint: flags[(shot, tile)] = 1 where the
 // shot has a receiver in the tile.
 __global__ void tile_flags_kernel(const int32_t* __restrict__ rec_idx, int S, int nrec, int nx, int ny,
-                                  int tiles_x, int tiles_y, uint8_t* __restrict__ flags) {
+                                  int tile_rows, int tiles_x, int tiles_y, uint8_t* __restrict__ flags) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= S * nrec) return;
   const int s = e / nrec;
   const int32_t idx = rec_idx[e];
   if (idx < 0 || (int64_t)idx >= (int64_t)nx * ny) return;  // ignored, as in the kernels
   const int gi = idx / ny, gj = idx - gi * ny;
-  flags[(size_t)s * tiles_x * tiles_y + (size_t)(gi / kTX) * tiles_y + gj / kTY] = 1;
+  flags[(size_t)s * tiles_x * tiles_y + (size_t)(gi / tile_rows) * tiles_y + gj / kTY] = 1;
 }
 
 // ----------------------------------------------------------------- host
@@ -759,14 +767,16 @@ cudaError_t wait_selftest(int* status_host, cudaStream_t st) {
   return cudaStreamSynchronize(st);
 }
 
-cudaError_t launch_tile_flags(const int32_t* rec_idx, int S, int nrec, int nx, int ny, uint8_t* flags,
-                              cudaStream_t st) {
-  const int tiles_x = (nx + kTX - 1) / kTX, tiles_y = (ny + kTY - 1) / kTY;
-  cudaError_t e = cudaMemsetAsync(flags, 0, tma_tiles(nx, ny, S), st);
+cudaError_t launch_tile_flags(int mode, const int32_t* rec_idx, int S, int nrec, int nx, int ny,
+                              uint8_t* flags, cudaStream_t st) {
+  const int tr = tma_adj_tile_rows(mode);
+  const int tiles_x = (nx + tr - 1) / tr, tiles_y = (ny + kTY - 1) / kTY;
+  cudaError_t e = cudaMemsetAsync(flags, 0, tma_tiles(nx, ny, S, tr), st);
   if (e != cudaSuccess) return e;
   const int n = S * nrec;
   return tracked_launch(kProfOther, st, [&] {
-    tile_flags_kernel<<<(n + 255) / 256, 256, 0, st>>>(rec_idx, S, nrec, nx, ny, tiles_x, tiles_y, flags);
+    tile_flags_kernel<<<(n + 255) / 256, 256, 0, st>>>(rec_idx, S, nrec, nx, ny, tr, tiles_x, tiles_y,
+                                                         flags);
   });
 }
 
@@ -776,8 +786,12 @@ bool tma_eligible(int mode, int nx, int ny, int S) {
   return (mode == kModeScalar || mode == kModeDField) && ny % 4 == 0 && encode_fn() != nullptr;
 }
 
-size_t tma_tiles(int nx, int ny, int S) {
-  return (size_t)S * ((nx + kTX - 1) / kTX) * ((ny + kTY - 1) / kTY);
+size_t tma_tiles(int nx, int ny, int S, int tile_rows) {
+  return (size_t)S * ((nx + tile_rows - 1) / tile_rows) * ((ny + kTY - 1) / kTY);
+}
+
+int tma_adj_tile_rows(int mode) {
+  return mode == kModeScalar ? AdjLayout<kModeScalar>::kTR : AdjLayout<kModeDField>::kTR;
 }
 
 namespace {
@@ -817,10 +831,11 @@ bool adj_maps(int mode, const AdjStep& a, CUtensorMap* cur_map, CUtensorMap* pre
   const bool ok = (mode == kModeScalar || (dfield && al16(a.field) && al16(a.gacc))) && a.ny % 4 == 0 &&
                   a.cur != nullptr && a.prev != nullptr && al16(a.cur) && al16(a.prev) && al16(a.out) &&
                   al16(a.u) && (a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
-  return ok && make_map(cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) &&
-         make_map(prev_map, a.prev, a.nx, a.ny, a.S, kTY, kTX) &&
-         make_map(u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, dfield ? kBW : kTY, dfield ? kBH : kTX) &&
-         make_map2(d_map, dfield ? a.field : a.cur, a.nx, a.ny, kBW, kBH);
+  const int tr = tma_adj_tile_rows(mode), bh = tr + 2;
+  return ok && make_map(cur_map, a.cur, a.nx, a.ny, a.S, kBW, bh) &&
+         make_map(prev_map, a.prev, a.nx, a.ny, a.S, kTY, tr) &&
+         make_map(u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, dfield ? kBW : kTY, dfield ? bh : tr) &&
+         make_map2(d_map, dfield ? a.field : a.cur, a.nx, a.ny, kBW, bh);
 }
 }  // namespace
 
@@ -835,7 +850,8 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
   if (!adj_maps(mode, a, &cur_map, &prev_map, &u_map, &d_map)) return launch_adj_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
-  const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
+  const int tr = tma_adj_tile_rows(mode);
+  const int tiles_x = (a.nx + tr - 1) / tr, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.S * tiles_x * tiles_y;
   int grid = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm : AdjLayout<kModeScalar>::kCtasPerSm);
   if (grid > ntiles) grid = ntiles;

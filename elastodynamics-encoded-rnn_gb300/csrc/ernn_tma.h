@@ -13,8 +13,10 @@ bool tma_eligible(int mode, int nx, int ny, int S);
 // Partial-sum rows reserved per shot by the tiled adjoint with per-shot
 // constants (its grid never exceeds this many CTAs).
 constexpr int kTiledRowsPerShot = 1024;
-// Number of 64 x 32 tiles of one step over all shots.
-size_t tma_tiles(int nx, int ny, int S);
+// Number of 64-column tiles of `tile_rows` rows of one step over all shots.
+size_t tma_tiles(int nx, int ny, int S, int tile_rows = 32);
+// Tile rows of the tiled adjoint for a mode (16 SCALAR, 32 DFIELD).
+int tma_adj_tile_rows(int mode);
 // Same contract as launch_fwd_step / launch_adj_step (SCALAR or DFIELD
 // mode); `err` is the call's device error word.
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st);
@@ -23,9 +25,10 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
 // (buffers on 16-byte boundaries, tensor maps encodable) rather than falling
 // back to the plain kernel.
 bool tma_adj_would_run(int mode, const AdjStep& a);
-// Per-call receiver table of the tiled adjoint (tma_tiles bytes at `flags`).
-cudaError_t launch_tile_flags(const int32_t* rec_idx, int S, int nrec, int nx, int ny, uint8_t* flags,
-                              cudaStream_t st);
+// Per-call receiver table of the tiled adjoint of `mode`
+// (tma_tiles(nx, ny, S, tma_adj_tile_rows(mode)) bytes at `flags`).
+cudaError_t launch_tile_flags(int mode, const int32_t* rec_idx, int S, int nrec, int nx, int ny,
+                              uint8_t* flags, cudaStream_t st);
 // Runs one bounded wait that cannot complete and copies the error word it
 // records into *status_host; synchronises `st`.
 cudaError_t wait_selftest(int* status_host, cudaStream_t st);
