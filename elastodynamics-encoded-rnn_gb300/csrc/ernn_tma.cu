@@ -194,20 +194,32 @@ __device__ __forceinline__ float4 one_minus(const float4 d) {
 // Stage: halo box of u^i, own box of u^{i-1}.  DFIELD reads its 4 weights
 // per row straight from global memory (one plane shared by every shot, L2
 // resident).
+// 64 x 16 tiles, one row per thread.
+struct FwdLayout {
+  static constexpr int kTR = 16;         // tile rows
+  static constexpr int kRT = kTR / 16;   // rows per thread
+  static constexpr int kBHa = kTR + 2;   // halo box rows
+  static constexpr int kHalo = 2 * kBHa * kBW;
+  static constexpr int kOwn = 2 * kTR * kTY;
+  static constexpr int kStage = (kHalo + kOwn + 31) / 32 * 32;  // 128-byte multiple
+  static constexpr int kCtasPerSm = 4;
+};
+
 template <int MODE>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
     tma_fwd_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, int tiles_x, int tiles_y, int has_prev,
                    int* err) {
   extern __shared__ float sm_raw[];
   float* sm = aligned128(sm_raw);
-  constexpr int kStage = kHaloFloats + kOwnFloats;
+  using F = FwdLayout;
+  constexpr int kStage = F::kStage;
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * kStage);
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
   const int ntiles = a.S * tiles_x * tiles_y;
-  const uint32_t bytes = (uint32_t)(kHaloFloats + (has_prev ? kOwnFloats : 0)) * 4u;
+  const uint32_t bytes = (uint32_t)(F::kHalo + (has_prev ? F::kOwn : 0)) * 4u;
 
   // receiver gather of the input state u^i, spread over the grid
   if (a.gframe >= 0) {
@@ -232,12 +244,12 @@ __global__ void __launch_bounds__(kThreads, 3)
   auto issue = [&](int k) {  // loads of this CTA's k-th tile into stage k & 1
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) return;
-    const TileId id = tile_of<kTX>(t, tiles_x, tiles_y);
+    const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
     tma_load3(st, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
-    if (has_prev) tma_load3(st + kHaloFloats, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
+    if (has_prev) tma_load3(st + F::kHalo, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
   };
   if (tid == 0) {
     issue(0);
@@ -248,7 +260,7 @@ __global__ void __launch_bounds__(kThreads, 3)
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = tile_of<kTX>(t, tiles_x, tiles_y);
+    const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
     // per-tile scalars, loaded before the wait (coefficients per shot with
     // per-shot constants)
     const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
@@ -256,11 +268,11 @@ __global__ void __launch_bounds__(kThreads, 3)
     const float amp = a.src_signal[(size_t)id.shot * a.nt + a.i] * K->kappa;
     const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
     const int gj = id.y0 + j;
-    const int r0 = 2 * rg;  // tile rows r0, r0 + 1 -> box rows r0 + 1, r0 + 2
-    float4 w4[2];
+    const int r0 = F::kRT * rg;  // tile row r0 + q2 -> box row r0 + q2 + 1
+    float4 w4[F::kRT];
     if (MODE == kModeDField) {  // issued before the wait: overlaps the tile's loads
 #pragma unroll
-      for (int q2 = 0; q2 < 2; ++q2) {
+      for (int q2 = 0; q2 < F::kRT; ++q2) {
         const int gi = id.x0 + r0 + q2;
         w4[q2] = (gi < nx && gj < ny)
                      ? one_minus(__ldg(reinterpret_cast<const float4*>(a.field + (size_t)gi * ny + gj)))
@@ -269,18 +281,18 @@ __global__ void __launch_bounds__(kThreads, 3)
     }
     bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
     const float* hb = sm + (k & 1) * kStage;
-    const float* pb = hb + kHaloFloats;
+    const float* pb = hb + F::kHalo;
     float* out = a.out + (size_t)id.shot * 2 * N;
     float wx[3][6], wy[3][6];
     win(hb, r0, j, wx[0]);
-    win(hb + kBH * kBW, r0, j, wy[0]);
+    win(hb + F::kBHa * kBW, r0, j, wy[0]);
     win(hb, r0 + 1, j, wx[1]);
-    win(hb + kBH * kBW, r0 + 1, j, wy[1]);
+    win(hb + F::kBHa * kBW, r0 + 1, j, wy[1]);
 #pragma unroll
-    for (int q2 = 0; q2 < 2; ++q2) {
+    for (int q2 = 0; q2 < F::kRT; ++q2) {
       const int r = r0 + q2;
       win(hb, r + 2, j, wx[2]);
-      win(hb + kBH * kBW, r + 2, j, wy[2]);
+      win(hb + F::kBHa * kBW, r + 2, j, wy[2]);
       Sums4 st;
       sums4(wx, wy, st);
       const int gi = id.x0 + r;
@@ -289,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 3)
       float4 pvx = make_float4(0.f, 0.f, 0.f, 0.f), pvy = pvx;
       if (has_prev) {
         pvx = *reinterpret_cast<const float4*>(pb + r * kTY + j);
-        pvy = *reinterpret_cast<const float4*>(pb + kTX * kTY + r * kTY + j);
+        pvy = *reinterpret_cast<const float4*>(pb + F::kTR * kTY + r * kTY + j);
       }
       float vx[4], vy[4];
 #pragma unroll
@@ -354,9 +366,9 @@ __global__ void __launch_bounds__(kThreads, 3)
 // before the wait (keeps two CTAs per SM within shared memory).
 template <int MODE>
 struct AdjLayout {
-  // SCALAR: 64 x 16 tiles, one row per thread (registers allow three CTAs
-  // per SM); DFIELD: 64 x 32 tiles, two rows per thread
-  static constexpr int kTR = (MODE == kModeScalar) ? 16 : 32;  // tile rows
+  // 64 x 16 tiles, one row per thread: registers (<= 85) and shared memory
+  // allow three CTAs per SM
+  static constexpr int kTR = 16;                               // tile rows
   static constexpr int kRT = kTR / 16;                         // rows per thread
   static constexpr int kBHa = kTR + 2;                         // halo box rows
   static constexpr int kHalo = 2 * kBHa * kBW;
@@ -368,7 +380,7 @@ struct AdjLayout {
   static constexpr int kD = kU + kHalo;  // DFIELD only
   static constexpr int kEnd = (MODE == kModeScalar) ? kU + kOwn : kD + kBHa * kBW;
   static constexpr int kStage = (kEnd + 31) / 32 * 32;  // 128-byte multiple
-  static constexpr int kCtasPerSm = (MODE == kModeScalar) ? 3 : 2;
+  static constexpr int kCtasPerSm = 3;
 };
 
 template <int MODE>
@@ -726,7 +738,7 @@ bool make_map2(CUtensorMap* m, const float* base, int nx, int ny, int bw, int bh
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-constexpr size_t kFwdSmem = 2 * (size_t)(kHaloFloats + kOwnFloats) * 4 + 16 + 128;
+constexpr size_t kFwdSmem = 2 * (size_t)FwdLayout::kStage * 4 + 16 + 128;
 template <int MODE>
 constexpr size_t adj_smem() {
   return 2 * (size_t)AdjLayout<MODE>::kStage * 4 + 16 + 128;
@@ -805,14 +817,14 @@ cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st
                   a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) && al16(a.copy0) &&
                   al16(a.copy1) && (a.frame < 0 || (al16(a.hist_x) && al16(a.hist_y)));
   CUtensorMap cur_map, prev_map;
-  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, kBH) ||
-      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, a.S, kTY, kTX))
+  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, FwdLayout::kBHa) ||
+      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, a.S, kTY, FwdLayout::kTR))
     return launch_fwd_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
-  const int tiles_x = (a.nx + kTX - 1) / kTX, tiles_y = (a.ny + kTY - 1) / kTY;
+  const int tiles_x = (a.nx + FwdLayout::kTR - 1) / FwdLayout::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.S * tiles_x * tiles_y;
-  int grid = num_sms() * 3;
+  int grid = num_sms() * FwdLayout::kCtasPerSm;
   if (grid > ntiles) grid = ntiles;
   const double cells = (double)a.S * a.nx * a.ny;
   const int hp = a.prev ? 1 : 0;
