@@ -366,9 +366,11 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
 // before the wait (keeps two CTAs per SM within shared memory).
 template <int MODE>
 struct AdjLayout {
-  // 64 x 16 tiles, one row per thread: registers (<= 85) and shared memory
-  // allow three CTAs per SM
-  static constexpr int kTR = 16;                               // tile rows
+  // SCALAR: 64 x 16 tiles, one row per thread (79 registers: three CTAs
+  // per SM).  DFIELD keeps 64 x 32 tiles and two rows per thread: with one
+  // row its three halo windows per output row (lam, u, D) cost more than the
+  // third CTA gains (24.4 vs 21.5 us per damage512 step)
+  static constexpr int kTR = (MODE == kModeScalar) ? 16 : 32;  // tile rows
   static constexpr int kRT = kTR / 16;                         // rows per thread
   static constexpr int kBHa = kTR + 2;                         // halo box rows
   static constexpr int kHalo = 2 * kBHa * kBW;
@@ -380,7 +382,7 @@ struct AdjLayout {
   static constexpr int kD = kU + kHalo;  // DFIELD only
   static constexpr int kEnd = (MODE == kModeScalar) ? kU + kOwn : kD + kBHa * kBW;
   static constexpr int kStage = (kEnd + 31) / 32 * 32;  // 128-byte multiple
-  static constexpr int kCtasPerSm = 3;
+  static constexpr int kCtasPerSm = (MODE == kModeScalar) ? 3 : 2;
 };
 
 template <int MODE>
