@@ -301,6 +301,31 @@ __device__ __forceinline__ void rows_from(const Tile& T, const KSr& ks, const St
   }
 }
 
+// Work unit of a thread in a ring step: (column quad, chunk of consecutive
+// rows).  The split depends only on the CTA's rows and the grid width, so it
+// is computed once per launch (integer divisions out of the step loop).
+struct Unit {
+  int items;        // units of a step; > kResThreads: several per thread
+  int rc;           // rows per chunk
+  bool active;      // single-unit case: this thread has a unit
+  int qc, ra, rb;   // its column quad and rows [ra, rb)
+};
+
+__device__ __forceinline__ Unit unit_of(int rows, int ny) {
+  Unit u;
+  const int ncq = ny / 4;
+  const int nchunk = max(1, kResThreads / ncq);
+  u.rc = (rows + nchunk - 1) / nchunk;
+  u.items = ncq * nchunk;
+  const int it = threadIdx.x;
+  u.active = it < u.items;
+  u.qc = u.active ? it % ncq : 0;
+  const int ch = u.active ? it / ncq : 0;
+  u.ra = ch * u.rc;
+  u.rb = min(u.ra + u.rc, rows);
+  return u;
+}
+
 // One step of the ring: interior rows first (they only read own rows of
 // cur), then wait for the neighbours' boundary rows of cur, then the two
 // boundary rows (pushed to the neighbours).  Work unit: (column quad, chunk
@@ -309,18 +334,16 @@ __device__ __forceinline__ void rows_from(const Tile& T, const KSr& ks, const St
 template <bool LAM, bool DENSE>
 __device__ __forceinline__ void ring_step(const Tile& T, const KSr& ks, const StepCtx& x,
                                           const Rhs& rhs, uint64_t* cur_bar, uint32_t parity,
-                                          bool wait, int* err) {
+                                          bool wait, int* err, const Unit& U) {
   const int ncq = x.ny / 4;
-  const int nchunk = max(1, kResThreads / ncq);
-  const int rc = (x.rows + nchunk - 1) / nchunk;
-  const int items = ncq * nchunk;
+  const int rc = U.rc;
+  const int items = U.items;
   const int last = x.rows - 1;
   if (items <= kResThreads) {
     // one unit per thread: carry the windows over the wait
-    const int it = threadIdx.x;
-    const bool active = it < items;
-    const int qc = active ? it % ncq : 0, ch = active ? it / ncq : 0;
-    const int ra = ch * rc, rb = min(ra + rc, x.rows);
+    const bool active = U.active;
+    const int qc = U.qc;
+    const int ra = U.ra, rb = U.rb;
     const int ia = max(ra, 1), ib = min(rb, last);
     float wx[3][6], wy[3][6];
     if (active && ia < ib) {
@@ -556,6 +579,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   // bytes each ring step receives: both components of one row per neighbour
   const uint32_t halo_bytes = (uint32_t)((has_up ? 1 : 0) + (has_dn ? 1 : 0)) * 2u * (uint32_t)ny * 4u;
   const uint32_t base_b = smem_u32(smem);
+  const Unit U = unit_of(rows, ny);
   StepCtx x;
   x.up_base = has_up ? map_rank(base_b, rank - 1) : 0u;
   x.dn_base = has_dn ? map_rank(base_b, rank + 1) : 0u;
@@ -591,6 +615,12 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     const float* sig = c.src_signal + (size_t)shot * c.nt;
     float amp_next = (f.i0 < f.i1) ? sig[f.i0] : 0.f;
     Rhs rhs{F, 0.f, c.src_comp, nullptr, nullptr, 0.f};
+    // i % stride, i / stride and the checkpoint phases of i + 1, i + 2, kept
+    // as counters (no integer division in the step loop)
+    int st_r = f.i0 % c.stride, st_q = f.i0 / c.stride;
+    const int ck_k = f.ckpt != nullptr ? f.ck_k : 1;
+    int c1_r = (f.i0 + 1) % ck_k, c1_q = (f.i0 + 1) / ck_k;
+    int c2_r = (f.i0 + 2) % ck_k, c2_q = (f.i0 + 2) / ck_k;
     for (int i = f.i0; i < f.i1; ++i) {
       const int t = i - f.i0;
       set_levels(t);
@@ -598,7 +628,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       rhs.amp = amp_next * kappa;
       amp_next = (i + 1 < f.i1) ? sig[i + 1] : 0.f;  // in flight during this step
       const bool w = step_wait(t);
-      ring_step<false, false>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err);
+      ring_step<false, false>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err, U);
       if (w) parity_bits ^= 1u << (t % 3);
       // bulk stores issued after the previous step read a level overwritten two
       // steps from now: make sure they are done reading before the barrier
@@ -610,13 +640,16 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       ptrdiff_t dst_y[4] = {(ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N};  // y plane offset
       if (f.states) dst[0] = f.states + (size_t)(i - f.i0) * f.state_stride + shot_off;
       if (f.ckpt != nullptr) {
-        if ((i + 1) % f.ck_k == 0 && (i + 1) / f.ck_k <= f.ck_nseg - 1)
-          dst[1] = f.ckpt + ((size_t)((i + 1) / f.ck_k - 1) * 2 + 0) * f.state_stride + shot_off;
-        if ((i + 2) % f.ck_k == 0 && (i + 2) / f.ck_k <= f.ck_nseg - 1)
-          dst[2] = f.ckpt + ((size_t)((i + 2) / f.ck_k - 1) * 2 + 1) * f.state_stride + shot_off;
+        if (c1_r == 0 && c1_q <= f.ck_nseg - 1)
+          dst[1] = f.ckpt + ((size_t)(c1_q - 1) * 2 + 0) * f.state_stride + shot_off;
+        if (c2_r == 0 && c2_q <= f.ck_nseg - 1)
+          dst[2] = f.ckpt + ((size_t)(c2_q - 1) * 2 + 1) * f.state_stride + shot_off;
       }
-      const bool rec_step = (i % c.stride) == 0;
-      const int frame = i / c.stride;
+      const bool rec_step = st_r == 0;
+      const int frame = st_q;
+      if (++st_r == c.stride) { st_r = 0; ++st_q; }
+      if (++c1_r == ck_k) { c1_r = 0; ++c1_q; }
+      if (++c2_r == ck_k) { c2_r = 0; ++c2_q; }
       if (DENSE && rec_step && f.hist_x) {
         dst[3] = f.hist_x + ((size_t)shot * c.nt_out + frame) * N;
         dst_y[3] = f.hist_y - f.hist_x;  // the y history relative to the x history
@@ -668,12 +701,15 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       bulk_commit();
     }
     Rhs rhs{nullptr, 0.f, 0, nullptr, nullptr, gs};
+    // (m - 1) % stride and (m - 1) / stride as counters stepping down with m
+    int sm_r = (a.m_hi - 1) % c.stride, sm_q = (a.m_hi - 1) / c.stride;
     for (int m = a.m_hi; m >= a.m_lo + 1; --m) {
       const int t = a.m_hi - m;  // cur = lam^{m+1}, prev = lam^{m+2}, nxt = lam^m
       set_levels(t);
       expect_next(t);
-      const bool src_step = ((m - 1) % c.stride) == 0;
-      const int frame = (m - 1) / c.stride;
+      const bool src_step = sm_r == 0;
+      const int frame = sm_q;
+      if (sm_r == 0) { sm_r = c.stride - 1; --sm_q; } else { --sm_r; }
       if (!DENSE && src_step) {
         // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: subtract g from the own
         // copy of lam^{m+2}, which only the owning thread reads this step
@@ -697,7 +733,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
         rhs.gy = a.g_y + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
       }
       const bool w = step_wait(t);
-      ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err);
+      ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err, U);
       if (w) parity_bits ^= 1u << (t % 3);
       if (tid == 0) bulk_wait_read_all();
       __syncthreads();
