@@ -166,6 +166,35 @@ struct TileId {
   int shot, x0, y0;
 };
 
+// The tiles t = first, first + stride, ... of a CTA, walked in (shot, row
+// block, column block) coordinates: the stride is split once into the same
+// mixed radix, so a step is an addition with two carries, not a division.
+template <int TR>
+struct TileWalk {
+  int shot, xt, yt, ds, dx, dy, tiles_x, tiles_y;
+  __device__ __forceinline__ void init(int first, int stride, int tx, int ty) {
+    tiles_x = tx;
+    tiles_y = ty;
+    const int per = tx * ty;
+    shot = first / per;
+    int r = first - shot * per;
+    xt = r / ty;
+    yt = r - xt * ty;
+    ds = stride / per;
+    r = stride - ds * per;
+    dx = r / ty;
+    dy = r - dx * ty;
+  }
+  __device__ __forceinline__ TileId id() const { return TileId{shot, xt * TR, yt * kTY}; }
+  __device__ __forceinline__ void next() {
+    yt += dy;
+    if (yt >= tiles_y) { yt -= tiles_y; ++xt; }
+    xt += dx;
+    if (xt >= tiles_x) { xt -= tiles_x; ++shot; }
+    shot += ds;
+  }
+};
+
 template <int TR>  // tile rows
 __device__ __forceinline__ TileId tile_of(int t, int tiles_x, int tiles_y) {
   const int per_shot = tiles_x * tiles_y;
@@ -257,10 +286,13 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   }
   const int qc = tid & 15, rg = tid >> 4;
   const int j = 4 * qc;
+  TileWalk<F::kTR> walk;
+  walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
+    const TileId id = walk.id();
+    walk.next();
     // per-tile scalars, loaded before the wait (coefficients per shot with
     // per-shot constants)
     const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
@@ -462,10 +494,13 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     }
     __syncthreads();  // red is free again
   };
+  TileWalk<L::kTR> walk;
+  walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = tile_of<L::kTR>(t, tiles_x, tiles_y);
+    const TileId id = walk.id();
+    walk.next();
     if (MODE == kModeScalar && per_shot && has_u && id.shot != acc_shot) {
       if (acc_shot >= 0) flush(acc_shot);
       acc_shot = id.shot;
