@@ -467,20 +467,23 @@ __device__ void imaging_role(const ResCommon& c, const ResImg& g, int shot, int 
   const size_t N = (size_t)c.nx * c.ny;
   const int ngr = (c.nx + 3) / 4, ncq = c.ny / 4;
   const int nn = g.n_hi - g.n_lo + 1;
-  const long long per_n = (long long)ngr * ncq;
-  const long long total = (long long)nn * per_n;
   double acc64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  for (long long it = (long long)cta * kResThreads + threadIdx.x; it < total;
-       it += (long long)ncta * kResThreads) {
-    const long long r = it;
-    const int dn = (int)(r / per_n);
-    const int rem = (int)(r - (long long)dn * per_n);
-    const int gi = rem / ncq, qc = rem - gi * ncq;
+  // items it = first, first + stride, ... walked as (dn, gi, qc) digits of
+  // radix (nn, ngr, ncq): an addition with carries per item, no division
+  const int first = cta * kResThreads + threadIdx.x, stride = ncta * kResThreads;
+  int qc = first % ncq, gi = (first / ncq) % ngr, dn = first / ncq / ngr;
+  const int sq = stride % ncq, sg = (stride / ncq) % ngr, sd = stride / ncq / ngr;
+  for (; dn < nn;) {
     const size_t slot = (size_t)dn * g.state_stride + (size_t)shot * 2 * N;
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     img_item(g.lbuf + slot, g.ubuf + slot, N, c.nx, c.ny, 4 * gi, 4 * qc, acc);
 #pragma unroll
     for (int t = 0; t < 6; ++t) acc64[t] += (double)acc[t];
+    qc += sq;
+    if (qc >= ncq) { qc -= ncq; ++gi; }
+    gi += sg;
+    if (gi >= ngr) { gi -= ngr; ++dn; }
+    dn += sd;
   }
   block_reduce6(acc64, g.partials + ((size_t)shot * ncta + cta) * 8);
 }
