@@ -58,6 +58,8 @@ def parse(argv=None):
                     help="kernel path of the library (auto picks per problem)")
     ap.add_argument("--eager", action="store_true",
                     help="launch every iteration from the host instead of replaying a CUDA graph")
+    ap.add_argument("--no-overlap", action="store_true",
+                    help="launch consecutive step kernels without programmatic dependent launch")
     ap.add_argument("--plain", action="store_true",
                     help="only run warmup + steps iterations (no timing, no JSON): a profiling target")
     return ap.parse_args(argv)
@@ -398,7 +400,8 @@ def run_ernn(args, dist):
                                f"ckpt every {inv.geom.ckpt_k} steps",
                    "cell_steps_per_iter": w.cell_steps,
                    "kernel_path": {0: "auto", 1: "step", 2: "resident", 3: "tiled"}[int(lib.ernn_last_path())],
-                   "launch": "one CUDA graph per iteration" if inv.graph is not None else "eager",
+                   "launch": ("one CUDA graph per iteration" if inv.graph is not None else "eager") +
+                             ("" if args.no_overlap else ", step kernels overlapped (programmatic dependent launch)"),
                    "path_choice": "measured (autotune)" if tuned else args.path,
                    "l2": "flushed between timed iterations (256 MiB write)",
                    "parallelism": f"replicas x{dist.world}"},
@@ -717,6 +720,9 @@ def gpu_autograd(args, w, iters=3):
 def main():
     args = parse()
     dist = Dist()
+    if args.no_overlap and args.impl == "ernn":
+        from ernn_gb300 import _lib
+        _lib.launch_overlap(False)
     try:
         if args.impl == "reference":
             rec = run_reference(args, dist)

@@ -47,6 +47,13 @@ class ErnnFemProblem(ctypes.Structure):
                 ("out_scale", ctypes.c_double)]
 
 
+class ErnnSeries(ctypes.Structure):
+    """Mirror of struct ErnnSeries (include/ernn.h)."""
+    _fields_ = [("series", ctypes.c_int64), ("frames", ctypes.c_int64), ("nx", ctypes.c_int32),
+                ("ny", ctypes.c_int32), ("frame_stride", ctypes.c_int32), ("space_stride", ctypes.c_int32),
+                ("wx", ctypes.c_double), ("wy", ctypes.c_double)]
+
+
 # name -> (restype, argtypes); the complete exported surface of include/ernn.h
 _P = ctypes.c_void_p
 SIGNATURES = {
@@ -68,8 +75,12 @@ SIGNATURES = {
     "ernn_fem_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(ErnnFemProblem)]),
     "ernn_fem_forward": (ctypes.c_int, [ctypes.POINTER(ErnnFemProblem), _P, _P, _P, _P, _P, _P,
                                         ctypes.c_size_t, _P]),
+    "ernn_misfit_workspace_bytes": (ctypes.c_size_t, []),
+    "ernn_misfit": (ctypes.c_int, [ctypes.POINTER(ErnnSeries), _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "ernn_misfit_grad": (ctypes.c_int, [ctypes.POINTER(ErnnSeries), _P, _P, _P, _P, _P, _P, _P, _P]),
     "ernn_launch_count": (ctypes.c_uint64, []),
     "ernn_last_path": (ctypes.c_int32, []),
+    "ernn_set_launch_overlap": (ctypes.c_int, [ctypes.c_int]),
     "ernn_device_status": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p]),
     "ernn_wait_selftest": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]),
@@ -81,6 +92,12 @@ SIGNATURES = {
 def profile(enable: bool) -> None:
     """Start (True) or stop (False) the library's event timing of its own launches."""
     call("ernn_profile_enable", int(enable))
+
+
+def launch_overlap(on: bool) -> bool:
+    """Turn the launch overlap of consecutive step kernels (programmatic
+    dependent launch) on or off; returns the previous setting."""
+    return bool(load().ernn_set_launch_overlap(int(bool(on))))
 
 
 def profile_read():

@@ -417,6 +417,7 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
     } else if (i >= 1 && (i - 1) % p->stride == 0) {
       a.gframe = (i - 1) / p->stride; a.tr_x = out_ux; a.tr_y = out_uy;
     }
+    a.chained = i > 0;  // step 0 follows the coefficient kernel
     ERNN_CUDA(fwd_step(a));
     last = a.out;
   }
@@ -511,6 +512,8 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     }
   }
   const bool tiled_adj = tiled != 0;
+  // every step launch after the first of the loop below follows a step kernel
+  bool chained = false;
   auto adj_step = [&](int m, const float* um) -> int {
     const int idx = p->nt - m;
     b.m = m;
@@ -519,6 +522,8 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     b.prev = b.out;
     b.u = (m <= p->nt - 1) ? um : nullptr;
     b.frame = ((m - 1) % p->stride == 0) ? (m - 1) / p->stride : -1;
+    b.chained = chained ? 1 : 0;
+    chained = true;
     const cudaError_t e = tiled ? launch_tma_adj(p->mode, b, &coef->err, st) : launch_adj_step(p->mode, b, st);
     return e == cudaSuccess ? ERNN_OK : ERNN_ERR_CUDA;
   };
@@ -538,6 +543,8 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
         a.out = seg(i - i0);
         a.cur = (i == i0) ? ck(j, 0) : seg(i - i0 - 1);
         a.prev = (i == i0) ? ck(j, 1) : (i == i0 + 1 ? ck(j, 0) : seg(i - i0 - 2));
+        a.chained = chained ? 1 : 0;
+        chained = true;
         ERNN_CUDA(tiled ? launch_tma_fwd(p->mode, a, &coef->err, st) : launch_fwd_step(p->mode, a, st));
       }
       for (int m = i1; m >= i0 + 1; --m)
@@ -582,6 +589,12 @@ int ernn_wait_selftest(int32_t* status_host, void* stream) {
 }
 
 int32_t ernn_last_path(void) { return g_last_path.load(std::memory_order_relaxed); }
+
+int ernn_set_launch_overlap(int on) {
+  const int was = launch_overlap_setting() ? 1 : 0;
+  set_launch_overlap(on != 0);
+  return was;
+}
 
 int ernn_profile_enable(int enable) {
   profile_enable(enable != 0);

@@ -46,6 +46,20 @@ struct Coef {
 constexpr long long kWaitLimitCycles = 1ll << 31;
 constexpr int kDeviceTimeout = 5;  // ERNN_ERR_TIMEOUT
 
+// Programmatic dependent launch.  A step kernel launched with the
+// programmatic-serialisation attribute may be scheduled while the previous
+// kernel of its stream still runs.  Every step kernel lets its dependents
+// launch as it starts (grid_dep_trigger: they are only scheduled once every
+// block of this grid has started, so they never take the place of one), loads
+// what no step kernel writes (coefficients, constant planes, source maps,
+// receiver tables, tensor maps), and then waits in grid_dep_wait until the
+// previous grid has completed and its writes are visible, before it reads or
+// writes any state.  Without the attribute both are no-ops.
+__device__ __forceinline__ void grid_dep_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Tile geometry of the per-step kernels: 32 rows (x) by 32 columns (y),
 // 256 threads as 8 row groups of one warp each; a thread owns 4 cells of
 // one column.

@@ -91,21 +91,26 @@ __device__ __forceinline__ void tri(const FemConsts& k, const FemStep& s, size_t
 
 template <bool FIELDS>
 __global__ void __launch_bounds__(256) fem_step_kernel(const FemStep s, const FemConsts k) {
+  grid_dep_trigger();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= s.nx || j >= s.ny) return;
   const int ny = s.ny;
   const size_t o = (size_t)i * ny + j;
+  const bool interior = i > 0 && i < s.nx - 1 && j > 0 && j < ny - 1;
+  // the load term needs no state: formed before the wait
+  const float lf = interior ? s.signal[s.n] * s.load[o] * k.rho_inv : 0.f;
+  grid_dep_wait();  // levels of the previous launch complete from here on
   float vx = 0.f, vy = 0.f;
-  if (i > 0 && i < s.nx - 1 && j > 0 && j < ny - 1) {
+  if (interior) {
     float ux[3][3], uy[3][3];
 #pragma unroll
     for (int di = 0; di < 3; ++di)
 #pragma unroll
       for (int dj = 0; dj < 3; ++dj) {
         const size_t q = o + (size_t)(di - 1) * ny + (dj - 1);
-        ux[di][dj] = __ldg(s.cur_x + q);
-        uy[di][dj] = __ldg(s.cur_y + q);
+        ux[di][dj] = s.cur_x[q];
+        uy[di][dj] = s.cur_y[q];
       }
     float fx = 0.f, fy = 0.f;
     float m;
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(256) fem_step_kernel(const FemStep s, const Fe
       tri<FIELDS, 2, 0, 0, 0>(k, s, o, ux, uy, fx, fy);
       m = k.m_odd;
     }
-    const float fext = (s.signal[s.n] * s.load[o] * k.rho_inv) * m;
+    const float fext = lf * m;
     vx = 2.f * ux[1][1] - s.prev_x[o] - k.dt2 * fx / m;
     vy = 2.f * uy[1][1] - s.prev_y[o] + k.dt2 * (fext - fy) / m;
   }
@@ -248,9 +253,10 @@ extern "C" int ernn_fem_forward(const ErnnFemProblem* p, const float* load, cons
     } else {
       s.frame_x = s.frame_y = nullptr;
     }
+    const bool chained = n > 1;  // the previous launch is the previous level's
     const cudaError_t e = tracked_launch(kProfForward, st, [&] {
-      if (C_fields != nullptr) fem_step_kernel<true><<<grid, block, 0, st>>>(s, k);
-      else fem_step_kernel<false><<<grid, block, 0, st>>>(s, k);
+      if (C_fields != nullptr) launch_step_kernel(fem_step_kernel<true>, grid, block, 0, st, chained, s, k);
+      else launch_step_kernel(fem_step_kernel<false>, grid, block, 0, st, chained, s, k);
     }, (double)N * (C_fields != nullptr ? 52.0 : 28.0));
     if (e != cudaSuccess) return ERNN_ERR_CUDA;
   }

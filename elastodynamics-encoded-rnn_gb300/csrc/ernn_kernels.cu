@@ -33,6 +33,11 @@ struct Profiler {
 Profiler g_prof;
 }  // namespace
 
+static std::atomic<bool> g_overlap{true};
+bool launch_overlap() { return g_overlap.load(std::memory_order_relaxed) && !g_prof.on; }
+bool launch_overlap_setting() { return g_overlap.load(std::memory_order_relaxed); }
+void set_launch_overlap(bool on) { g_overlap.store(on, std::memory_order_relaxed); }
+
 void profile_enable(bool on) {
   g_prof.on = on;
   for (int c = 0; c < kProfClasses; ++c) {
@@ -151,10 +156,10 @@ __device__ __forceinline__ KS load_ks(const Coef* c) {
   return k;
 }
 
-// Per-cell constants of FIELDS mode, scaled by q.
-__device__ __forceinline__ KS cell_ks(const float* __restrict__ f, size_t N, size_t o, float q) {
-  const float C11 = f[o], C22 = f[N + o], C12 = f[2 * N + o];
-  const float C16 = f[3 * N + o], C26 = f[4 * N + o], C66 = f[5 * N + o];
+// Per-cell constants of FIELDS mode (C11, C22, C12, C16, C26, C66 of one
+// cell), scaled by q.
+__device__ __forceinline__ KS cell_ks(const float c[6], float q) {
+  const float C11 = c[0], C22 = c[1], C12 = c[2], C16 = c[3], C26 = c[4], C66 = c[5];
   KS k;
   k.k11 = C11 * q; k.k22 = C22 * q; k.k66 = C66 * q;
   k.k16 = C16 * q; k.k26 = C26 * q;
@@ -215,10 +220,41 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
   constexpr int RPT_ = T / (NTHR / TY);  // rows per thread
   __shared__ float sx[T + 2][HY];
   __shared__ float sy[T + 2][HY];
+  grid_dep_trigger();
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TY + tx;
   const int y0 = blockIdx.x * TY, x0 = blockIdx.y * T, s = blockIdx.z;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
+
+  // Inputs no step writes, loaded before the wait (a chained launch loads
+  // them while the previous step runs): coefficients, source, and the
+  // per-cell constants of the thread's cells (FIELDS: the six planes;
+  // DFIELD: 1 - D).
+  const Coef* K = a.coef + (size_t)s * a.coef_stride;
+  const float amp = a.src_signal[(size_t)s * a.nt + a.i] * K->kappa;
+  const bool has_src = a.bx > 0 && a.by > 0;
+  const int ox = has_src ? a.src_origin[2 * s] : 0, oy = has_src ? a.src_origin[2 * s + 1] : 0;
+  KS ks;
+  if (MODE != kModeFields) ks = load_ks(K);
+  const float q = K->q;
+  const int gj = y0 + tx;
+  float cf[RPT_][MODE == kModeFields ? 6 : 1];
+  if (MODE != kModeScalar) {
+#pragma unroll
+    for (int k = 0; k < RPT_; ++k) {
+      const int gi = x0 + ty + (NTHR / TY) * k;
+      const bool in = gi < nx && gj < ny;
+      const size_t o = in ? (size_t)gi * ny + gj : 0;
+      if (MODE == kModeFields) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) cf[k][c] = in ? a.field[c * N + o] : 0.f;
+      } else {
+        cf[k][0] = in ? 1.f - a.field[o] : 0.f;
+      }
+    }
+  }
+  grid_dep_wait();
+
   const float* cur = a.cur ? a.cur + (size_t)s * 2 * N : nullptr;
   stage_pair<T>(sx, sy, cur, nx, ny, N, x0, y0, tid);
 
@@ -234,16 +270,8 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
   }
   __syncthreads();
 
-  const Coef* K = a.coef + (size_t)s * a.coef_stride;
-  const float amp = a.src_signal[(size_t)s * a.nt + a.i] * K->kappa;
-  const bool has_src = a.bx > 0 && a.by > 0;
-  const int ox = has_src ? a.src_origin[2 * s] : 0, oy = has_src ? a.src_origin[2 * s + 1] : 0;
-  KS ks;
-  if (MODE != kModeFields) ks = load_ks(K);
-  const float q = K->q;
   const float* prev = a.prev ? a.prev + (size_t)s * 2 * N : nullptr;
   float* out = a.out + (size_t)s * 2 * N;
-  const int gj = y0 + tx;
 #pragma unroll
   for (int k = 0; k < RPT_; ++k) {
     const int r = ty + (NTHR / TY) * k;
@@ -253,14 +281,13 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
     const Sten st = stencils(sx, sy, r, tx);
     float lx, ly;
     if (MODE == kModeFields) {
-      const KS kc = cell_ks(a.field, N, o, q);
+      const KS kc = cell_ks(cf[k], q);
       apply_ks(kc, st, lx, ly);
     } else {
       apply_ks(ks, st, lx, ly);
       if (MODE == kModeDField) {
-        const float w = 1.f - a.field[o];
-        lx *= w;
-        ly *= w;
+        lx *= cf[k][0];
+        ly *= cf[k][0];
       }
     }
     const float px = prev ? prev[o] : 0.f;
@@ -298,6 +325,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   __shared__ float sl[NL][T + 2][HY];
   __shared__ float su[2][T + 2][HY];
   __shared__ double red[NTHR / 32][6];
+  grid_dep_trigger();
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TY + tx;
   const int y0 = blockIdx.x * TY, x0 = blockIdx.y * T, s = blockIdx.z;
   const int nx = a.nx, ny = a.ny;
@@ -308,26 +336,55 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   const float q = K->q;
 
   // Stage lam^{m+1} (weighted as A^T needs it) and u^m with a one-cell halo.
-  for (int e = tid; e < (T + 2) * HY; e += NTHR) {
+  // The per-cell constants of the staged cells are loaded before the wait on
+  // 8-row tiles (two staged cells per thread; a chained launch loads them
+  // while the previous step runs), inside the staging loop on 32-row tiles.
+  constexpr int kStaged = (T + 2) * HY;
+  constexpr int kIt = (kStaged + NTHR - 1) / NTHR;
+  constexpr bool kPre = MODE != kModeScalar && T == 8;
+  constexpr int kNF = MODE == kModeFields ? 6 : 1;
+  float fpre[kPre ? kIt : 1][kNF];
+  auto staged_field = [&](int e, float f[kNF]) {
+    const int r = e / HY, c = e - r * HY;
+    const int gi = x0 + r - 1, gj = y0 + c - 1;
+    const bool in = e < kStaged && gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+    const size_t o = in ? (size_t)gi * ny + gj : 0;
+#pragma unroll
+    for (int k = 0; k < kNF; ++k) f[k] = in ? a.field[k * N + o] : 0.f;
+  };
+  if (kPre) {
+#pragma unroll
+    for (int it = 0; it < kIt; ++it) staged_field(tid + it * NTHR, fpre[kPre ? it : 0]);
+  }
+  grid_dep_wait();
+#pragma unroll
+  for (int it = 0; it < kIt; ++it) {
+    const int e = tid + it * NTHR;
+    if (e >= kStaged) break;
     const int r = e / HY, c = e - r * HY;
     const int gi = x0 + r - 1, gj = y0 + c - 1;
     const bool in = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
     const size_t o = in ? (size_t)gi * ny + gj : 0;
     const float lx = in ? cur[o] : 0.f;
     const float ly = in ? cur[N + o] : 0.f;
+    float fv[kNF];
+    if (MODE != kModeScalar) {
+      if (kPre) {
+#pragma unroll
+        for (int k = 0; k < kNF; ++k) fv[k] = fpre[kPre ? it : 0][k];
+      } else {
+        staged_field(e, fv);
+      }
+    }
     if (MODE == kModeScalar) {
       sl[0][r][c] = lx;
       sl[1][r][c] = ly;
     } else if (MODE == kModeDField) {
-      const float w = in ? 1.f - a.field[o] : 0.f;
+      const float w = in ? 1.f - fv[0] : 0.f;
       sl[0][r][c] = w * lx;
       sl[1][r][c] = w * ly;
     } else {
-      float C11 = 0.f, C22 = 0.f, C12 = 0.f, C16 = 0.f, C26 = 0.f, C66 = 0.f;
-      if (in) {
-        C11 = a.field[o]; C22 = a.field[N + o]; C12 = a.field[2 * N + o];
-        C16 = a.field[3 * N + o]; C26 = a.field[4 * N + o]; C66 = a.field[5 * N + o];
-      }
+      const float C11 = fv[0], C22 = fv[1], C12 = fv[2], C16 = fv[3], C26 = fv[4], C66 = fv[5];
       const float c1266 = C12 + C66;
       sl[0][r][c] = C11 * lx + C16 * ly;
       sl[1][r][c] = C66 * lx + C26 * ly;
@@ -638,16 +695,16 @@ cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st) {
   return tracked(kProfForward, st, [&] {
     switch (mode) {
       case kModeScalar:
-        if (small) fwd_step_kernel<kModeScalar, 8><<<grid, block, 0, st>>>(a);
-        else fwd_step_kernel<kModeScalar, TX><<<grid, block, 0, st>>>(a);
+        if (small) launch_step_kernel(fwd_step_kernel<kModeScalar, 8>, grid, block, 0, st, a.chained != 0, a);
+        else launch_step_kernel(fwd_step_kernel<kModeScalar, TX>, grid, block, 0, st, a.chained != 0, a);
         break;
       case kModeDField:
-        if (small) fwd_step_kernel<kModeDField, 8><<<grid, block, 0, st>>>(a);
-        else fwd_step_kernel<kModeDField, TX><<<grid, block, 0, st>>>(a);
+        if (small) launch_step_kernel(fwd_step_kernel<kModeDField, 8>, grid, block, 0, st, a.chained != 0, a);
+        else launch_step_kernel(fwd_step_kernel<kModeDField, TX>, grid, block, 0, st, a.chained != 0, a);
         break;
       default:
-        if (small) fwd_step_kernel<kModeFields, 8><<<grid, block, 0, st>>>(a);
-        else fwd_step_kernel<kModeFields, TX><<<grid, block, 0, st>>>(a);
+        if (small) launch_step_kernel(fwd_step_kernel<kModeFields, 8>, grid, block, 0, st, a.chained != 0, a);
+        else launch_step_kernel(fwd_step_kernel<kModeFields, TX>, grid, block, 0, st, a.chained != 0, a);
         break;
     }
   }, cells * alg_bytes_forward(mode));
@@ -660,16 +717,16 @@ cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st) {
   return tracked(kProfAdjoint, st, [&] {
     switch (mode) {
       case kModeScalar:
-        if (small) adj_step_kernel<kModeScalar, 8><<<grid, block, 0, st>>>(a);
-        else adj_step_kernel<kModeScalar, TX><<<grid, block, 0, st>>>(a);
+        if (small) launch_step_kernel(adj_step_kernel<kModeScalar, 8>, grid, block, 0, st, a.chained != 0, a);
+        else launch_step_kernel(adj_step_kernel<kModeScalar, TX>, grid, block, 0, st, a.chained != 0, a);
         break;
       case kModeDField:
-        if (small) adj_step_kernel<kModeDField, 8><<<grid, block, 0, st>>>(a);
-        else adj_step_kernel<kModeDField, TX><<<grid, block, 0, st>>>(a);
+        if (small) launch_step_kernel(adj_step_kernel<kModeDField, 8>, grid, block, 0, st, a.chained != 0, a);
+        else launch_step_kernel(adj_step_kernel<kModeDField, TX>, grid, block, 0, st, a.chained != 0, a);
         break;
       default:
-        if (small) adj_step_kernel<kModeFields, 8><<<grid, block, 0, st>>>(a);
-        else adj_step_kernel<kModeFields, TX><<<grid, block, 0, st>>>(a);
+        if (small) launch_step_kernel(adj_step_kernel<kModeFields, 8>, grid, block, 0, st, a.chained != 0, a);
+        else launch_step_kernel(adj_step_kernel<kModeFields, TX>, grid, block, 0, st, a.chained != 0, a);
         break;
     }
   }, cells * alg_bytes_adjoint(mode));

@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <functional>
+#include <utility>
 #include <cuda_runtime.h>
 
 #include "ernn_common.cuh"
@@ -36,6 +37,7 @@ struct FwdStep {
   const float* src_map;
   const int32_t* src_origin;
   int bx, by, src_comp;
+  int chained;  // previous launch on the stream is a step kernel of the same loop
 };
 
 // Per-step arguments of the adjoint kernel: computes lam^m from lam^{m+1},
@@ -59,6 +61,7 @@ struct AdjStep {
   // tiled kernels: non-zero for the 64 x 32 tiles (shot-major) holding a
   // receiver, or nullptr (every tile scans the receivers)
   const uint8_t* tile_flags;
+  int chained;  // previous launch on the stream is a step kernel of the same loop
 };
 
 dim3 step_grid(int nx, int ny, int S);
@@ -86,6 +89,32 @@ cudaError_t launch_operator(int S, int nx, int ny, int mode, double h, const flo
 
 uint64_t launches();
 void count_launch();
+
+// Launch overlap of consecutive step kernels (programmatic dependent launch,
+// see grid_dep_wait): on unless switched off, and off while the diagnostic
+// profiler brackets launches with events.
+bool launch_overlap();
+bool launch_overlap_setting();  // the switch alone
+void set_launch_overlap(bool on);
+
+// Enqueue `kernel` on st; `chained`: as a programmatic dependent of the
+// previous kernel on st (a step kernel that calls grid_dep_wait before it
+// touches state).
+template <class... KArgs, class... Args>
+inline void launch_step_kernel(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                               cudaStream_t st, bool chained, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = (chained && launch_overlap()) ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // kernel classes of the diagnostic profiler
 constexpr int kProfForward = 0;

@@ -114,6 +114,7 @@ extern "C" int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, f
     } else if (i >= 1 && (i - 1) % p->stride == 0) {
       a.gframe = (i - 1) / p->stride; a.tr_x = out_ux; a.tr_y = out_uy;
     }
+    a.chained = i > 0;  // step 0 follows the coefficient kernel
     if (launch_fwd_step(p->mode, a, st) != cudaSuccess) return ERNN_ERR_CUDA;
     last = a.out;
   }

@@ -36,6 +36,12 @@ __device__ __forceinline__ uint32_t s32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// Fetch a tensor map (a __grid_constant__ kernel parameter) into the
+// descriptor cache ahead of its first copy.
+__device__ __forceinline__ void prefetch_map(const CUtensorMap* m) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
+}
+
 __device__ __forceinline__ void bar_init(uint64_t* b) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(s32(b)) : "memory");
 }
@@ -249,6 +255,17 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   const size_t N = (size_t)nx * ny;
   const int ntiles = a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(F::kHalo + (has_prev ? F::kOwn : 0)) * 4u;
+  grid_dep_trigger();
+  __shared__ int done[2];
+  if (tid == 0) {
+    prefetch_map(&cur_map);
+    prefetch_map(&prev_map);
+    bar_init(&bar[0]);
+    bar_init(&bar[1]);
+    done[0] = done[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  grid_dep_wait();  // the state of the previous step is complete from here on
 
   // receiver gather of the input state u^i, spread over the grid
   if (a.gframe >= 0) {
@@ -260,13 +277,6 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
       a.tr_x[o] = ok ? a.cur[(size_t)s * 2 * N + idx] : 0.f;
       a.tr_y[o] = ok ? a.cur[(size_t)s * 2 * N + N + idx] : 0.f;
     }
-  }
-  __shared__ int done[2];
-  if (tid == 0) {
-    bar_init(&bar[0]);
-    bar_init(&bar[1]);
-    done[0] = done[1] = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   const bool has_src = a.bx > 0 && a.by > 0;
@@ -434,14 +444,19 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   const uint32_t bytes = (uint32_t)(MODE == kModeScalar
                                         ? L::kHalo + L::kOwn + (has_u ? L::kOwn : 0)
                                         : L::kHalo + L::kBHa * kBW + (has_u ? L::kHalo : 0)) * 4u;
+  grid_dep_trigger();
   __shared__ int done[2];
   if (tid == 0) {
+    prefetch_map(&cur_map);
+    prefetch_map(MODE == kModeScalar ? &prev_map : &d_map);
+    if (has_u) prefetch_map(&u_map);
     bar_init(&bar[0]);
     bar_init(&bar[1]);
     done[0] = done[1] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  grid_dep_wait();  // the state of the previous step is complete from here on
   const float gs = a.coef->gscale;  // one scale for every shot
   auto issue = [&](int k) {
     const int t = blockIdx.x + k * gridDim.x;
@@ -849,6 +864,14 @@ inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) 
 
 // Steps the tiled kernels cannot take (u^i == 0 at the first step, buffers
 // not on 16-byte boundaries) run on the first per-step kernels instead.
+// Launch overlap of the tiled kernels.  Their grids fill every SM (one
+// CTA per resident slot), so a dependent grid cannot start early on an SM
+// that is still busy; measured on a GB300 in graph replay, chaining the
+// scalar-constant kernels gains 1 % (1024^2 x 16 shots: 935 -> 926 ms per
+// iteration) and chaining the D-field kernels loses 7 % (512^2 x 8 shots:
+// 82.0 -> 88.6 ms, all of it in the adjoint).  Only the former are chained.
+static bool chain_tiled(int mode) { return mode == kModeScalar; }
+
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st) {
   const bool ok = (mode == kModeScalar || (mode == kModeDField && al16(a.field))) && a.cur != nullptr &&
                   a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) && al16(a.copy0) &&
@@ -865,11 +888,14 @@ cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st
   if (grid > ntiles) grid = ntiles;
   const double cells = (double)a.S * a.nx * a.ny;
   const int hp = a.prev ? 1 : 0;
+  const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfForward, st, [&] {
     if (mode == kModeScalar)
-      tma_fwd_kernel<kModeScalar><<<grid, kThreads, kFwdSmem, st>>>(a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+      launch_step_kernel(tma_fwd_kernel<kModeScalar>, grid, dim3(kThreads), kFwdSmem, st, chained,
+                         a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
     else
-      tma_fwd_kernel<kModeDField><<<grid, kThreads, kFwdSmem, st>>>(a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+      launch_step_kernel(tma_fwd_kernel<kModeDField>, grid, dim3(kThreads), kFwdSmem, st, chained,
+                         a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
   }, cells * alg_bytes_forward(mode));
 }
 
@@ -907,13 +933,14 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
   if (grid > kTiledRowsPerShot) grid = kTiledRowsPerShot;
   const double cells = (double)a.S * a.nx * a.ny;
   const int hu = a.u ? 1 : 0;
+  const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfAdjoint, st, [&] {
     if (!dfield)
-      tma_adj_kernel<kModeScalar><<<grid, kThreads, adj_smem<kModeScalar>(), st>>>(
-          a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+      launch_step_kernel(tma_adj_kernel<kModeScalar>, grid, dim3(kThreads), adj_smem<kModeScalar>(), st,
+                         chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
     else
-      tma_adj_kernel<kModeDField><<<grid, kThreads, adj_smem<kModeDField>(), st>>>(
-          a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+      launch_step_kernel(tma_adj_kernel<kModeDField>, grid, dim3(kThreads), adj_smem<kModeDField>(), st,
+                         chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
   }, cells * alg_bytes_adjoint(mode));
 }
 

@@ -218,6 +218,48 @@ int ernn_fem_forward(const ErnnFemProblem* p, const float* load, const float* si
                      const float* C_fields, float* frames_x, float* frames_y, void* workspace,
                      size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Misfit (the step between the forward and the adjoint): the loss of
+ * predicted against observed series and its gradient, which is the adjoint
+ * source.  Series are laid out series x frames x nx x ny floats, as the
+ * histories (S, nt_out, nx, ny) of ernn_forward (traces (S, nt_out, nrec):
+ * nx = 1, ny = nrec).  Counted: frames 0, frame_stride, ... and within them
+ * cells (i, j) with i and j multiples of space_stride; count = series x
+ * ceil(frames / frame_stride) x ceil(nx / space_stride) x ceil(ny / space_stride).
+ *   loss = wx * sum((px - ox)^2) / count + wy * sum((py - oy)^2) / count
+ * over the counted elements, with predictions and observations in the same
+ * layout.  This is compute_loss of Parameter_inversion/Inversion_adam.py:358-391
+ * (wx = wy = 1, [:, ::ts, ::ss, ::ss] of both, :339-342) and the data term of
+ * Damage_inversion/Inversion_adam.py:441-463 (wx = 5, wy = 1, [:, ::ts] of
+ * both, :420-422). */
+typedef struct ErnnSeries {
+  int64_t series;        /* series (shots) */
+  int64_t frames;        /* frames per series */
+  int32_t nx, ny;        /* frame shape, ny contiguous */
+  int32_t frame_stride;  /* >= 1 */
+  int32_t space_stride;  /* >= 1 */
+  double wx, wy;         /* weights of the two components, >= 0 */
+} ErnnSeries;
+
+/* Device workspace of ernn_misfit (block partials; fixed size). */
+size_t ernn_misfit_workspace_bytes(void);
+
+/* loss: 3 device doubles <- (loss, mean square of x, mean square of y).
+ * Differences in FP32, sums in FP64, fixed summation order (reproducible).
+ * Enqueued on `stream`; ERNN_ERR_INVALID for a bad layout or weights. */
+int ernn_misfit(const ErnnSeries* s, const float* px, const float* py, const float* ox,
+                const float* oy, double* loss, void* workspace, size_t workspace_bytes,
+                void* stream);
+
+/* Gradient of the three outputs of ernn_misfit against the upstream
+ * gradients grad_loss = 3 device doubles (g0, g1, g2) of (loss, mean square
+ * x, mean square y), or NULL for (1, 0, 0):
+ *   gx = 2 (wx g0 + g1) (px - ox) / count on counted elements, 0 elsewhere
+ *   gy = 2 (wy g0 + g2) (py - oy) / count
+ * over the whole series x frames x nx x ny layout. */
+int ernn_misfit_grad(const ErnnSeries* s, const float* px, const float* py, const float* ox,
+                     const float* oy, const double* grad_loss, float* gx, float* gy, void* stream);
+
 /* Number of kernels this library has launched since it was loaded. (host call)
  * Diagnostic; no counterpart in the reference. */
 uint64_t ernn_launch_count(void);
@@ -243,6 +285,14 @@ int ernn_wait_selftest(int32_t* status_host, void* stream);
  * the last ernn_forward / ernn_adjoint call of this process (ERNN_PATH_AUTO
  * before any call). (host call)  Diagnostic; no counterpart in the reference. */
 int32_t ernn_last_path(void);
+
+/* Launch overlap of consecutive time-step kernels on the per-step and tiled
+ * paths and of the FEM generator's levels (programmatic dependent launch: a
+ * step kernel is scheduled while the previous one drains, loads its
+ * step-independent inputs, then waits for the previous step's state).  On by
+ * default; results are bitwise the same either way.  Returns the previous
+ * setting. (host call)  No counterpart in the reference. */
+int ernn_set_launch_overlap(int on);
 
 /* Diagnostic kernel timing (no counterpart in the reference): while enabled,
  * every launch of the library is bracketed by CUDA events on its stream.

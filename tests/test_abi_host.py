@@ -155,3 +155,12 @@ def test_device_status_validates_before_any_device_call():
     assert lib.ernn_device_status(ctypes.byref(p), ctypes.c_void_p(16), 0, None, None) == 1
     assert lib.ernn_wait_selftest(None, None) == 1
     assert lib.ernn_last_path() in (0, 1, 2, 3)
+
+
+def test_launch_overlap_switch_is_a_host_setting():
+    was = E._lib.launch_overlap(False)
+    try:
+        assert E._lib.launch_overlap(True) is False
+        assert E._lib.launch_overlap(True) is True
+    finally:
+        E._lib.launch_overlap(was)
