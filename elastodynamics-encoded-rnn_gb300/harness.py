@@ -27,6 +27,7 @@ import numpy as np
 import torch
 
 from . import materials, sources
+from .misfit import series_misfit
 from .propagate import Geometry, check_device_status, propagate
 
 H, DT, RHO = 1e-4, 5e-9, 1560.0
@@ -117,7 +118,7 @@ def fields301():
     c = FIELDS301
     return Workload("fields301", c["nx"], c["nx"], c["nt"], np.asarray(c["C0"]), [(c["nx"] // 2, c["nx"] // 2)],
                     [], stride=c["stride"], f0=c["f0"], amplitude=c["amplitude"],
-                    gaussian_param=c["gaussian_param"], extra={"fields": True})
+                    gaussian_param=c["gaussian_param"], extra={"fields": True, "restart": True})
 
 
 WORKLOADS = {"plate128": plate128, "rot256": rot256, "shots1024": shots1024,
@@ -159,10 +160,10 @@ def observed(w: Workload, geom: Geometry, device, noise=0.005, seed=0):
 
 
 def trace_misfit(pred_x, pred_y, obs_x, obs_y):
-    """MSE(ux) + MSE(uy) (the loss of Parameter_inversion/Inversion_adam.py:389-391),
-    summed in FP64."""
-    return ((pred_x.double() - obs_x.double()) ** 2).mean() + \
-           ((pred_y.double() - obs_y.double()) ** 2).mean()
+    """MSE(ux) + MSE(uy) (the loss of Parameter_inversion/Inversion_adam.py:389-391)
+    of (S, nt_out, nrec) traces, summed in FP64: one fused pass of the library,
+    whose gradient (the adjoint source) is a second one."""
+    return series_misfit(pred_x, pred_y, obs_x, obs_y)
 
 
 class NormalisedConstants(torch.nn.Module):
@@ -351,8 +352,27 @@ class FieldsInversion(_GraphedIteration):
         self.obs = (tx.contiguous(), ty.contiguous())
         self.opt = torch.optim.Adam(self.sim.parameters(), lr=c["lr"] if lr is None else lr,
                                     capturable=graph)
+        self._start = [p.detach().clone() for p in self.sim.parameters()]
         if graph:
             self.capture()
+
+    def restart(self):
+        """Back to the initial guess with a fresh optimiser state, in place (a
+        captured graph keeps its tensors).  On this synthetic target the loop's
+        12th Adam step leaves the first cells with a stiffness that is not
+        positive-definite (the reference's loop does the same), and a few
+        iterations later the wavefield overflows."""
+        with torch.no_grad():
+            for p, p0 in zip(self.sim.parameters(), self._start):
+                p.copy_(p0)
+            for st in self.opt.state.values():
+                for k in ("exp_avg", "exp_avg_sq"):
+                    if k in st:
+                        st[k].zero_()
+                if torch.is_tensor(st.get("step")):
+                    st["step"].zero_()
+                elif "step" in st:
+                    st["step"] = 0
 
     @property
     def geom(self):

@@ -20,6 +20,7 @@ import torch
 import torch.nn as nn
 
 from . import sources as S
+from .misfit import series_misfit
 from .propagate import Geometry, propagate
 
 
@@ -299,13 +300,23 @@ def damage_loss(sim: SpatiallyVaryingAnisotropicSimulator, pred_ux, pred_uy, tar
     `secondary_time_stride`-th frame of the (1, nt_out, nx, ny) histories,
     5:1 weighted mean squared errors of u_x and u_y, plus lambda_tv times the
     total variation of the six constant fields of `sim`.  Targets are the
-    full-rate histories.  Returns (total, data, tv)."""
-    ts = secondary_time_stride
-    px, py = pred_ux[:, ::ts], pred_uy[:, ::ts]
-    tx, ty = target_ux[:, ::ts], target_uy[:, ::ts]
-    data = 5 * torch.mean((px - tx) ** 2) + torch.mean((py - ty) ** 2)
+    full-rate histories.  The data term is one fused pass of the library
+    (FP64 sums, float64 result) whose gradient is the adjoint source.
+    Returns (total, data, tv)."""
+    data = series_misfit(pred_ux, pred_uy, target_ux, target_uy, 5.0, 1.0, secondary_time_stride)
     tv = 0.0
     if lambda_tv > 0:
         C = sim.get_material_params()[:6]
         tv = lambda_tv * sum(total_variation_2d(c) for c in C)
     return data + tv, data, tv
+
+
+def parameter_loss(pred_ux, pred_uy, target_ux, target_uy, secondary_time_stride: int = 1,
+                   secondary_space_stride: int = 1):
+    """The parameter inversion's objective, as its inverter computes it
+    (Parameter_inversion/Inversion_adam.py:339-342, 358-391): [:, ::ts, ::ss,
+    ::ss] of the (1, nt_out, nx, ny) histories and of the full-rate targets,
+    mean squared error of u_x plus that of u_y; one fused pass of the
+    library (FP64 sums, float64 result)."""
+    return series_misfit(pred_ux, pred_uy, target_ux, target_uy, 1.0, 1.0, secondary_time_stride,
+                         secondary_space_stride)

@@ -266,6 +266,62 @@ def fem_case(F, kw):
                 **{f"arg_{k}": np.asarray(v) for k, v in kw.items()})
 
 
+def damage_invert_case(Dm, domain=(20, 20), nt=120, stride=5, ts=2, epochs=12, lr=0.02,
+                       lambda_tv=1e-21):
+    """The reference's own damage loop, SpatiallyVaryingParameterInverter.invert
+    (Damage_inversion/Inversion_adam.py:465-557), for a few Adam epochs in
+    float32 at its learning rate and TV weight (:827-830): targets from the
+    same simulator with every constant halved inside a disc of radius 3 cells
+    around cell (12, 8); loss history and mean constants after every epoch."""
+    torch.set_default_dtype(torch.float32)
+    base = dict(C11_init=130.74e9, C22_init=11.50e9, C12_init=10.49e9, C16_init=30.67e9,
+                C26_init=3.75e9, C66_init=14.77e9)
+    def make():
+        return Dm.SpatiallyVaryingAnisotropicSimulator(
+            domain, H, DT, nt, stride, source_component="y", total_time=nt * DT,
+            rho_known=RHO, use_log_params=True, **base, **SRC)
+    true = make()
+    ii, jj = np.meshgrid(np.arange(domain[0]), np.arange(domain[1]), indexing="ij")
+    disc = torch.tensor(((ii - 12) ** 2 + (jj - 8) ** 2 <= 9)[None], dtype=torch.float32)
+    with torch.no_grad():
+        for n in ["log_C11", "log_C22", "log_C12", "log_C16", "log_C26", "log_C66"]:
+            getattr(true, n).add_(disc * float(np.log(0.5)))
+        tx, ty = true()
+    sim = make()
+    inv = Dm.SpatiallyVaryingParameterInverter(sim, tx, ty, secondary_time_stride=ts, lambda_tv=lambda_tv)
+    inv.get_results = lambda *a, **k: None  # the summary printout is not part of the loop
+    inv.invert(max_epochs=epochs, lr=lr)
+    h = inv.history
+    return dict(nx=domain[0], ny=domain[1], nt=nt, stride=stride, ts=ts, h=H, dt=DT, rho=RHO,
+                epochs=epochs, lr=lr, lambda_tv=lambda_tv, disc=disc.numpy()[0],
+                target_ux=tx.double().numpy(), target_uy=ty.double().numpy(),
+                loss=np.array(h["loss"]), loss_data=np.array(h["loss_data"]),
+                means=np.array([h[k] for k in ("C11_mean", "C22_mean", "C12_mean", "C16_mean",
+                                               "C26_mean", "C66_mean")]).T)
+
+
+def misfit_case(P, Dm, shape=(1, 9, 13, 11), ts=2, ss=3, seed=5):
+    """The two inverters' compute_loss (Parameter_inversion/Inversion_adam.py:358-391,
+    Damage_inversion/Inversion_adam.py:441-463, without TV) on random float32
+    histories, with the gradients of each loss to the predicted histories."""
+    torch.set_default_dtype(torch.float32)
+    g = torch.Generator().manual_seed(seed)
+    px, py, tx, ty = (torch.randn(shape, generator=g) for _ in range(4))
+    out = dict(px=px.numpy(), py=py.numpy(), tx=tx.numpy(), ty=ty.numpy(), ts=ts, ss=ss)
+    for tag, inv in (("param", P.CFRPParameterInverterRicker(None, tx, ty, secondary_time_stride=ts,
+                                                            secondary_space_stride=ss)),
+                     ("damage", Dm.SpatiallyVaryingParameterInverter(None, tx, ty, secondary_time_stride=ts,
+                                                                     lambda_tv=0.0))):
+        ax, ay = px.clone().requires_grad_(True), py.clone().requires_grad_(True)
+        loss = inv.compute_loss(ax, ay)
+        loss = loss[0] if isinstance(loss, tuple) else loss
+        loss.backward()
+        out[f"{tag}_loss"] = float(loss)
+        out[f"{tag}_gx"] = ax.grad.numpy()
+        out[f"{tag}_gy"] = ay.grad.numpy()
+    return out
+
+
 def main():
     torch.manual_seed(0)
     P = load_param_module()
@@ -278,6 +334,8 @@ def main():
         np.savez_compressed(os.path.join(OUT, f"damage_inversion_tv_{tag}.npz"),
                             **damage_case(Dm, dtype, lambda_tv=1e-21))
     np.savez_compressed(os.path.join(OUT, "param_invert_f32.npz"), **invert_case(P))
+    np.savez_compressed(os.path.join(OUT, "misfit.npz"), **misfit_case(P, Dm))
+    np.savez_compressed(os.path.join(OUT, "damage_invert_f32.npz"), **damage_invert_case(Dm))
     F = load_fem_module()
     torch.set_default_dtype(torch.float32)
     for name, kw in FEM_CASES.items():

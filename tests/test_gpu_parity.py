@@ -444,3 +444,40 @@ def test_dropin_adam_trajectory_matches_reference_invert():
         params.append(sim.get_current_params_values()[:6])
     assert rel(np.array(losses), g["loss"]) <= 1e-4, (losses, g["loss"])
     assert rel(np.array(params), g["params"]) <= 1e-6, (params, g["params"])
+
+
+@pytest.mark.parametrize("fused_objective", [True, False])
+def test_damage_loop_trajectory_vs_reference_invert(fused_objective):
+    # the reference's own damage loop (SpatiallyVaryingParameterInverter.invert,
+    # float32, lr 0.02, TV 1e-21): twelve epochs through the drop-in six-field
+    # simulator give its losses and mean constants, with the library's fused
+    # objective (damage_loss) or the reference's torch expression
+    g = np.load(os.path.join(GOLDEN, "damage_invert_f32.npz"))
+    base = dict(C11_init=130.74e9, C22_init=11.50e9, C12_init=10.49e9, C16_init=30.67e9,
+                C26_init=3.75e9, C66_init=14.77e9)
+    nt = int(g["nt"])
+    sim = E.SpatiallyVaryingAnisotropicSimulator(
+        (int(g["nx"]), int(g["ny"])), float(g["h"]), float(g["dt"]), nt, int(g["stride"]),
+        source_component="y", total_time=nt * float(g["dt"]), rho_known=float(g["rho"]),
+        use_log_params=True, source_f0=4e6, source_t0=2.5e-7, source_amplitude=1e10,
+        gaussian_param=5e6, **base).to(DEV)
+    tx = torch.tensor(g["target_ux"], dtype=torch.float32, device=DEV)
+    ty = torch.tensor(g["target_uy"], dtype=torch.float32, device=DEV)
+    ts, lam = int(g["ts"]), float(g["lambda_tv"])
+    opt = torch.optim.Adam(sim.parameters(), lr=float(g["lr"]), betas=(0.9, 0.999), eps=1e-8)
+    losses, means = [], []
+    for _ in range(int(g["epochs"])):
+        opt.zero_grad()
+        ux, uy = sim(save_all_steps=False)
+        if fused_objective:
+            total, _, _ = E.damage_loss(sim, ux, uy, tx, ty, ts, lam)
+        else:
+            C = sim.get_material_params()[:6]
+            total = _reference_loss(ux, uy, tx, ty, ts, 1, wx=5.0) + \
+                lam * sum(E.total_variation_2d(c) for c in C)
+        total.backward()
+        opt.step()
+        losses.append(total.item())
+        means.append(sim.get_mean_params()[:6])
+    assert rel(np.array(losses), g["loss"]) <= 1e-4, (losses, g["loss"])
+    assert rel(np.array(means), g["means"]) <= 1e-6, (means, g["means"])
