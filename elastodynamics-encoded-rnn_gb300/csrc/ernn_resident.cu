@@ -3,14 +3,19 @@
 // every step of a launch.
 //
 // Partition: CTA c of the cluster owns grid rows [c R, c R + R) (x), all ny
-// columns.  Its shared memory holds two levels of the field (ping-pong) with
-// one halo row above and below:  buf[level][comp][R + 2][ny].
-// One step: every thread computes 4 x 4-cell items from the current level,
-// writes the new values into the other level (which holds the level before,
-// read by the same thread first), and pushes its CTA's first and last row
-// into the halo rows of the neighbouring CTAs through DSMEM stores.  One
-// cluster barrier (release/acquire) per step publishes the pushes.  States
-// that must reach global memory leave through TMA bulk copies.
+// columns.  Its shared memory holds a ring of three levels of the field with
+// one halo row above and below, L[level][comp][R + 2][ny], and the CTA's
+// force map.  Step t reads level t % 3 and writes level (t + 1) % 3 over the
+// level before it (each thread reads its own cells of that level first).
+// One step: a thread computes (column quad, row chunk) units; the interior
+// rows first (they read only this CTA's rows), then a bounded wait on the
+// level's mbarrier for the neighbours' boundary rows, then the first and
+// last row, which go into the neighbours' halo rows of the next level as
+// st.async stores completing transaction bytes on the neighbour's mbarrier
+// of that level.  No cluster barrier per step: waiting for the neighbours'
+// rows of level t means they have finished step t - 2, the last reader of
+// the level this CTA's pushes overwrite.  States that must reach global
+// memory leave through TMA bulk copies.
 //
 // A launch runs up to three roles, selected by blockIdx.z:
 //   FWD  steps i0..i1-1 of the forward recursion (the forward pass, or the

@@ -458,9 +458,19 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   __syncthreads();
   grid_dep_wait();  // the state of the previous step is complete from here on
   const float gs = a.coef->gscale;  // one scale for every shot
+  // This CTA's tiles: t_first + k t_step below t_end.  Strided over the grid
+  // (CTAs working at the same time touch neighbouring tiles, which share
+  // halo rows in L2), or, with per-shot constants and imaging, a contiguous
+  // chunk: the sums are flushed whenever the list enters another shot, and a
+  // strided list would do that at almost every tile.
+  const bool per_shot = a.coef_stride != 0;
+  const bool chunked = MODE == kModeScalar && per_shot && has_u;
+  const int t_first = chunked ? (int)((long long)blockIdx.x * ntiles / gridDim.x) : (int)blockIdx.x;
+  const int t_end = chunked ? (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x) : ntiles;
+  const int t_step = chunked ? 1 : (int)gridDim.x;
   auto issue = [&](int k) {
-    const int t = blockIdx.x + k * gridDim.x;
-    if (t >= ntiles) return;
+    const int t = t_first + k * t_step;
+    if (t >= t_end) return;
     const TileId id = tile_of<L::kTR>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * L::kStage;
     fence_async();
@@ -485,10 +495,9 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   // imaging sums (SCALAR): FP32 over a thread's 8 cells of a tile,
   // accumulated over tiles as FP32 pairs (TwoSum), FP64 across threads and
   // launches.  Partial row: blockIdx.x; with per-shot constants
-  // shot * kTiledRowsPerShot + blockIdx.x, flushed when the CTA's strided
+  // shot * kTiledRowsPerShot + blockIdx.x, flushed when the CTA's
   // tile list moves on to the next shot (shots never recur: t increases).
   float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  const bool per_shot = a.coef_stride != 0;
   int acc_shot = -1;
   auto flush = [&](int shot) {  // CTA-uniform: every warp calls it at the same point
     const int lane = tid & 31, warp = tid >> 5;
@@ -510,10 +519,10 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     __syncthreads();  // red is free again
   };
   TileWalk<L::kTR> walk;
-  walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+  walk.init(t_first, t_step, tiles_x, tiles_y);
   for (int k = 0;; ++k) {
-    const int t = blockIdx.x + k * gridDim.x;
-    if (t >= ntiles) break;
+    const int t = t_first + k * t_step;
+    if (t >= t_end) break;
     const TileId id = walk.id();
     walk.next();
     if (MODE == kModeScalar && per_shot && has_u && id.shot != acc_shot) {
