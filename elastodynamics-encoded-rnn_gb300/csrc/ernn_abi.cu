@@ -538,14 +538,23 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
       // recompute u^{i0+1} .. u^{i1} into the segment buffer; u^{nt} is never
       // imaged, so the last segment stops one step short
       const int iend = i1 < p->nt ? i1 : p->nt - 1;
-      for (int i = i0; i < iend; ++i) {
+      // on the tiled path, pairs of steps go through the two-step kernel
+      for (int i = i0; i < iend;) {
         a.i = i;
         a.out = seg(i - i0);
         a.cur = (i == i0) ? ck(j, 0) : seg(i - i0 - 1);
         a.prev = (i == i0) ? ck(j, 1) : (i == i0 + 1 ? ck(j, 0) : seg(i - i0 - 2));
         a.chained = chained ? 1 : 0;
         chained = true;
+        a.out2 = (tiled && i + 1 < iend) ? seg(i + 1 - i0) : nullptr;
+        if (a.out2 != nullptr && tma_fwd2_would_run(p->mode, a)) {
+          ERNN_CUDA(launch_tma_fwd2(p->mode, a, &coef->err, st));
+          i += 2;
+          continue;
+        }
+        a.out2 = nullptr;
         ERNN_CUDA(tiled ? launch_tma_fwd(p->mode, a, &coef->err, st) : launch_fwd_step(p->mode, a, st));
+        ++i;
       }
       for (int m = i1; m >= i0 + 1; --m)
         if ((rc = adj_step(m, seg(m - 1 - i0)))) return rc;

@@ -19,6 +19,7 @@ struct FwdStep {
   const float* cur;   // u^i (nullptr: zero state)
   const float* prev;  // u^{i-1} (nullptr: zero state)
   float* out;         // u^{i+1}
+  float* out2;        // two-step launches: u^{i+2}; otherwise nullptr
   float* copy0;       // optional second destination of u^{i+1} (checkpoint), or nullptr
   float* copy1;       // optional third destination, or nullptr
   // dense history: frame index (>= 0 when this step records), bases of (S, nt_out, N)

@@ -396,6 +396,197 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   }
 }
 
+// ------------------------------------------------------- two-step forward
+// u^{i+1} and u^{i+2} of a tile in one pass (temporal blocking).  The box of
+// u^i with a two-cell halo and the box of u^{i-1} with a one-cell halo give
+// u^{i+1} on the tile and on a one-cell ring around it (cells outside the
+// grid forced to zero: the scheme's ghost ring), kept in shared memory; from
+// it and u^i's own cells, u^{i+2} on the tile.  HBM traffic per two steps:
+// read u^i and u^{i-1}, write u^{i+1} and u^{i+2} (16 B per cell-step
+// instead of 24).  Steps without history frames, checkpoint copies or
+// receiver gathers only: the recompute segments of the adjoint.
+struct Fwd2Layout {
+  static constexpr int kTR = 16;                    // tile rows
+  static constexpr int kBH2 = kTR + 4;              // u^i box rows: tile rows -2 .. kTR+1
+  static constexpr int kBH1 = kTR + 2;              // u^{i-1} box and u^{i+1} rows: -1 .. kTR
+  static constexpr int kCur = 2 * kBH2 * kBW;
+  static constexpr int kPrev = 2 * kBH1 * kBW;
+  static constexpr int kStage = (kCur + kPrev + 31) / 32 * 32;  // 128-byte multiple
+  static constexpr int kMid = 2 * kBH1 * kBW;       // u^{i+1}; one buffer per tile parity
+  static constexpr int kQuads = kBW / 4;            // quads per box row
+  static constexpr int kItems1 = kBH1 * kQuads;     // first-step quads (18 x 18)
+  static constexpr int kCtasPerSm = 3;
+};
+
+// window [b-1 .. b+4] of box row r at box column b (b % 4 == 0); zero
+// beyond the box's kBW columns (only the box's first and last columns of
+// u^{i+1} depend on those, and the second step never reads them)
+__device__ __forceinline__ void win_box(const float* __restrict__ box, int r, int b, float w[6]) {
+  const float* p = box + r * kBW + b;
+  const float4 m = *reinterpret_cast<const float4*>(p);
+  w[0] = b > 0 ? p[-1] : 0.f;
+  w[1] = m.x;
+  w[2] = m.y;
+  w[3] = m.z;
+  w[4] = m.w;
+  w[5] = b + 4 < kBW ? p[4] : 0.f;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
+    tma_fwd2_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
+                    const __grid_constant__ CUtensorMap prev_map, int tiles_x, int tiles_y, int has_prev,
+                    int* err) {
+  extern __shared__ float sm_raw[];
+  float* sm = aligned128(sm_raw);
+  using F = Fwd2Layout;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * F::kStage + 2 * F::kMid);
+  const int tid = threadIdx.x;
+  const int nx = a.nx, ny = a.ny;
+  const size_t N = (size_t)nx * ny;
+  const int ntiles = a.S * tiles_x * tiles_y;
+  const uint32_t bytes = (uint32_t)(F::kCur + (has_prev ? F::kPrev : 0)) * 4u;
+  grid_dep_trigger();
+  __shared__ int done[2];
+  if (tid == 0) {
+    prefetch_map(&cur_map);
+    prefetch_map(&prev_map);
+    bar_init(&bar[0]);
+    bar_init(&bar[1]);
+    done[0] = done[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  grid_dep_wait();  // the state of the previous step is complete from here on
+  const bool has_src = a.bx > 0 && a.by > 0;
+  auto issue = [&](int k) {  // loads of this CTA's k-th tile into stage k & 1
+    const int t = blockIdx.x + k * gridDim.x;
+    if (t >= ntiles) return;
+    const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
+    float* st = sm + (k & 1) * F::kStage;
+    fence_async();
+    bar_expect(&bar[k & 1], bytes);
+    tma_load3(st, &cur_map, id.y0 - 4, id.x0 - 2, 2 * id.shot, &bar[k & 1]);
+    if (has_prev) tma_load3(st + F::kCur, &prev_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+  };
+  if (tid == 0) {
+    issue(0);
+    issue(1);
+  }
+  const int qc = tid & 15, rg = tid >> 4;
+  const int j = 4 * qc;
+  TileWalk<F::kTR> walk;
+  walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+  for (int k = 0;; ++k) {
+    const int t = blockIdx.x + k * gridDim.x;
+    if (t >= ntiles) break;
+    const TileId id = walk.id();
+    walk.next();
+    const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
+    const Coefs ks = coefs(K);
+    const float* sig = a.src_signal + (size_t)id.shot * a.nt;
+    const float amp1 = sig[a.i] * K->kappa, amp2 = sig[a.i + 1] * K->kappa;
+    const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
+    const float* smap = has_src ? a.src_map + (size_t)id.shot * a.bx * a.by : nullptr;
+    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
+    const float* cb = sm + (k & 1) * F::kStage;           // u^i: rows -2 .. kTR+1
+    const float* pb = cb + F::kCur;                        // u^{i-1}: rows -1 .. kTR
+    float* mid = sm + 2 * F::kStage + (k & 1) * F::kMid;  // u^{i+1}: rows -1 .. kTR
+    float* out1 = a.out + (size_t)id.shot * 2 * N;
+    float* out2 = a.out2 + (size_t)id.shot * 2 * N;
+
+    // step i: u^{i+1} on rows -1 .. kTR of every box column (box column b is
+    // grid column y0 - 4 + b)
+    for (int it = tid; it < F::kItems1; it += kThreads) {
+      const int m = it / F::kQuads, b = 4 * (it - m * F::kQuads);
+      float wx[3][6], wy[3][6];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        win_box(cb, m + d, b, wx[d]);
+        win_box(cb + F::kBH2 * kBW, m + d, b, wy[d]);
+      }
+      Sums4 st;
+      sums4(wx, wy, st);
+      float4 pvx = make_float4(0.f, 0.f, 0.f, 0.f), pvy = pvx;
+      if (has_prev) {
+        pvx = *reinterpret_cast<const float4*>(pb + m * kBW + b);
+        pvy = *reinterpret_cast<const float4*>(pb + F::kBH1 * kBW + m * kBW + b);
+      }
+      const int gi = id.x0 + m - 1, gj = id.y0 - 4 + b;  // ny % 4 == 0: a quad is in or out
+      const bool inside = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+      float vx[4], vy[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float lx, ly;
+        apply(ks, st, q, lx, ly);
+        vx[q] = inside ? (2.f * st.cx[q] - g4(pvx, q)) + lx : 0.f;
+        vy[q] = inside ? (2.f * st.cy[q] - g4(pvy, q)) + ly : 0.f;
+      }
+      const int sa = gi - ox;
+      if (inside && has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int sb = gj + q - oy;
+          if ((unsigned)sb < (unsigned)a.by) {
+            const float f = amp1 * smap[(size_t)sa * a.by + sb];
+            if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
+          }
+        }
+      }
+      const float4 nvx = make_float4(vx[0], vx[1], vx[2], vx[3]);
+      const float4 nvy = make_float4(vy[0], vy[1], vy[2], vy[3]);
+      *reinterpret_cast<float4*>(mid + m * kBW + b) = nvx;
+      *reinterpret_cast<float4*>(mid + F::kBH1 * kBW + m * kBW + b) = nvy;
+      if (inside && m >= 1 && m <= F::kTR && b >= 4 && b < 4 + kTY) {
+        const size_t o = (size_t)gi * ny + gj;
+        *reinterpret_cast<float4*>(out1 + o) = nvx;
+        *reinterpret_cast<float4*>(out1 + N + o) = nvy;
+      }
+    }
+    __syncthreads();  // u^{i+1} complete (and the other buffer's readers are done)
+
+    // step i + 1: u^{i+2} on the tile from u^{i+1} and u^i's own cells
+    {
+      float wx[3][6], wy[3][6];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        win(mid, rg + d, j, wx[d]);
+        win(mid + F::kBH1 * kBW, rg + d, j, wy[d]);
+      }
+      Sums4 st;
+      sums4(wx, wy, st);
+      const float4 pvx = *reinterpret_cast<const float4*>(cb + (rg + 2) * kBW + j + 4);
+      const float4 pvy = *reinterpret_cast<const float4*>(cb + F::kBH2 * kBW + (rg + 2) * kBW + j + 4);
+      const int gi = id.x0 + rg, gj = id.y0 + j;
+      float vx[4], vy[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float lx, ly;
+        apply(ks, st, q, lx, ly);
+        vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
+        vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
+      }
+      const int sa = gi - ox;
+      if (has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int sb = gj + q - oy;
+          if ((unsigned)sb < (unsigned)a.by) {
+            const float f = amp2 * smap[(size_t)sa * a.by + sb];
+            if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
+          }
+        }
+      }
+      if (gi < nx && gj < ny) {
+        const size_t o = (size_t)gi * ny + gj;
+        *reinterpret_cast<float4*>(out2 + o) = make_float4(vx[0], vx[1], vx[2], vx[3]);
+        *reinterpret_cast<float4*>(out2 + N + o) = make_float4(vy[0], vy[1], vy[2], vy[3]);
+      }
+    }
+    release(done, k, [&] { issue(k + 2); });
+  }
+}
+
 // ----------------------------------------------------------------- adjoint
 // Stage (SCALAR): halo box of lam^{m+1}, own boxes of lam^{m+2} and u^m
 // (u^m enters only through its own cells).  The six
@@ -800,6 +991,7 @@ bool make_map2(CUtensorMap* m, const float* base, int nx, int ny, int bw, int bh
 }
 
 constexpr size_t kFwdSmem = 2 * (size_t)FwdLayout::kStage * 4 + 16 + 128;
+constexpr size_t kFwd2Smem = (2 * (size_t)Fwd2Layout::kStage + 2 * (size_t)Fwd2Layout::kMid) * 4 + 16 + 128;
 template <int MODE>
 constexpr size_t adj_smem() {
   return 2 * (size_t)AdjLayout<MODE>::kStage * 4 + 16 + 128;
@@ -810,9 +1002,10 @@ cudaError_t set_smem() {
   static cudaError_t result = cudaSuccess;
   std::call_once(once, [] {
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e[4] = {
+    cudaError_t e[5] = {
         cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar>, at, (int)kFwdSmem),
         cudaFuncSetAttribute(tma_fwd_kernel<kModeDField>, at, (int)kFwdSmem),
+        cudaFuncSetAttribute(tma_fwd2_kernel<kModeScalar>, at, (int)kFwd2Smem),
         cudaFuncSetAttribute(tma_adj_kernel<kModeScalar>, at, (int)adj_smem<kModeScalar>()),
         cudaFuncSetAttribute(tma_adj_kernel<kModeDField>, at, (int)adj_smem<kModeDField>())};
     for (cudaError_t x : e)
@@ -880,6 +1073,32 @@ inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) 
 // iteration) and chaining the D-field kernels loses 7 % (512^2 x 8 shots:
 // 82.0 -> 88.6 ms, all of it in the adjoint).  Only the former are chained.
 static bool chain_tiled(int mode) { return mode == kModeScalar; }
+
+bool tma_fwd2_would_run(int mode, const FwdStep& a) {
+  return mode == kModeScalar && a.cur != nullptr && a.out2 != nullptr && a.ny % 4 == 0 &&
+         a.frame < 0 && a.gframe < 0 && a.copy0 == nullptr && a.copy1 == nullptr && al16(a.cur) &&
+         al16(a.prev) && al16(a.out) && al16(a.out2) && encode_fn() != nullptr;
+}
+
+cudaError_t launch_tma_fwd2(int mode, const FwdStep& a, int* err, cudaStream_t st) {
+  using F = Fwd2Layout;
+  CUtensorMap cur_map, prev_map;
+  if (!tma_fwd2_would_run(mode, a) || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, F::kBH2) ||
+      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, a.S, kBW, F::kBH1))
+    return cudaErrorNotSupported;
+  cudaError_t e = set_smem();
+  if (e != cudaSuccess) return e;
+  const int tiles_x = (a.nx + F::kTR - 1) / F::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
+  const int ntiles = a.S * tiles_x * tiles_y;
+  int grid = num_sms() * F::kCtasPerSm;
+  if (grid > ntiles) grid = ntiles;
+  const int hp = a.prev ? 1 : 0;
+  const bool chained = a.chained != 0 && chain_tiled(mode);
+  return tracked_launch(kProfForward, st, [&] {
+    launch_step_kernel(tma_fwd2_kernel<kModeScalar>, dim3(grid), dim3(kThreads), kFwd2Smem, st, chained, a,
+                       cur_map, prev_map, tiles_x, tiles_y, hp, err);
+  }, 2.0 * (double)a.S * a.nx * a.ny * 16.0);
+}
 
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st) {
   const bool ok = (mode == kModeScalar || (mode == kModeDField && al16(a.field))) && a.cur != nullptr &&

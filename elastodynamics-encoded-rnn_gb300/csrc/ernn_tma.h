@@ -20,6 +20,11 @@ int tma_adj_tile_rows(int mode);
 // Same contract as launch_fwd_step / launch_adj_step (SCALAR or DFIELD
 // mode); `err` is the call's device error word.
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st);
+// Two steps in one launch (u^{i+1} into a.out, u^{i+2} into a.out2) when
+// tma_fwd2_would_run: scalar constants, u^i given, no frames, copies or
+// receiver gathers in either step; cudaErrorNotSupported otherwise.
+bool tma_fwd2_would_run(int mode, const FwdStep& a);
+cudaError_t launch_tma_fwd2(int mode, const FwdStep& a, int* err, cudaStream_t st);
 cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st);
 // Whether launch_tma_adj takes the tiled kernel for steps shaped like `a`
 // (buffers on 16-byte boundaries, tensor maps encodable) rather than falling
