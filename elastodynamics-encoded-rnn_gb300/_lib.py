@@ -54,6 +54,17 @@ class ErnnSeries(ctypes.Structure):
                 ("wx", ctypes.c_double), ("wy", ctypes.c_double)]
 
 
+class ErnnAdamTensor(ctypes.Structure):
+    """Mirror of struct ErnnAdamTensor (include/ernn.h)."""
+    _fields_ = [("param", ctypes.c_void_p), ("grad", ctypes.c_void_p), ("exp_avg", ctypes.c_void_p),
+                ("exp_avg_sq", ctypes.c_void_p), ("n", ctypes.c_int64)]
+
+
+class ErnnAdamHyper(ctypes.Structure):
+    """Mirror of struct ErnnAdamHyper (include/ernn.h)."""
+    _fields_ = [(n, ctypes.c_double) for n in ("lr", "beta1", "beta2", "eps", "weight_decay")]
+
+
 # name -> (restype, argtypes); the complete exported surface of include/ernn.h
 _P = ctypes.c_void_p
 SIGNATURES = {
@@ -78,6 +89,7 @@ SIGNATURES = {
     "ernn_misfit_workspace_bytes": (ctypes.c_size_t, []),
     "ernn_misfit": (ctypes.c_int, [ctypes.POINTER(ErnnSeries), _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "ernn_misfit_grad": (ctypes.c_int, [ctypes.POINTER(ErnnSeries), _P, _P, _P, _P, _P, _P, _P, _P]),
+    "ernn_adam_step": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(ErnnAdamHyper), _P, _P]),
     "ernn_launch_count": (ctypes.c_uint64, []),
     "ernn_last_path": (ctypes.c_int32, []),
     "ernn_set_launch_overlap": (ctypes.c_int, [ctypes.c_int]),

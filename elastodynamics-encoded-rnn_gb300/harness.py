@@ -28,6 +28,7 @@ import torch
 
 from . import materials, sources
 from .misfit import series_misfit
+from .optim import FusedAdam
 from .propagate import Geometry, check_device_status, propagate
 
 H, DT, RHO = 1e-4, 5e-9, 1560.0
@@ -214,8 +215,9 @@ class _GraphedIteration:
 
     def capture(self):
         dev = self.device
-        for group in self.opt.param_groups:  # optimiser state kept on the device
-            group["capturable"] = True
+        if isinstance(self.opt, torch.optim.Adam):  # optimiser state kept on the device
+            for group in self.opt.param_groups:
+                group["capturable"] = True
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
@@ -250,7 +252,7 @@ class Inversion(_GraphedIteration):
         self.obs = observed(w, self.geom, device, seed=seed)
         self.rho = torch.tensor(RHO, device=device)
         self.params = NormalisedConstants(initial_guess(w, seed), scales(w.C_true)).to(device)
-        self.opt = torch.optim.Adam(self.params.parameters(), lr=lr, capturable=graph)
+        self.opt = FusedAdam(self.params.parameters(), lr=lr)
         if graph:
             self.capture()
 
@@ -293,7 +295,7 @@ class DamageInversion(_GraphedIteration):
         self.rho = torch.tensor(RHO, device=device)
         self.C0 = torch.tensor(w.C_true, dtype=torch.float32, device=device)
         self.D = torch.nn.Parameter(torch.zeros((w.nx, w.ny), device=device))
-        self.opt = torch.optim.Adam([self.D], lr=lr, capturable=graph)
+        self.opt = FusedAdam([self.D], lr=lr)
         if graph:
             self.capture()
 
@@ -504,7 +506,7 @@ class MultiInversion:
                 self.stream_of.append(1 + small % nsmall)
                 small += 1
         params = [inv.params.theta for inv in self.invs]
-        self.opt = torch.optim.Adam(params, lr=lr, capturable=graph)
+        self.opt = FusedAdam(params, lr=lr)  # one launch for every instance's constants
         self.streams = [torch.cuda.Stream(device) for _ in range(nstreams)]
         self.obs = [o for g in self.groups for o in g.obs]
         self.cell_steps = sum(w.cell_steps for w in ws)

@@ -260,6 +260,33 @@ int ernn_misfit(const ErnnSeries* s, const float* px, const float* py, const flo
 int ernn_misfit_grad(const ErnnSeries* s, const float* px, const float* py, const float* ox,
                      const float* oy, const double* grad_loss, float* gx, float* gy, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Fused Adam step over every parameter tensor of an optimiser in one launch
+ * (torch.optim.Adam of the inversion loops, Parameter_inversion/Inversion_adam.py:421-447,
+ * Damage_inversion/Inversion_adam.py:477-514; no amsgrad).  Per element, t =
+ * step count after this step:
+ *   g = grad + weight_decay p;  m += (1 - beta1)(g - m);  v = beta2 v + (1 - beta2) g^2
+ *   p += -lr / (1 - beta1^t) * m / (sqrt(v) / sqrt(1 - beta2^t) + eps)
+ * FP32 state, bias corrections in FP64.  The step count is device state, so
+ * a CUDA graph that captured the call advances it on every replay. */
+typedef struct ErnnAdamTensor {
+  float* param;          /* n floats, updated in place */
+  const float* grad;     /* n floats */
+  float* exp_avg;        /* n floats, zero before the first step */
+  float* exp_avg_sq;     /* n floats, zero before the first step */
+  int64_t n;
+} ErnnAdamTensor;
+
+typedef struct ErnnAdamHyper {
+  double lr, beta1, beta2, eps, weight_decay;
+} ErnnAdamHyper;
+
+/* tensors: DEVICE array of ntensors descriptors; max_numel: the largest n;
+ * h: host; state: 2 device int32 (step count, then a ticket that must be 0
+ * before the first call; both zero-initialised by the caller). */
+int ernn_adam_step(const ErnnAdamTensor* tensors, int32_t ntensors, int64_t max_numel,
+                   const ErnnAdamHyper* h, int32_t* state, void* stream);
+
 /* Number of kernels this library has launched since it was loaded. (host call)
  * Diagnostic; no counterpart in the reference. */
 uint64_t ernn_launch_count(void);

@@ -164,3 +164,11 @@ def test_launch_overlap_switch_is_a_host_setting():
         assert E._lib.launch_overlap(True) is True
     finally:
         E._lib.launch_overlap(was)
+
+
+def test_fused_adam_refuses_cpu_parameters():
+    from ernn_gb300.optim import FusedAdam
+    p = torch.zeros(4, requires_grad=True)
+    p.grad = torch.ones(4)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        FusedAdam([p]).step()
