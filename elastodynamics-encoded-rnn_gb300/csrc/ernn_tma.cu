@@ -432,6 +432,25 @@ __device__ __forceinline__ void win_box(const float* __restrict__ box, int r, in
   w[5] = b + 4 < kBW ? p[4] : 0.f;
 }
 
+// The same window for a warp whose lanes hold consecutive quads of a row:
+// the edge cells come from the neighbouring lanes (left_ok / right_ok: the
+// lane before / after holds the quad before / after in the same row), so a
+// window costs one 16-byte load per lane and the edge loads run only in the
+// lanes at the ends of a row or of the warp.  Every lane of the warp calls it.
+__device__ __forceinline__ void win_lanes(const float* __restrict__ box, int r, int b, bool left_ok,
+                                          bool right_ok, float w[6]) {
+  const float* p = box + r * kBW + b;
+  const float4 m = *reinterpret_cast<const float4*>(p);
+  const float from_left = __shfl_up_sync(0xffffffffu, m.w, 1);
+  const float from_right = __shfl_down_sync(0xffffffffu, m.x, 1);
+  w[0] = left_ok ? from_left : (b > 0 ? p[-1] : 0.f);
+  w[1] = m.x;
+  w[2] = m.y;
+  w[3] = m.z;
+  w[4] = m.w;
+  w[5] = right_ok ? from_right : (b + 4 < kBW ? p[4] : 0.f);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     tma_fwd2_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
@@ -496,14 +515,21 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     float* out2 = a.out2 + (size_t)id.shot * 2 * N;
 
     // step i: u^{i+1} on rows -1 .. kTR of every box column (box column b is
-    // grid column y0 - 4 + b)
-    for (int it = tid; it < F::kItems1; it += kThreads) {
-      const int m = it / F::kQuads, b = 4 * (it - m * F::kQuads);
+    // grid column y0 - 4 + b).  Items run warp by warp (every lane takes part
+    // in the window shuffles); lanes past the last item compute a copy of it
+    // and store nothing.
+    const int lane = tid & 31;
+    for (int base = tid - lane; base < F::kItems1; base += kThreads) {
+      const int it = base + lane;
+      const bool valid = it < F::kItems1;
+      const int itc = valid ? it : F::kItems1 - 1;
+      const int m = itc / F::kQuads, qb = itc - m * F::kQuads, b = 4 * qb;
+      const bool left_ok = lane > 0 && qb > 0, right_ok = lane < 31 && qb < F::kQuads - 1 && valid;
       float wx[3][6], wy[3][6];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        win_box(cb, m + d, b, wx[d]);
-        win_box(cb + F::kBH2 * kBW, m + d, b, wy[d]);
+        win_lanes(cb, m + d, b, left_ok, right_ok, wx[d]);
+        win_lanes(cb + F::kBH2 * kBW, m + d, b, left_ok, right_ok, wy[d]);
       }
       Sums4 st;
       sums4(wx, wy, st);
@@ -535,6 +561,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
       }
       const float4 nvx = make_float4(vx[0], vx[1], vx[2], vx[3]);
       const float4 nvy = make_float4(vy[0], vy[1], vy[2], vy[3]);
+      if (!valid) continue;
       *reinterpret_cast<float4*>(mid + m * kBW + b) = nvx;
       *reinterpret_cast<float4*>(mid + F::kBH1 * kBW + m * kBW + b) = nvy;
       if (inside && m >= 1 && m <= F::kTR && b >= 4 && b < 4 + kTY) {
@@ -546,12 +573,13 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     __syncthreads();  // u^{i+1} complete (and the other buffer's readers are done)
 
     // step i + 1: u^{i+2} on the tile from u^{i+1} and u^i's own cells
+    // (lanes 0-15 and 16-31 of a warp hold the 16 quads of two rows)
     {
       float wx[3][6], wy[3][6];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        win(mid, rg + d, j, wx[d]);
-        win(mid + F::kBH1 * kBW, rg + d, j, wy[d]);
+        win_lanes(mid, rg + d, j + 4, qc > 0, qc < 15, wx[d]);
+        win_lanes(mid + F::kBH1 * kBW, rg + d, j + 4, qc > 0, qc < 15, wy[d]);
       }
       Sums4 st;
       sums4(wx, wy, st);
