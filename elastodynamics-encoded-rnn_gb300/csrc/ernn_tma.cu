@@ -1,16 +1,18 @@
 // Per-step kernels for large grids (sm_103a), TMA-pipelined.
 //
 // One launch per time step, as the first per-step kernels, but each CTA is
-// persistent over a strided list of 64 (y) x 32 (x) tiles of the step and
+// persistent over a list of 64 (y) x TR (x) tiles of the step (TR = 16 for
+// the forward and the scalar adjoint, 32 for the D-field adjoint) and
 // streams them through a two-stage shared-memory pipeline: while a tile is
 // computed, the tensor-memory-accelerator loads of the next tile are in
 // flight (cp.async.bulk.tensor, completion on an mbarrier per stage).
 //
-// The halo box of a tile is 72 x 34 cells: rows x0-1 .. x0+32 and columns
-// y0-4 .. y0+67 (the innermost coordinate must be a multiple of four floats,
-// so the box reaches four columns to the left where one is needed).  Cells
-// outside the grid are filled with zeros by the copy engine: that is the
-// zero ghost ring of the scheme, with no predicated loads.
+// The halo box of a tile is 72 x (TR + 2) cells: rows x0-1 .. x0+TR and
+// columns y0-4 .. y0+67 (the innermost coordinate must be a multiple of four
+// floats, so the box reaches four columns to the left where one is needed).
+// Cells outside the grid are filled with zeros by the copy engine: that is
+// the zero ghost ring of the scheme, with no predicated loads.  The two-step
+// forward (recompute segments) takes a box two cells deep instead.
 //
 // Scalar constants (ERNN_MODE_SCALAR) and the degradation map (ERNN_MODE_DFIELD),
 // ny % 4 == 0.
@@ -26,11 +28,9 @@ namespace ernn {
 
 namespace {
 
-constexpr int kTY = 64, kTX = 32;          // tile: 64 columns (y) by 32 rows (x)
-constexpr int kBW = kTY + 8, kBH = kTX + 2;  // halo box
-constexpr int kThreads = 256;              // 16 column quads x 16 row pairs
-constexpr int kHaloFloats = 2 * kBH * kBW;  // both components
-constexpr int kOwnFloats = 2 * kTX * kTY;
+constexpr int kTY = 64;                    // tile columns (y); rows per kernel layout
+constexpr int kBW = kTY + 8;               // halo box width: tile + 4 columns each side
+constexpr int kThreads = 256;              // 16 column quads x 16 rows
 
 __device__ __forceinline__ uint32_t s32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -296,6 +296,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   }
   const int qc = tid & 15, rg = tid >> 4;
   const int j = 4 * qc;
+  const Coefs ks0 = coefs(a.coef);  // every shot's, unless per-shot constants
   TileWalk<F::kTR> walk;
   walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
   for (int k = 0;; ++k) {
@@ -306,7 +307,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
     // per-tile scalars, loaded before the wait (coefficients per shot with
     // per-shot constants)
     const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
-    const Coefs ks = coefs(K);
+    const Coefs ks = a.coef_stride != 0 ? coefs(K) : ks0;
     const float amp = a.src_signal[(size_t)id.shot * a.nt + a.i] * K->kappa;
     const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
     const int gj = id.y0 + j;
@@ -418,21 +419,10 @@ struct Fwd2Layout {
   static constexpr int kCtasPerSm = 3;
 };
 
-// window [b-1 .. b+4] of box row r at box column b (b % 4 == 0); zero
-// beyond the box's kBW columns (only the box's first and last columns of
-// u^{i+1} depend on those, and the second step never reads them)
-__device__ __forceinline__ void win_box(const float* __restrict__ box, int r, int b, float w[6]) {
-  const float* p = box + r * kBW + b;
-  const float4 m = *reinterpret_cast<const float4*>(p);
-  w[0] = b > 0 ? p[-1] : 0.f;
-  w[1] = m.x;
-  w[2] = m.y;
-  w[3] = m.z;
-  w[4] = m.w;
-  w[5] = b + 4 < kBW ? p[4] : 0.f;
-}
-
-// The same window for a warp whose lanes hold consecutive quads of a row:
+// Window [b-1 .. b+4] of box row r at box column b (b % 4 == 0), zero beyond
+// the box's kBW columns (only the box's first and last columns of u^{i+1}
+// depend on those, and the second step never reads them), for a warp whose
+// lanes hold consecutive quads of a row:
 // the edge cells come from the neighbouring lanes (left_ok / right_ok: the
 // lane before / after holds the quad before / after in the same row), so a
 // window costs one 16-byte load per lane and the edge loads run only in the
@@ -494,6 +484,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   }
   const int qc = tid & 15, rg = tid >> 4;
   const int j = 4 * qc;
+  const Coefs ks0 = coefs(a.coef);  // every shot's, unless per-shot constants
   TileWalk<F::kTR> walk;
   walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
   for (int k = 0;; ++k) {
@@ -502,7 +493,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     const TileId id = walk.id();
     walk.next();
     const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
-    const Coefs ks = coefs(K);
+    const Coefs ks = a.coef_stride != 0 ? coefs(K) : ks0;
     const float* sig = a.src_signal + (size_t)id.shot * a.nt;
     const float amp1 = sig[a.i] * K->kappa, amp2 = sig[a.i + 1] * K->kappa;
     const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
@@ -716,9 +707,23 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   // launches.  Partial row: blockIdx.x; with per-shot constants
   // shot * kTiledRowsPerShot + blockIdx.x, flushed when the CTA's
   // tile list moves on to the next shot (shots never recur: t increases).
+  // (the FP32 sums of a thread's cells are folded into the pair every two
+  // tiles and before a flush)
   float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  auto fold = [&] {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {  // TwoSum(hi, acc)
+      const float s = hi[q] + acc[q];
+      const float bp = s - hi[q];
+      lo[q] += (hi[q] - (s - bp)) + (acc[q] - bp);
+      hi[q] = s;
+      acc[q] = 0.f;
+    }
+  };
   int acc_shot = -1;
   auto flush = [&](int shot) {  // CTA-uniform: every warp calls it at the same point
+    fold();
     const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
@@ -737,6 +742,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     }
     __syncthreads();  // red is free again
   };
+  const Coefs ks0 = coefs(a.coef);  // every shot's, unless per-shot constants
   TileWalk<L::kTR> walk;
   walk.init(t_first, t_step, tiles_x, tiles_y);
   for (int k = 0;; ++k) {
@@ -748,7 +754,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       if (acc_shot >= 0) flush(acc_shot);
       acc_shot = id.shot;
     }
-    const Coefs ks = coefs(a.coef + (size_t)id.shot * a.coef_stride);
+    const Coefs ks = per_shot ? coefs(a.coef + (size_t)id.shot * a.coef_stride) : ks0;
     const int gj = id.y0 + j;
     const int r0 = L::kRT * rg;
     // receivers in this tile (uniform over the CTA): the injection and its
@@ -811,7 +817,6 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       win(ub, r0 + 1, j, vx_[1]);
       win(ub + L::kBHa * kBW, r0 + 1, j, vy_[1]);
     }
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int q2 = 0; q2 < L::kRT; ++q2) {
       const int r = r0 + q2;
@@ -907,15 +912,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       shift(wx);
       shift(wy);
     }
-    if (MODE == kModeScalar) {
-#pragma unroll
-      for (int q = 0; q < 6; ++q) {  // TwoSum(hi, acc)
-        const float s = hi[q] + acc[q];
-        const float bp = s - hi[q];
-        lo[q] += (hi[q] - (s - bp)) + (acc[q] - bp);
-        hi[q] = s;
-      }
-    }
+    if (MODE == kModeScalar && (k & 1)) fold();
     if (MODE == kModeDField && tile_inject) {
       // adjoint source at receiver cells, added to the stored lam^m (several
       // receivers may share a cell); the block's own stores are visible
