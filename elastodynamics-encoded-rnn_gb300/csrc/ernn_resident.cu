@@ -114,6 +114,15 @@ __device__ __forceinline__ void bulk_s2g(void* gdst, const void* ssrc, uint32_t 
                "r"(smem_u32(ssrc)), "r"(bytes)
                : "memory");
 }
+// 1D bulk copy global -> shared (this CTA), completing on mbarrier `bar`.
+__device__ __forceinline__ void bulk_g2s(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(sdst)),
+               "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 // wait until the committed bulk stores have finished reading shared memory
 __device__ __forceinline__ void bulk_wait_read_all() {
@@ -525,7 +534,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   float* F = smem + 3 * level_floats;   // FWD role: source load of the own rows [R][ny]
   int* rec_list = reinterpret_cast<int*>(F + R * ny);  // [kResMaxRec][2]
   int* rec_count = rec_list + 2 * kResMaxRec;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(rec_count + 4);  // [3], 8-byte aligned
+  uint64_t* bar = reinterpret_cast<uint64_t*>(rec_count + 4);  // [4], 8-byte aligned
+  // bar[0..2]: halo rows of the ring levels; bar[3]: the initial state
 
   const Coef* K = c.coef + (size_t)shot * c.coef_stride;
   const KSr ks{K->k11, K->k22, K->kq12, K->k16, K->k26, K->k66, K->k16h, K->k26h};
@@ -533,10 +543,14 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   const size_t shot_off = (size_t)shot * 2 * N;
 
   // -------- initial state: zero the levels and the load, then load
-  for (int e = tid; e < 3 * level_floats + R * ny; e += kResThreads) smem[e] = 0.f;
+  {
+    float4* z4 = reinterpret_cast<float4*>(smem);  // ny % 4 == 0: whole float4s
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int e = tid; e < (3 * level_floats + R * ny) / 4; e += kResThreads) z4[e] = zero;
+  }
   if (tid == 0) {
     *rec_count = 0;
-    for (int l = 0; l < 3; ++l) mbar_init(&bar[l], 1);
+    for (int l = 0; l < 4; ++l) mbar_init(&bar[l], 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -568,16 +582,42 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   }
   const float* init_cur = is_fwd ? f.init_cur : (a.first ? nullptr : a.lam_save);
   const float* init_prev = is_fwd ? f.init_prev : (a.first ? nullptr : a.lam_save + a.save_stride);
-  // step 0 reads L[0] (with halo rows, from global memory) and L[2] (own rows)
-  for (int e = tid; e < 2 * (rows + 2) * ny; e += kResThreads) {
-    const int comp = e / ((rows + 2) * ny);
-    const int rem = e - comp * (rows + 2) * ny;
-    const int s = rem / ny, j = rem - s * ny;
-    const int gi = r0 + s - 1;
-    if (gi < 0 || gi >= nx) continue;
-    const size_t gidx = shot_off + (size_t)comp * N + (size_t)gi * ny + j;
-    if (init_cur) T.comp(Lv(0), comp)[T.at(s, j)] = init_cur[gidx];
-    if (init_prev && s >= 1 && s <= rows) T.comp(Lv(2), comp)[T.at(s, j)] = init_prev[gidx];
+  // step 0 reads L[0] (with halo rows, from global memory) and L[2] (own
+  // rows): one bulk copy per component and level (rows are contiguous in
+  // both layouts; rows outside the grid stay zero), or element by element
+  // when a source is not on a 16-byte boundary
+  const bool bulk_init = (init_cur == nullptr || al16(init_cur)) && (init_prev == nullptr || al16(init_prev));
+  if (bulk_init) {
+    const int g_lo = max(r0 - 1, 0), g_hi = min(r0 + rows + 1, nx);  // rows of cur with its halo
+    const uint32_t cur_bytes = (uint32_t)((size_t)(g_hi - g_lo) * ny * sizeof(float));
+    const uint32_t prev_bytes = (uint32_t)((size_t)rows * ny * sizeof(float));
+    const uint32_t total = (init_cur ? 2u * cur_bytes : 0u) + (init_prev ? 2u * prev_bytes : 0u);
+    if (total > 0) {
+      if (tid == 0) {
+        fence_proxy_async();  // the zero stores above before the copies' writes
+        mbar_arrive_expect_tx(&bar[3], total);
+        for (int comp = 0; comp < 2; ++comp) {
+          if (init_cur)
+            bulk_g2s(T.comp(Lv(0), comp) + T.at(g_lo - r0 + 1, 0),
+                     init_cur + shot_off + (size_t)comp * N + (size_t)g_lo * ny, cur_bytes, &bar[3]);
+          if (init_prev)
+            bulk_g2s(T.comp(Lv(2), comp) + T.at(1, 0), init_prev + shot_off + (size_t)comp * N + (size_t)r0 * ny,
+                     prev_bytes, &bar[3]);
+        }
+      }
+      halo_wait(&bar[3], 0u, c.err);
+    }
+  } else {
+    for (int e = tid; e < 2 * (rows + 2) * ny; e += kResThreads) {
+      const int comp = e / ((rows + 2) * ny);
+      const int rem = e - comp * (rows + 2) * ny;
+      const int s = rem / ny, j = rem - s * ny;
+      const int gi = r0 + s - 1;
+      if (gi < 0 || gi >= nx) continue;
+      const size_t gidx = shot_off + (size_t)comp * N + (size_t)gi * ny + j;
+      if (init_cur) T.comp(Lv(0), comp)[T.at(s, j)] = init_cur[gidx];
+      if (init_prev && s >= 1 && s <= rows) T.comp(Lv(2), comp)[T.at(s, j)] = init_prev[gidx];
+    }
   }
   __syncthreads();
   cluster.sync();  // every CTA initialised (levels, mbarriers) before any push
@@ -760,7 +800,18 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     halo_wait(&bar[(t_last + 1) % 3], (parity_bits >> ((t_last + 1) % 3)) & 1u, c.err);
   if (tid == 0) bulk_wait_all();
   __syncthreads();
-  if (!is_fwd && a.m_hi >= a.m_lo + 1) {
+  if (!is_fwd && a.m_hi >= a.m_lo + 1 && al16(a.lam_save) && al16(a.lam_save + a.save_stride)) {
+    // lam^{m_lo+1} (level of step t_last + 1) and lam^{m_lo+2} -> lam_save,
+    // own rows by bulk copies
+    if (tid == 0) {
+      fence_proxy_async();
+      store_level(Lv((t_last + 1) % 3), a.lam_save + shot_off, (ptrdiff_t)N);
+      store_level(Lv(t_last % 3), a.lam_save + a.save_stride + shot_off, (ptrdiff_t)N);
+      bulk_commit();
+      bulk_wait_all();
+    }
+    __syncthreads();
+  } else if (!is_fwd && a.m_hi >= a.m_lo + 1) {
     // lam^{m_lo+1} (level of step t_last + 1) and lam^{m_lo+2} -> lam_save
     float* last = Lv((t_last + 1) % 3);
     float* before = Lv(t_last % 3);
@@ -779,7 +830,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
 // ---------------------------------------------------------------- host side
 size_t resident_smem_bytes(const ResCommon& c) {
   const size_t level = 2 * (size_t)(c.R + 2) * c.ny * sizeof(float);
-  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 3 * sizeof(uint64_t) + 16;
+  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 4 * sizeof(uint64_t) + 16;
   return 3 * level + (size_t)c.R * c.ny * sizeof(float) + tail;
 }
 
