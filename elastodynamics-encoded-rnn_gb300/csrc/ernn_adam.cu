@@ -28,10 +28,16 @@ __global__ void __launch_bounds__(kAdamThreads)
     adam_kernel(const ErnnAdamTensor* __restrict__ tensors, ErnnAdamHyper h, int32_t* __restrict__ state) {
   const ErnnAdamTensor T = tensors[blockIdx.y];
   const int32_t t = state[0] + 1;
-  const double bc1 = 1.0 - pow(h.beta1, (double)t);
-  const double bc2 = 1.0 - pow(h.beta2, (double)t);
-  const float step_size = (float)(h.lr / bc1);
-  const float sqrt_bc2 = (float)sqrt(bc2);
+  // bias corrections in FP64 by one thread (the FP64 pipe is narrow), shared
+  __shared__ float corr[2];
+  if (threadIdx.x == 0) {
+    const double bc1 = 1.0 - pow(h.beta1, (double)t);
+    const double bc2 = 1.0 - pow(h.beta2, (double)t);
+    corr[0] = (float)(h.lr / bc1);
+    corr[1] = (float)sqrt(bc2);
+  }
+  __syncthreads();
+  const float step_size = corr[0], sqrt_bc2 = corr[1];
   const float b1 = (float)h.beta1, b2 = (float)h.beta2, eps = (float)h.eps, wd = (float)h.weight_decay;
   for (int64_t e = (int64_t)blockIdx.x * kAdamThreads + threadIdx.x; e < T.n;
        e += (int64_t)gridDim.x * kAdamThreads) {
