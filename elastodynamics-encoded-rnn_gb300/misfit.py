@@ -55,9 +55,9 @@ class SeriesMisfit(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, px, py, ox, oy, wx, wy, frame_stride, space_stride):
+        s = _series(px, frame_stride, space_stride, wx, wy)  # layout first: host-side checks
         px, py, ox, oy = (t.contiguous() for t in (px, py, ox, oy))
         _check(px, py, ox, oy)
-        s = _series(px, frame_stride, space_stride, wx, wy)
         lib = _lib.load()
         dev = px.device
         with torch.cuda.device(dev):

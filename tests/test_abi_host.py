@@ -172,3 +172,21 @@ def test_fused_adam_refuses_cpu_parameters():
     p.grad = torch.ones(4)
     with pytest.raises(RuntimeError, match="CUDA"):
         FusedAdam([p]).step()
+
+
+def test_series_misfit_validates_on_the_host():
+    from ernn_gb300.misfit import series_misfit
+    a = torch.zeros((1, 4, 6))
+    with pytest.raises(RuntimeError, match="CUDA"):
+        series_misfit(a, a, a, a)
+    with pytest.raises(ValueError):
+        series_misfit(torch.zeros(3), torch.zeros(3), torch.zeros(3), torch.zeros(3))
+
+
+def test_fused_adam_rejects_bad_hyper_parameters():
+    from ernn_gb300.optim import FusedAdam
+    p = torch.zeros(3, requires_grad=True)
+    for kw in (dict(lr=-1.0), dict(betas=(1.0, 0.9)), dict(betas=(0.9, 1.0)), dict(eps=-1.0),
+               dict(weight_decay=-0.1)):
+        with pytest.raises(ValueError):
+            FusedAdam([p], **kw)
