@@ -439,6 +439,84 @@ def run_ernn(args, dist):
     return rec
 
 
+def _dense_load(geom, dtype, device):
+    """(S, nx, ny) load of a geometry's cropped source boxes."""
+    S = geom.nshots
+    load = torch.zeros((S, geom.nx, geom.ny), dtype=dtype)
+    smap = geom.src_map.detach().cpu().to(dtype)
+    org = geom.src_origin.detach().cpu().tolist()
+    bx, by = smap.shape[1], smap.shape[2]
+    for s in range(S):
+        ox, oy = org[s]
+        a0, a1 = max(0, -ox), min(bx, geom.nx - ox)
+        b0, b1 = max(0, -oy), min(by, geom.ny - oy)
+        if a0 < a1 and b0 < b1:
+            load[s, ox + a0:ox + a1, oy + b0:oy + b1] = smap[s, a0:a1, b0:b1]
+    return load.to(device)
+
+
+def multi_grad_errors(inv, max_side=128, count=3):
+    """Hand-adjoint gradients (FP32 fields, FP64 sums) of the first `count`
+    instances with side <= max_side against the restated reference path in
+    FP64 with autograd on the host cores, at the instances' current
+    constants: relative L2 error of the gradient of the normalised constants."""
+    import ernn_gb300.harness as Hn
+    from oracle import torch_ref
+    out = []
+    for one in inv.invs:
+        if len(out) >= count or one.w.nx > max_side:
+            continue
+        g = one.geom
+        theta = one.params.theta
+        theta.grad = None
+        ux, uy = Hn.propagate(one.params(), one.rho, g)
+        Hn.trace_misfit(ux, uy, one.obs[0], one.obs[1]).backward()
+        g32 = theta.grad.detach().double().cpu()
+        t64 = theta.detach().double().cpu().requires_grad_(True)
+        C = t64 * one.params.scale.detach().double().cpu()
+        rho = torch.tensor(float(one.rho), dtype=torch.float64)
+        px, py = torch_ref.propagate([C[i] for i in range(6)], rho, g.nx, g.ny, g.nt, g.h, g.dt,
+                                     g.src_signal.detach().double().cpu(), _dense_load(g, torch.float64, "cpu"),
+                                     g.stride, g.rec_idx.detach().cpu(), g.src_comp)
+        ox, oy = (o.detach().double().cpu() for o in one.obs)
+        (((px - ox) ** 2).mean() + ((py - oy) ** 2).mean()).backward()
+        e = float((g32 - t64.grad).norm() / t64.grad.norm())
+        out.append({"side": g.nx, "nt": g.nt, "grad_rel_err": round(e, 9)})
+    return out
+
+
+def multi_plain_autograd(inv, dev, nt=100, count=8):
+    """The restated reference path with autograd on the GPU (FP32), looped over
+    `count` instances spread over the sizes, `nt` steps each: cell-steps per
+    second of forward + backward (the plain form config 5 compares with)."""
+    import ernn_gb300.harness as Hn
+    from oracle import torch_ref
+    order = sorted(range(len(inv.invs)), key=lambda k: inv.invs[k].w.nx)
+    pick = [order[round(i * (len(order) - 1) / max(1, count - 1))] for i in range(count)]
+    cells, secs = 0, 0.0
+    for k in pick:
+        one = inv.invs[k]
+        g = one.geom
+        C = one.params().detach().clone().requires_grad_(True)
+        load = _dense_load(g, torch.float32, dev)
+        sig = g.src_signal[:, :nt].contiguous()
+        rec = g.rec_idx
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            px, py = torch_ref.propagate([C[i] for i in range(6)], one.rho, g.nx, g.ny, nt, g.h, g.dt,
+                                         sig, load, g.stride, rec, g.src_comp)
+            ((px.double() ** 2).mean() + (py.double() ** 2).mean()).backward()
+            torch.cuda.synchronize()
+            if rep == 1:
+                secs += time.perf_counter() - t0
+                cells += g.nx * g.ny * nt
+    return {"value": round(cells / secs / 1e9, 5), "unit": "Gcell-steps/s",
+            "sample": f"{count} of {len(inv.invs)} instances (sides "
+                      f"{sorted(inv.invs[k].w.nx for k in pick)}), {nt} steps each, "
+                      f"PyTorch restatement of the reference path with autograd on the same GPU"}
+
+
 def run_multi(args, dist):
     """multi64: 64 uneven inversions, one CUDA-graph-captured Adam iteration."""
     import ernn_gb300 as E
@@ -491,6 +569,15 @@ def run_multi(args, dist):
     torch.cuda.synchronize()
     e2e_ms = dist.max(sum(a.elapsed_time(b) for a, b in e2e) / args.steps)
     sides = [w.nx for w in ws]
+    # library kernels of one iteration (an eager iteration: replays make no host calls)
+    n_eager = lib.ernn_launch_count()
+    inv._eager_step()
+    torch.cuda.synchronize()
+    per_iter = lib.ernn_launch_count() - n_eager
+    extra = {}
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        extra["grad_error_vs_fp64"] = multi_grad_errors(inv)
+        extra["plain_autograd_loop"] = multi_plain_autograd(inv, dev)
     return {
         "metric": "Gcell-steps/s fwd+adj (hand adjoint, one Adam iteration)",
         "value": round(value, 4), "unit": "Gcell-steps/s", "n_gpus": dist.world,
@@ -508,7 +595,8 @@ def run_multi(args, dist):
                 "d2h_bytes_per_step": out_h.numel() * 8},
         "ms_per_iter": round(ms, 3), "graph_capture_setup_s": round(setup_s, 2),
         "host_launch_calls_in_timed_region": int(launches),
-        "clocks": clk, "loss": float(loss),
+        "gpu_launches": int(per_iter * args.steps),
+        "clocks": clk, "loss": float(loss), **extra,
     }
 
 
