@@ -527,7 +527,9 @@ def run_multi(args, dist):
     lib = E.load_library()
     ws = Hn.multi_instances(64)
     t0 = time.perf_counter()
-    inv = Hn.MultiInversion(ws, dev)
+    # configuration 5: kernel path per group from the autotuner, unless one is forced
+    tuned = args.path in ("auto", "tuned")
+    inv = Hn.MultiInversion(ws, dev, tuned=tuned, path=None if tuned else PATHS[args.path])
     setup_s = time.perf_counter() - t0
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(max(args.warmup, 0)):
@@ -589,6 +591,7 @@ def run_multi(args, dist):
                                f"{len(inv.groups)} groups of equal instances, each one call with "
                                f"per-shot constants, on 8 streams",
                    "cell_steps_per_iter": inv.cell_steps,
+                   "path_choice": "measured per group (autotune)" if tuned else args.path,
                    "l2": "flushed between timed iterations (256 MiB write)"},
         "e2e": {"value": round(dist.world * inv.cell_steps / (e2e_ms * 1e-3) / 1e9, 4),
                 "unit": "Gcell-steps/s", "h2d_bytes_per_step": sum(o.numel() * 4 for o in obs_h),

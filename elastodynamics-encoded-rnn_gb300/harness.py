@@ -437,7 +437,7 @@ class _InstanceGroup:
     the shots of one propagation with per-shot constants: each keeps its own
     constants, density, observations and gradient."""
 
-    def __init__(self, invs, device, budget_fraction):
+    def __init__(self, invs, device, budget_fraction, tuned=False):
         from .propagate import choose_ckpt_k
         from ._lib import FLAG_SHOT_CONSTANTS
         self.invs = invs
@@ -452,6 +452,10 @@ class _InstanceGroup:
                                          flags=FLAG_SHOT_CONSTANTS if S > 1 else 0)
         self.obs = [torch.cat([inv.obs[c] for inv in invs]).contiguous() for c in (0, 1)]
         self.rho = torch.full((S,), RHO, dtype=torch.float32, device=device)
+        if tuned:  # measured kernel path at the memory-sized interval (autotune keeps a fixed one)
+            from . import autotune
+            C = torch.stack([inv.params() for inv in invs]).detach() if S > 1 else invs[0].params().detach()
+            self.geom.path, self.geom.ckpt_k = autotune.tune(self.geom, C, self.rho if S > 1 else self.rho[0])
 
     def loss(self):
         if len(self.invs) == 1:
@@ -459,9 +463,10 @@ class _InstanceGroup:
             return trace_misfit(ux, uy, self.obs[0], self.obs[1])
         C = torch.stack([inv.params() for inv in self.invs])
         ux, uy = propagate(C, self.rho, self.geom)
-        # the sum of each instance's own misfit
-        return sum(trace_misfit(ux[s:s + 1], uy[s:s + 1], self.obs[0][s:s + 1], self.obs[1][s:s + 1])
-                   for s in range(len(self.invs)))
+        # the sum of each instance's own misfit: the instances share frames and
+        # receivers, so it is S times the mean over the group (one fused pass)
+        S = len(self.invs)
+        return series_misfit(ux, uy, self.obs[0], self.obs[1], float(S), float(S))
 
 
 class MultiInversion:
@@ -474,7 +479,7 @@ class MultiInversion:
     its own."""
 
     def __init__(self, ws, device, lr=1e-2, seed=0, nstreams=8, graph=True, group=True, path=None,
-                 serial_big=False):
+                 serial_big=False, tuned=False):
         self.ws = ws
         self.device = device
         if path is not None:
@@ -488,7 +493,7 @@ class MultiInversion:
             keyed.setdefault(key, []).append(inv)
         # largest work first: the longest groups start earliest on the streams
         members = sorted(keyed.values(), key=lambda g: -sum(i.w.cell_steps for i in g))
-        self.groups = [_InstanceGroup(g, device, 0.4 * len(g) / len(ws)) for g in members]
+        self.groups = [_InstanceGroup(g, device, 0.4 * len(g) / len(ws), tuned=tuned) for g in members]
         # streams: round robin over the groups, or (serial_big) groups large
         # enough for the tiled kernels one after another on the first stream
         # and the smaller ones on the others
