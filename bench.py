@@ -274,10 +274,14 @@ def run_ernn(args, dist):
     if args.path == "tuned":  # measured path and checkpoint interval (ernn_gb300.autotune)
         from ernn_gb300 import autotune
         damage = isinstance(inv, Hn.DamageInversion)
-        C = inv.C0 if damage else inv.params()
-        D = inv.D.detach() if damage else None
-        tuned = autotune.tune(inv.geom, C.detach(), inv.rho, D=D)
+        with torch.no_grad():  # no autograd graph outlives the probes
+            C = (inv.C0 if damage else inv.params()).detach()
+            D = inv.D.detach() if damage else None
+        tuned = autotune.tune(inv.geom, C, inv.rho, D=D)
+        del C, D
         inv.geom.path, inv.geom.ckpt_k = tuned
+        torch.cuda.synchronize()
+        E.check_device_status()
     if not args.eager:  # the whole iteration as one CUDA graph, replayed per step
         inv.capture()
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)

@@ -6,8 +6,8 @@ the state fits a cluster, tiled when a step has >= 4 tiles per SM, plain
 otherwise).  The rules are right for one problem running alone; for problems
 that share the GPU with others (the streams of a multi-instance iteration) or
 sit near a threshold, `tune` times the candidates instead: every eligible
-path — and, when the tape does not fit, the memory-sized interval and twice
-it — on a short forward + adjoint of the same problem (`probe_steps` steps,
+path — and, when the tape does not fit, the memory-sized interval and half
+of it — on a short forward + adjoint of the same problem (`probe_steps` steps,
 the problem's own shots, grid and receivers), and keeps the fastest.  Results
 are cached per (device name, grid, shots, steps, mode, record, per-shot
 constants) for the process, and optionally in a JSON file.
@@ -66,8 +66,11 @@ def tune(geom: Geometry, C: torch.Tensor, rho: torch.Tensor, D=None, probe_steps
     if geom.ckpt_k is not None:  # an interval the caller fixed is kept
         ks = [geom.ckpt_k]
     else:
+        # intervals within the same memory budget: the memory-sized one and
+        # half of it (a larger one would not leave room for a captured
+        # graph's own workspace pool)
         k_mem = choose_ckpt_k(geom, mode, dev, flags=flags)
-        ks = [k_mem] if k_mem >= geom.nt else sorted({k_mem, min(2 * k_mem, geom.nt - 1)})
+        ks = [k_mem] if k_mem >= geom.nt else sorted({max(1, k_mem // 2), k_mem})
     best = None
     for path in (_lib.PATH_RESIDENT, _lib.PATH_TILED, _lib.PATH_STEP):
         for k in ks:

@@ -61,8 +61,10 @@ Plan make_plan(const ErnnProblem& p) {
   // two recompute segments: the cluster-resident path recomputes segment j-1
   // while the adjoint consumes segment j
   pl.s_seg = off; if (!pl.store_all) off += (size_t)2 * pl.k * pl.state_bytes;
-  // lam buffers of the resident reverse pass: two segments of kres steps
+  // lam buffers of the resident reverse pass: two segments of kres steps,
+  // only where that path can run
   pl.kres = pl.store_all ? (p.nt < kResStoreAllSegment ? p.nt : kResStoreAllSegment) : pl.k;
+  if (!resident_possible(p.mode, p.nx, p.ny)) pl.kres = 0;
   pl.s_lbuf = off; off += (size_t)2 * pl.kres * pl.state_bytes;
   pl.s_gacc = off;
   if (p.mode == kModeDField) off += align_up((size_t)p.nshots * pl.N * sizeof(float));
@@ -165,7 +167,7 @@ int use_tiled(const ErnnProblem& p, int* tiled) {
 // Cluster-resident configuration: CL CTAs of R rows each.  Returns false when
 // the problem does not fit the path (mode, alignment, receivers, memory).
 bool pick_resident(const ErnnProblem& p, const ErnnInputs& in, Coef* coef, ResCommon& rc) {
-  if (p.mode != kModeScalar || p.ny % 4 != 0) return false;
+  if (!resident_possible(p.mode, p.nx, p.ny)) return false;  // (the plan reserved no lam buffers)
   if (p.record == kRecordReceivers && p.nrec > kResMaxRec) return false;
   rc.nx = p.nx; rc.ny = p.ny; rc.S = p.nshots; rc.nt = p.nt; rc.stride = p.stride;
   rc.nt_out = (p.nt + p.stride - 1) / p.stride;

@@ -886,11 +886,21 @@ static std::vector<std::pair<FeasKey, bool>> g_feas;
 
 static bool feasible_uncached(const ResCommon& c, bool dense, size_t smem);
 
+constexpr size_t kResSmemLimit = 220 * 1024;
+
+bool resident_possible(int mode, int nx, int ny) {
+  if (mode != kModeScalar || ny % 4 != 0 || nx < 1) return false;
+  ResCommon c{};
+  c.ny = ny;
+  c.R = (nx + 15) / 16;  // the most CTAs per cluster give the fewest rows per CTA
+  return resident_smem_bytes(c) <= kResSmemLimit;
+}
+
 bool resident_feasible(const ResCommon& c, bool dense) {
   if (c.CL < 1 || c.CL > 16 || c.ny % 4 != 0 || c.nrec > kResMaxRec) return false;
   if ((c.CL - 1) * c.R >= c.nx) return false;  // every CTA owns >= 1 row
   const size_t smem = resident_smem_bytes(c);
-  if (smem > 220 * 1024) return false;
+  if (smem > kResSmemLimit) return false;
   std::lock_guard<std::mutex> lock(g_feas_mu);
   for (const auto& kv : g_feas)
     if (kv.first.dense == dense && kv.first.CL == c.CL && kv.first.smem == smem) return kv.second;

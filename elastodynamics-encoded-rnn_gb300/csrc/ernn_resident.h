@@ -70,6 +70,9 @@ struct ResRoles {
 };
 
 size_t resident_smem_bytes(const ResCommon& c);
+// Whether any cluster size can hold a shot of this grid (the adjoint scratch
+// reserves the path's lam buffers only then).
+bool resident_possible(int mode, int nx, int ny);
 bool resident_feasible(const ResCommon& c, bool dense);
 // IMG clusters along z for one launch (total IMG CTAs = this x S x CL)
 int resident_img_clusters(const ResCommon& c);

@@ -226,6 +226,10 @@ class _GraphedIteration:
         torch.cuda.current_stream(dev).wait_stream(side)
         torch.cuda.synchronize(dev)
         check_device_status()
+        # the graph allocates from its own pool: hand the warm-up iterations'
+        # cached blocks back first, so no allocation during capture has to
+        # free memory (not allowed while capturing)
+        torch.cuda.empty_cache()
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self._loss = self.step_eager()
@@ -548,6 +552,7 @@ class MultiInversion:
         torch.cuda.current_stream(self.device).wait_stream(side)
         torch.cuda.synchronize(self.device)
         check_device_status()
+        torch.cuda.empty_cache()  # the graph's own pool allocates next
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.loss = self._eager_step()
