@@ -69,7 +69,9 @@ __device__ __forceinline__ void bar_wait(uint64_t* b, uint32_t parity, int* err)
   if (bar_try(b, parity)) return;
   if (*(volatile int*)err != 0) return;
   const long long t0 = clock64();
-  while (!bar_try(b, parity)) {
+  for (;;) {
+    for (int k = 0; k < 64; ++k)  // the clock is read once per 64 polls
+      if (bar_try(b, parity)) return;
     if (clock64() - t0 > kWaitLimitCycles) {
       atomicExch(err, kDeviceTimeout);
       return;
@@ -879,14 +881,14 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         const float4 u4x = *reinterpret_cast<const float4*>(ub + r * kTY + j);
         const float4 u4y = *reinterpret_cast<const float4*>(ub + L::kTR * kTY + r * kTY + j);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 4; ++q) {  // each sum as a chain of fused multiply-adds
           const float ux = g4(u4x, q), uy = g4(u4y, q);
-          acc[0] += ux * st.xx_x[q];
-          acc[1] += uy * st.yy_y[q];
-          acc[2] += uy * st.xy_x[q] + ux * st.xy_y[q];
-          acc[3] += ux * (0.5f * st.xy_x[q] + st.xx_y[q]) + uy * st.xx_x[q];
-          acc[4] += uy * (st.yy_x[q] + 0.5f * st.xy_y[q]) + ux * st.yy_y[q];
-          acc[5] += ux * st.yy_x[q] + uy * st.xx_y[q];
+          acc[0] = fmaf(ux, st.xx_x[q], acc[0]);
+          acc[1] = fmaf(uy, st.yy_y[q], acc[1]);
+          acc[2] = fmaf(ux, st.xy_y[q], fmaf(uy, st.xy_x[q], acc[2]));
+          acc[3] = fmaf(uy, st.xx_x[q], fmaf(ux, fmaf(0.5f, st.xy_x[q], st.xx_y[q]), acc[3]));
+          acc[4] = fmaf(ux, st.yy_y[q], fmaf(uy, fmaf(0.5f, st.xy_y[q], st.yy_x[q]), acc[4]));
+          acc[5] = fmaf(uy, st.xx_y[q], fmaf(ux, st.yy_x[q], acc[5]));
         }
       }
       if (MODE == kModeDField && has_u) {
