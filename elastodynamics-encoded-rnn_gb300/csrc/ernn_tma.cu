@@ -94,12 +94,16 @@ __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int
 // others between tiles.  The values read from the stage are all consumed
 // (in registers) before a lane arrives.
 template <typename F>
-__device__ __forceinline__ void release(int* done, int k, F&& refill) {
+__device__ __forceinline__ void release_stage(int* done, int stage, F&& refill) {
   __syncwarp();
   if ((threadIdx.x & 31) == 0) {
-    const int old = atomicAdd(&done[k & 1], 1);
+    const int old = atomicAdd(&done[stage], 1);
     if (old % (kThreads / 32) == kThreads / 32 - 1) refill();
   }
+}
+template <typename F>
+__device__ __forceinline__ void release(int* done, int k, F&& refill) {
+  release_stage(done, k & 1, refill);
 }
 
 // TMA destinations start on 128-byte boundaries: the dynamic shared block is
@@ -636,6 +640,10 @@ struct AdjLayout {
   static constexpr int kD = kU + kHalo;  // DFIELD only
   static constexpr int kEnd = (MODE == kModeScalar) ? kU + kOwn : kD + kBHa * kBW;
   static constexpr int kStage = (kEnd + 31) / 32 * 32;  // 128-byte multiple
+  // two stages (one tile in flight while one is computed); three stages at
+  // two CTAs per SM measured slower for SCALAR (150 vs 114 us per shots1024
+  // step): the kernel needs the third CTA's warps more than a deeper pipeline
+  static constexpr int kStages = 2;
   static constexpr int kCtasPerSm = (MODE == kModeScalar) ? 3 : 2;
 };
 
@@ -647,7 +655,8 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   using L = AdjLayout<MODE>;
   extern __shared__ float sm_raw[];
   float* sm = aligned128(sm_raw);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * L::kStage);
+  constexpr int NS = L::kStages;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + NS * L::kStage);
   __shared__ double red[kThreads / 32][6];
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
@@ -657,14 +666,15 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
                                         ? L::kHalo + L::kOwn + (has_u ? L::kOwn : 0)
                                         : L::kHalo + L::kBHa * kBW + (has_u ? L::kHalo : 0)) * 4u;
   grid_dep_trigger();
-  __shared__ int done[2];
+  __shared__ int done[NS];
   if (tid == 0) {
     prefetch_map(&cur_map);
     prefetch_map(MODE == kModeScalar ? &prev_map : &d_map);
     if (has_u) prefetch_map(&u_map);
-    bar_init(&bar[0]);
-    bar_init(&bar[1]);
-    done[0] = done[1] = 0;
+    for (int q = 0; q < NS; ++q) {
+      bar_init(&bar[q]);
+      done[q] = 0;
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -684,23 +694,22 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     const int t = t_first + k * t_step;
     if (t >= t_end) return;
     const TileId id = tile_of<L::kTR>(t, tiles_x, tiles_y);
-    float* st = sm + (k & 1) * L::kStage;
+    const int sg = k % NS;
+    float* st = sm + sg * L::kStage;
     fence_async();
-    bar_expect(&bar[k & 1], bytes);
-    tma_load3(st + L::kLam, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+    bar_expect(&bar[sg], bytes);
+    tma_load3(st + L::kLam, &cur_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[sg]);
     if (MODE == kModeScalar)
-      tma_load3(st + L::kPrev, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
+      tma_load3(st + L::kPrev, &prev_map, id.y0, id.x0, 2 * id.shot, &bar[sg]);
     else
-      tma_load2(st + L::kD, &d_map, id.y0 - 4, id.x0 - 1, &bar[k & 1]);
+      tma_load2(st + L::kD, &d_map, id.y0 - 4, id.x0 - 1, &bar[sg]);
     if (has_u) {
-      if (MODE == kModeScalar) tma_load3(st + L::kU, &u_map, id.y0, id.x0, 2 * id.shot, &bar[k & 1]);
-      else tma_load3(st + L::kU, &u_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[k & 1]);
+      if (MODE == kModeScalar) tma_load3(st + L::kU, &u_map, id.y0, id.x0, 2 * id.shot, &bar[sg]);
+      else tma_load3(st + L::kU, &u_map, id.y0 - 4, id.x0 - 1, 2 * id.shot, &bar[sg]);
     }
   };
-  if (tid == 0) {
-    issue(0);
-    issue(1);
-  }
+  if (tid == 0)
+    for (int q = 0; q < NS; ++q) issue(q);
   const int qc = tid & 15, rg = tid >> 4;
   const int j = 4 * qc;
   const bool inject = a.frame >= 0 && a.record == kRecordReceivers;
@@ -773,8 +782,9 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         pv[q2][1] = in ? *reinterpret_cast<const float4*>(a.prev + N + o) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
-    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
-    float* hb = sm + (k & 1) * L::kStage;
+    const int stage = k % NS;
+    bar_wait(&bar[stage], (uint32_t)(k / NS) & 1u, err);
+    float* hb = sm + stage * L::kStage;
     float* pb = hb + L::kPrev;
     const float* ub = hb + L::kU;
     const float* db = hb + L::kD;
@@ -931,7 +941,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         }
       }
     }
-    release(done, k, [&] { issue(k + 2); });
+    release_stage(done, stage, [&] { issue(k + NS); });
   }
   if (MODE != kModeScalar || !has_u) return;
   flush(per_shot ? acc_shot : 0);
@@ -1021,7 +1031,7 @@ constexpr size_t kFwdSmem = 2 * (size_t)FwdLayout::kStage * 4 + 16 + 128;
 constexpr size_t kFwd2Smem = (2 * (size_t)Fwd2Layout::kStage + 2 * (size_t)Fwd2Layout::kMid) * 4 + 16 + 128;
 template <int MODE>
 constexpr size_t adj_smem() {
-  return 2 * (size_t)AdjLayout<MODE>::kStage * 4 + 16 + 128;
+  return (size_t)AdjLayout<MODE>::kStages * AdjLayout<MODE>::kStage * 4 + 8 * AdjLayout<MODE>::kStages + 128;
 }
 
 cudaError_t set_smem() {
