@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
 // before the wait (keeps two CTAs per SM within shared memory).
 template <int MODE>
 struct AdjLayout {
-  // SCALAR: 64 x 16 tiles, one row per thread (79 registers: three CTAs
+  // SCALAR: 64 x 16 tiles, one row per thread (80 registers: three CTAs
   // per SM).  DFIELD keeps 64 x 32 tiles and two rows per thread: with one
   // row its three halo windows per output row (lam, u, D) cost more than the
   // third CTA gains (24.4 vs 21.5 us per damage512 step)
