@@ -176,6 +176,28 @@ def profiled_traffic(kernel, workload):
 
 
 # --------------------------------------------------------------------------
+_CPU_EXTRA = {}
+
+
+def _cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), or "unknown"."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
 def cpu_sample(workload, nt_sample, iters=2):
     """The reference path (PyTorch restatement, autograd) on the host cores:
     forward (receiver traces) -> misfit -> backward -> Adam, truncated to
@@ -200,9 +222,13 @@ def cpu_sample(workload, nt_sample, iters=2):
     theta = torch.nn.Parameter(torch.tensor(Hn.initial_guess(w) / Hn.scales(w.C_true), dtype=torch.float32))
     sc = torch.tensor(Hn.scales(w.C_true), dtype=torch.float32)
     opt = torch.optim.Adam([theta], lr=1e-2)
-    with torch.no_grad():
+    with torch.no_grad():  # the observations: also the forward-only timing
         Ct = [torch.tensor(float(c)) for c in w.C_true]
+        t0 = time.perf_counter()
         ox, oy = torch_ref.propagate(Ct, rho, w.nx, w.ny, nt_sample, Hn.H, Hn.DT, sig, load, 1, rec)
+        t_fwd = time.perf_counter() - t0
+    _CPU_EXTRA["forward_only"] = round(w.nshots * w.nx * w.ny * nt_sample / t_fwd / 1e9, 6)
+    _CPU_EXTRA["cpu_model"] = _cpu_model()
     times = []
     for _ in range(iters):
         t0 = time.perf_counter()
@@ -439,7 +465,8 @@ def run_ernn(args, dist):
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         v, thr, sample = cpu_sample(args.workload, args.cpu_sample_steps)
         rec["cpu_baseline"] = {"value": round(v, 6), "unit": "Gcell-steps/s", "cores": thr,
-                               "kind": "port", "sample": sample + " (PyTorch restatement of the reference path, autograd)"}
+                               "kind": "port", "sample": sample + " (PyTorch restatement of the reference path, autograd)",
+                               **_CPU_EXTRA}
     return rec
 
 
@@ -729,7 +756,7 @@ def run_reference(args, dist):
         "config": {"workload": f"{w.name}: {w.nx}x{w.ny} grid, {w.nt} steps (sampled {nts}), "
                                f"{w.nshots} shot(s), {len(w.rec_cells)} receivers"},
         "cpu_baseline": {"value": round(value, 6), "unit": "Gcell-steps/s", "cores": thr,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": sample, **_CPU_EXTRA},
         "e2e": {"value": round(value, 6), "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
