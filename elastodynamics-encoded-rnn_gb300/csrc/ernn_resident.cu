@@ -158,19 +158,48 @@ struct Quad {
   float xx_x[4], yy_x[4], xy_x[4], xx_y[4], yy_y[4], xy_y[4];
 };
 
+// Packed FP32 (sm_100 family): one instruction for two cells of a quad, each
+// lane rounded as the scalar operation.  The step loop is issue bound; sums
+// whose operands are column neighbours (not register pairs of the window)
+// are formed by scalar adds first, so every value keeps the association and
+// rounding of the scalar formulas.
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 pair(const float v[4], int p) { return make_float2(v[2 * p], v[2 * p + 1]); }
+__device__ __forceinline__ float2 pair4(const float4& v, int p) {
+  return p == 0 ? make_float2(v.x, v.y) : make_float2(v.z, v.w);
+}
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void put(float v[4], int p, float2 a) {
+  v[2 * p] = a.x;
+  v[2 * p + 1] = a.y;
+}
+
+// One component (cell q at window column k = q + 1):
+//   xx = (u[0][k] + u[2][k]) - 2 u[1][k],  yy = (u[1][k-1] + u[1][k+1]) - 2 u[1][k],
+//   xy = (u[2][k+1] + u[0][k-1]) - (u[2][k-1] + u[0][k+1]).
+__device__ __forceinline__ void comp_stencils(const float u[3][6], float xx[4], float yy[4], float xy[4]) {
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int k = 2 * p + 1;
+    const float2 m0 = make_float2(u[0][k], u[0][k + 1]);
+    const float2 m1 = make_float2(u[1][k], u[1][k + 1]);
+    const float2 m2 = make_float2(u[2][k], u[2][k + 1]);
+    put(xx, p, __ffma2_rn(dup2(-2.f), m1, __fadd2_rn(m0, m2)));
+    put(yy, p, __ffma2_rn(dup2(-2.f), m1, make_float2(u[1][k - 1] + u[1][k + 1], u[1][k] + u[1][k + 2])));
+    const float2 a = make_float2(u[2][k + 1] + u[0][k - 1], u[2][k + 2] + u[0][k]);
+    const float2 b = make_float2(u[2][k - 1] + u[0][k + 1], u[2][k] + u[0][k + 2]);
+    put(xy, p, __fadd2_rn(a, neg2(b)));
+  }
+}
+
 __device__ __forceinline__ void quad_stencils(const float ux[3][6], const float uy[3][6], Quad& s) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const int k = q + 1;
-    s.cx[q] = ux[1][k];
-    s.cy[q] = uy[1][k];
-    s.xx_x[q] = (ux[0][k] + ux[2][k]) - 2.f * ux[1][k];
-    s.yy_x[q] = (ux[1][k - 1] + ux[1][k + 1]) - 2.f * ux[1][k];
-    s.xy_x[q] = (ux[2][k + 1] + ux[0][k - 1]) - (ux[2][k - 1] + ux[0][k + 1]);
-    s.xx_y[q] = (uy[0][k] + uy[2][k]) - 2.f * uy[1][k];
-    s.yy_y[q] = (uy[1][k - 1] + uy[1][k + 1]) - 2.f * uy[1][k];
-    s.xy_y[q] = (uy[2][k + 1] + uy[0][k - 1]) - (uy[2][k - 1] + uy[0][k + 1]);
+    s.cx[q] = ux[1][q + 1];
+    s.cy[q] = uy[1][q + 1];
   }
+  comp_stencils(ux, s.xx_x, s.yy_x, s.xy_x);
+  comp_stencils(uy, s.xx_y, s.yy_y, s.xy_y);
 }
 
 struct KSr {
@@ -182,6 +211,22 @@ __device__ __forceinline__ void lq(const KSr& k, const Quad& s, int q, float& lx
        k.k16 * s.xx_y[q] + k.k26 * s.yy_y[q];
   ly = k.k66 * s.xx_y[q] + k.k22 * s.yy_y[q] + k.kq12 * s.xy_x[q] + k.k16 * s.xx_x[q] +
        k.k26 * s.yy_x[q] + k.k26h * s.xy_y[q];
+}
+
+// (L u) of cells 2p and 2p+1: the terms of lq() in the same order.
+__device__ __forceinline__ void lq2(const KSr& k, const Quad& s, int p, float2& lx, float2& ly) {
+  lx = __fmul2_rn(dup2(k.k11), pair(s.xx_x, p));
+  lx = __ffma2_rn(dup2(k.k66), pair(s.yy_x, p), lx);
+  lx = __ffma2_rn(dup2(k.kq12), pair(s.xy_y, p), lx);
+  lx = __ffma2_rn(dup2(k.k16h), pair(s.xy_x, p), lx);
+  lx = __ffma2_rn(dup2(k.k16), pair(s.xx_y, p), lx);
+  lx = __ffma2_rn(dup2(k.k26), pair(s.yy_y, p), lx);
+  ly = __fmul2_rn(dup2(k.k66), pair(s.xx_y, p));
+  ly = __ffma2_rn(dup2(k.k22), pair(s.yy_y, p), ly);
+  ly = __ffma2_rn(dup2(k.kq12), pair(s.xy_x, p), ly);
+  ly = __ffma2_rn(dup2(k.k16), pair(s.xx_x, p), ly);
+  ly = __ffma2_rn(dup2(k.k26), pair(s.yy_x, p), ly);
+  ly = __ffma2_rn(dup2(k.k26h), pair(s.xy_y, p), ly);
 }
 
 __device__ __forceinline__ void shift6(float u[3][6]) {
@@ -235,31 +280,35 @@ __device__ __forceinline__ void row_step(const Tile& T, const KSr& ks, const Ste
   quad_stencils(wx, wy, st);
   const float4 pvx = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(x.prev), 0) + T.at(s, j));
   const float4 pvy = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(x.prev), 1) + T.at(s, j));
-  float vx[4], vy[4];
+  // v = (2 c - p) + L u (2 c is exact: one rounding either way), then the
+  // right-hand side; two cells per instruction
+  float2 v2x[2], v2y[2];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    float lx, ly;
-    lq(ks, st, q, lx, ly);
-    vx[q] = (2.f * st.cx[q] - at4(pvx, q)) + lx;
-    vy[q] = (2.f * st.cy[q] - at4(pvy, q)) + ly;
+  for (int p = 0; p < 2; ++p) {
+    float2 lx, ly;
+    lq2(ks, st, p, lx, ly);
+    const float2 px = pair4(pvx, p), py = pair4(pvy, p);
+    v2x[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cx, p), neg2(px)), lx);
+    v2y[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cy, p), neg2(py)), ly);
   }
   if (!LAM) {
     const float4 fl = *reinterpret_cast<const float4*>(rhs.F + lr * ny + j);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const float fz = rhs.amp * at4(fl, q);
-      if (rhs.src_comp == 0) vx[q] += fz; else vy[q] += fz;
+    for (int p = 0; p < 2; ++p) {
+      const float2 fz = __fmul2_rn(dup2(rhs.amp), pair4(fl, p));
+      if (rhs.src_comp == 0) v2x[p] = __fadd2_rn(v2x[p], fz); else v2y[p] = __fadd2_rn(v2y[p], fz);
     }
   } else if (DENSE && rhs.gx != nullptr) {
     const float4 a4 = *reinterpret_cast<const float4*>(rhs.gx + (size_t)lr * ny + j);
     const float4 b4 = *reinterpret_cast<const float4*>(rhs.gy + (size_t)lr * ny + j);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      vx[q] += rhs.gs * at4(a4, q);
-      vy[q] += rhs.gs * at4(b4, q);
+    for (int p = 0; p < 2; ++p) {
+      v2x[p] = __ffma2_rn(dup2(rhs.gs), pair4(a4, p), v2x[p]);
+      v2y[p] = __ffma2_rn(dup2(rhs.gs), pair4(b4, p), v2y[p]);
     }
   }
-  const float4 nvx = f4(vx), nvy = f4(vy);
+  const float4 nvx = make_float4(v2x[0].x, v2x[0].y, v2x[1].x, v2x[1].y);
+  const float4 nvy = make_float4(v2y[0].x, v2y[0].y, v2y[1].x, v2y[1].y);
   *reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j)) = nvx;
   *reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j)) = nvy;
   if (lr == 0 && x.up_base) {  // into rank-1's bottom halo row

@@ -139,22 +139,72 @@ __device__ __forceinline__ void win(const float* __restrict__ box, int r, int j,
   w[5] = p[4];
 }
 
+// Packed FP32 (sm_100 family): one instruction applies the same operation to
+// two cells of a quad, each lane rounded as the scalar operation would be.
+// The kernels are issue bound, so halving the arithmetic instructions is
+// what counts.  Sums whose operands are column neighbours (not register
+// pairs of the window) are formed by scalar adds first, so every value keeps
+// the association and rounding of the scalar formulas.
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 pair(const float v[4], int p) { return make_float2(v[2 * p], v[2 * p + 1]); }
+__device__ __forceinline__ float2 pair4(const float4& v, int p) {
+  return p == 0 ? make_float2(v.x, v.y) : make_float2(v.z, v.w);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void put(float v[4], int p, float2 a) {
+  v[2 * p] = a.x;
+  v[2 * p + 1] = a.y;
+}
+
 struct Sums4 {
   float cx[4], cy[4], xx_x[4], yy_x[4], xy_x[4], xx_y[4], yy_y[4], xy_y[4];
 };
 
-__device__ __forceinline__ void sums4(const float ux[3][6], const float uy[3][6], Sums4& s) {
+// Second differences of one component at the four cells of a window row
+// (cell q at window column q + 1):
+//   xx = (u[0][k] + u[2][k]) - 2 u[1][k],  yy = (u[1][k-1] + u[1][k+1]) - 2 u[1][k],
+//   xy = (u[2][k+1] + u[0][k-1]) - (u[2][k-1] + u[0][k+1]).
+__device__ __forceinline__ void comp_sums(const float u[3][6], float xx[4], float yy[4], float xy[4]) {
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int k = 2 * p + 1;
+    const float2 m0 = make_float2(u[0][k], u[0][k + 1]);
+    const float2 m1 = make_float2(u[1][k], u[1][k + 1]);
+    const float2 m2 = make_float2(u[2][k], u[2][k + 1]);
+    put(xx, p, fma2(dup2(-2.f), m1, __fadd2_rn(m0, m2)));
+    put(yy, p, fma2(dup2(-2.f), m1, make_float2(u[1][k - 1] + u[1][k + 1], u[1][k] + u[1][k + 2])));
+    const float2 a = make_float2(u[2][k + 1] + u[0][k - 1], u[2][k + 2] + u[0][k]);
+    const float2 b = make_float2(u[2][k - 1] + u[0][k + 1], u[2][k] + u[0][k + 2]);
+    put(xy, p, __fadd2_rn(a, neg2(b)));
+  }
+}
+
+// The same sums one cell per instruction (identical values: every sum is
+// the same rounded operation); for kernels at their register limit.
+__device__ __forceinline__ void comp_sums_scalar(const float u[3][6], float xx[4], float yy[4], float xy[4]) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int k = q + 1;
-    s.cx[q] = ux[1][k];
-    s.cy[q] = uy[1][k];
-    s.xx_x[q] = (ux[0][k] + ux[2][k]) - 2.f * ux[1][k];
-    s.yy_x[q] = (ux[1][k - 1] + ux[1][k + 1]) - 2.f * ux[1][k];
-    s.xy_x[q] = (ux[2][k + 1] + ux[0][k - 1]) - (ux[2][k - 1] + ux[0][k + 1]);
-    s.xx_y[q] = (uy[0][k] + uy[2][k]) - 2.f * uy[1][k];
-    s.yy_y[q] = (uy[1][k - 1] + uy[1][k + 1]) - 2.f * uy[1][k];
-    s.xy_y[q] = (uy[2][k + 1] + uy[0][k - 1]) - (uy[2][k - 1] + uy[0][k + 1]);
+    xx[q] = (u[0][k] + u[2][k]) - 2.f * u[1][k];
+    yy[q] = (u[1][k - 1] + u[1][k + 1]) - 2.f * u[1][k];
+    xy[q] = (u[2][k + 1] + u[0][k - 1]) - (u[2][k - 1] + u[0][k + 1]);
+  }
+}
+
+template <bool PACKED = true>
+__device__ __forceinline__ void sums4(const float ux[3][6], const float uy[3][6], Sums4& s) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    s.cx[q] = ux[1][q + 1];
+    s.cy[q] = uy[1][q + 1];
+  }
+  if (PACKED) {
+    comp_sums(ux, s.xx_x, s.yy_x, s.xy_x);
+    comp_sums(uy, s.xx_y, s.yy_y, s.xy_y);
+  } else {
+    comp_sums_scalar(ux, s.xx_x, s.yy_x, s.xy_x);
+    comp_sums_scalar(uy, s.xx_y, s.yy_y, s.xy_y);
   }
 }
 
@@ -172,6 +222,46 @@ __device__ __forceinline__ void shift(float u[3][6]) {
 
 __device__ __forceinline__ float g4(const float4& v, int q) {
   return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w;
+}
+
+// (L u) of cells 2p and 2p+1: the terms of apply() in the same order.
+__device__ __forceinline__ void apply2(const Coefs& k, const Sums4& s, int p, float2& lx, float2& ly) {
+  lx = __fmul2_rn(dup2(k.k11), pair(s.xx_x, p));
+  lx = fma2(dup2(k.k66), pair(s.yy_x, p), lx);
+  lx = fma2(dup2(k.kq12), pair(s.xy_y, p), lx);
+  lx = fma2(dup2(k.k16h), pair(s.xy_x, p), lx);
+  lx = fma2(dup2(k.k16), pair(s.xx_y, p), lx);
+  lx = fma2(dup2(k.k26), pair(s.yy_y, p), lx);
+  ly = __fmul2_rn(dup2(k.k66), pair(s.xx_y, p));
+  ly = fma2(dup2(k.k22), pair(s.yy_y, p), ly);
+  ly = fma2(dup2(k.kq12), pair(s.xy_x, p), ly);
+  ly = fma2(dup2(k.k16), pair(s.xx_x, p), ly);
+  ly = fma2(dup2(k.k26), pair(s.yy_x, p), ly);
+  ly = fma2(dup2(k.k26h), pair(s.xy_y, p), ly);
+}
+
+// Leapfrog update of a quad: v = (2 c - p) + w (L u), w = 1 unless WEIGHT
+// (2 c is exact, so 2 c - p is one rounding either way).
+template <bool WEIGHT>
+__device__ __forceinline__ void leap4(const Coefs& k, const Sums4& s, const float cx[4], const float cy[4],
+                                      const float4& pvx, const float4& pvy, const float4& w, float vx[4],
+                                      float vy[4]) {
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    float2 lx, ly;
+    apply2(k, s, p, lx, ly);
+    if (WEIGHT) {
+      lx = __fmul2_rn(lx, pair4(w, p));
+      ly = __fmul2_rn(ly, pair4(w, p));
+    }
+    const float2 px = pair4(pvx, p), py = pair4(pvy, p);
+    const float2 ax = __fadd2_rn(fma2(dup2(2.f), pair(cx, p), neg2(px)), lx);
+    const float2 ay = __fadd2_rn(fma2(dup2(2.f), pair(cy, p), neg2(py)), ly);
+    vx[2 * p] = ax.x;
+    vx[2 * p + 1] = ax.y;
+    vy[2 * p] = ay.x;
+    vy[2 * p + 1] = ay.y;
+  }
 }
 
 struct TileId {
@@ -353,17 +443,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
         pvy = *reinterpret_cast<const float4*>(pb + F::kTR * kTY + r * kTY + j);
       }
       float vx[4], vy[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        float lx, ly;
-        apply(ks, st, q, lx, ly);
-        if (MODE == kModeDField) {
-          lx *= g4(w4[q2], q);
-          ly *= g4(w4[q2], q);
-        }
-        vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
-        vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
-      }
+      leap4<MODE == kModeDField>(ks, st, st.cx, st.cy, pvx, pvy, MODE == kModeDField ? w4[q2] : pvx, vx, vy);
       // source box: rows and columns of this thread's 4 cells inside it
       const int sa = gi - ox;
       if (has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
@@ -529,7 +609,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
         win_lanes(cb + F::kBH2 * kBW, m + d, b, left_ok, right_ok, wy[d]);
       }
       Sums4 st;
-      sums4(wx, wy, st);
+      sums4<false>(wx, wy, st);
       float4 pvx = make_float4(0.f, 0.f, 0.f, 0.f), pvy = pvx;
       if (has_prev) {
         pvx = *reinterpret_cast<const float4*>(pb + m * kBW + b);
@@ -538,12 +618,11 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
       const int gi = id.x0 + m - 1, gj = id.y0 - 4 + b;  // ny % 4 == 0: a quad is in or out
       const bool inside = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
       float vx[4], vy[4];
+      leap4<false>(ks, st, st.cx, st.cy, pvx, pvy, pvx, vx, vy);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        float lx, ly;
-        apply(ks, st, q, lx, ly);
-        vx[q] = inside ? (2.f * st.cx[q] - g4(pvx, q)) + lx : 0.f;
-        vy[q] = inside ? (2.f * st.cy[q] - g4(pvy, q)) + ly : 0.f;
+        vx[q] = inside ? vx[q] : 0.f;
+        vy[q] = inside ? vy[q] : 0.f;
       }
       const int sa = gi - ox;
       if (inside && has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
@@ -584,13 +663,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
       const float4 pvy = *reinterpret_cast<const float4*>(cb + F::kBH2 * kBW + (rg + 2) * kBW + j + 4);
       const int gi = id.x0 + rg, gj = id.y0 + j;
       float vx[4], vy[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        float lx, ly;
-        apply(ks, st, q, lx, ly);
-        vx[q] = (2.f * st.cx[q] - g4(pvx, q)) + lx;
-        vy[q] = (2.f * st.cy[q] - g4(pvy, q)) + ly;
-      }
+      leap4<false>(ks, st, st.cx, st.cy, pvx, pvy, pvx, vx, vy);
       const int sa = gi - ox;
       if (has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
 #pragma unroll
@@ -718,18 +791,21 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   // launches.  Partial row: blockIdx.x; with per-shot constants
   // shot * kTiledRowsPerShot + blockIdx.x, flushed when the CTA's
   // tile list moves on to the next shot (shots never recur: t increases).
-  // (the FP32 sums of a thread's cells are folded into the pair every two
-  // tiles and before a flush)
+  // (the FP32 sums of a thread's cells, two lanes of packed sums, are folded
+  // into the pair every four tiles and before a flush)
   float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float2 acc[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) acc[q] = dup2(0.f);
   auto fold = [&] {
 #pragma unroll
     for (int q = 0; q < 6; ++q) {  // TwoSum(hi, acc)
-      const float s = hi[q] + acc[q];
+      const float a = acc[q].x + acc[q].y;
+      const float s = hi[q] + a;
       const float bp = s - hi[q];
-      lo[q] += (hi[q] - (s - bp)) + (acc[q] - bp);
+      lo[q] += (hi[q] - (s - bp)) + (a - bp);
       hi[q] = s;
-      acc[q] = 0.f;
+      acc[q] = dup2(0.f);
     }
   };
   int acc_shot = -1;
@@ -865,13 +941,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         pvy = pv[q2][1];
       }
       float vx[4], vy[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        float lx, ly;
-        apply(ks, st, q, lx, ly);
-        vx[q] = (2.f * c1x[q] - g4(pvx, q)) + lx;
-        vy[q] = (2.f * c1y[q] - g4(pvy, q)) + ly;
-      }
+      leap4<false>(ks, st, c1x, c1y, pvx, pvy, pvx, vx, vy);
       if (in) {
         if (a.frame >= 0 && a.record == kRecordFields) {
           const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * N + o;
@@ -891,14 +961,16 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
         const float4 u4x = *reinterpret_cast<const float4*>(ub + r * kTY + j);
         const float4 u4y = *reinterpret_cast<const float4*>(ub + L::kTR * kTY + r * kTY + j);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {  // each sum as a chain of fused multiply-adds
-          const float ux = g4(u4x, q), uy = g4(u4y, q);
-          acc[0] = fmaf(ux, st.xx_x[q], acc[0]);
-          acc[1] = fmaf(uy, st.yy_y[q], acc[1]);
-          acc[2] = fmaf(ux, st.xy_y[q], fmaf(uy, st.xy_x[q], acc[2]));
-          acc[3] = fmaf(uy, st.xx_x[q], fmaf(ux, fmaf(0.5f, st.xy_x[q], st.xx_y[q]), acc[3]));
-          acc[4] = fmaf(ux, st.yy_y[q], fmaf(uy, fmaf(0.5f, st.xy_y[q], st.yy_x[q]), acc[4]));
-          acc[5] = fmaf(uy, st.xx_y[q], fmaf(ux, st.yy_x[q], acc[5]));
+        for (int p = 0; p < 2; ++p) {  // each sum as a chain of fused multiply-adds, two cells per op
+          const float2 ux = pair4(u4x, p), uy = pair4(u4y, p);
+          const float2 xx_x = pair(st.xx_x, p), yy_x = pair(st.yy_x, p), xy_x = pair(st.xy_x, p);
+          const float2 xx_y = pair(st.xx_y, p), yy_y = pair(st.yy_y, p), xy_y = pair(st.xy_y, p);
+          acc[0] = fma2(ux, xx_x, acc[0]);
+          acc[1] = fma2(uy, yy_y, acc[1]);
+          acc[2] = fma2(ux, xy_y, fma2(uy, xy_x, acc[2]));
+          acc[3] = fma2(uy, xx_x, fma2(ux, fma2(dup2(0.5f), xy_x, xx_y), acc[3]));
+          acc[4] = fma2(ux, yy_y, fma2(uy, fma2(dup2(0.5f), xy_y, yy_x), acc[4]));
+          acc[5] = fma2(uy, xx_y, fma2(ux, yy_x, acc[5]));
         }
       }
       if (MODE == kModeDField && has_u) {
@@ -924,7 +996,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       shift(wx);
       shift(wy);
     }
-    if (MODE == kModeScalar && (k & 1)) fold();
+    if (MODE == kModeScalar && (k & 3) == 3) fold();
     if (MODE == kModeDField && tile_inject) {
       // adjoint source at receiver cells, added to the stored lam^m (several
       // receivers may share a cell); the block's own stores are visible
