@@ -159,10 +159,11 @@ struct Quad {
 };
 
 // Packed FP32 (sm_100 family): one instruction for two cells of a quad, each
-// lane rounded as the scalar operation.  The step loop is issue bound; sums
-// whose operands are column neighbours (not register pairs of the window)
-// are formed by scalar adds first, so every value keeps the association and
-// rounding of the scalar formulas.
+// lane rounded as the scalar operation; it shortens every row of the step
+// loop, whose per-step chain sets the time.  Sums whose operands are column
+// neighbours (not register pairs of the window) are formed by scalar adds
+// first, so every value keeps the association and rounding of the scalar
+// formulas.
 __device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 pair(const float v[4], int p) { return make_float2(v[2 * p], v[2 * p + 1]); }
 __device__ __forceinline__ float2 pair4(const float4& v, int p) {

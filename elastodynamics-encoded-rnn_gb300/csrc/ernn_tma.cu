@@ -140,11 +140,11 @@ __device__ __forceinline__ void win(const float* __restrict__ box, int r, int j,
 }
 
 // Packed FP32 (sm_100 family): one instruction applies the same operation to
-// two cells of a quad, each lane rounded as the scalar operation would be.
-// The kernels are issue bound, so halving the arithmetic instructions is
-// what counts.  Sums whose operands are column neighbours (not register
-// pairs of the window) are formed by scalar adds first, so every value keeps
-// the association and rounding of the scalar formulas.
+// two cells of a quad, each lane rounded as the scalar operation would be,
+// which halves the arithmetic instructions of a quad.  Sums whose operands
+// are column neighbours (not register pairs of the window) are formed by
+// scalar adds first, so every value keeps the association and rounding of
+// the scalar formulas.
 __device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 pair(const float v[4], int p) { return make_float2(v[2 * p], v[2 * p + 1]); }
 __device__ __forceinline__ float2 pair4(const float4& v, int p) {
