@@ -790,7 +790,24 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
         }
       }
     };
-    if (!DENSE && next_src >= a.m_lo + 1) load_g(next_src);
+    // The residuals of every frame of this launch, gathered once into the
+    // load area F (unused by this role): entry (frame - f_lo) * nloc + e, x
+    // and y interleaved.  The per-step injection then reads shared memory
+    // only; when they do not fit, each step loads the next frame's residuals.
+    const int f_lo = (a.m_lo + c.stride - 1) / c.stride;  // frames f: f * stride in [m_lo, m_hi - 1]
+    const int nfr = a.m_hi >= a.m_lo + 1 ? (a.m_hi - 1) / c.stride - f_lo + 1 : 0;
+    const bool staged = !DENSE && nloc > 0 && nfr > 0 && (long long)nfr * nloc * 2 <= (long long)R * ny;
+    if (staged) {
+      for (int idx = tid; idx < nfr * nloc; idx += kResThreads) {
+        const int fr = idx / nloc, e = idx - fr * nloc;
+        const size_t go = ((size_t)shot * c.nt_out + f_lo + fr) * c.nrec + rec_list[2 * e + 1];
+        F[2 * idx] = a.g_x[go];
+        F[2 * idx + 1] = a.g_y[go];
+      }
+      __syncthreads();
+    } else if (!DENSE && next_src >= a.m_lo + 1) {
+      load_g(next_src);
+    }
     // lam^{m_hi+1} is the imaging partner of u^{m_hi}: store it first
     if (tid == 0 && a.lbuf && a.store_init) {
       fence_proxy_async();
@@ -816,12 +833,15 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
           const int e = tid + h * kResThreads;
           if (e < nloc) {
             const int off = rec_list[2 * e];
-            atomicAdd(&T.comp(const_cast<float*>(x.prev), 0)[off], -gs * gnx[h]);
-            atomicAdd(&T.comp(const_cast<float*>(x.prev), 1)[off], -gs * gny[h]);
+            const int si = (frame - f_lo) * nloc + e;
+            const float vx = staged ? F[2 * si] : gnx[h];
+            const float vy = staged ? F[2 * si + 1] : gny[h];
+            atomicAdd(&T.comp(const_cast<float*>(x.prev), 0)[off], -gs * vx);
+            atomicAdd(&T.comp(const_cast<float*>(x.prev), 1)[off], -gs * vy);
           }
         }
         next_src = m - c.stride;
-        if (next_src >= a.m_lo + 1) load_g(next_src);
+        if (!staged && next_src >= a.m_lo + 1) load_g(next_src);
         __syncthreads();
       }
       rhs.gx = nullptr;
