@@ -772,7 +772,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     // ================================================================ LAM role
     const float gs = c.coef->gscale;  // one scale for every shot
     // residuals of the receivers this thread injects (entries tid + h * kResThreads),
-    // loaded one recording step ahead
+    // loaded one recording step ahead when the launch's frames are not staged
+    // in shared memory (below)
     constexpr int kRecPerThread = (kResMaxRec + kResThreads - 1) / kResThreads;
     float gnx[kRecPerThread], gny[kRecPerThread];
 #pragma unroll
