@@ -36,6 +36,8 @@ import numpy as np  # noqa: E402
 import torch  # noqa: E402
 
 L2_BYTES = 129 * 1024 * 1024
+# the CPU baseline times the whole iteration up to this many cell-steps
+CPU_FULL_CELL_STEPS = 2.0e8
 FLUSH_BYTES = 256 * 1024 * 1024
 
 
@@ -49,8 +51,8 @@ def parse(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ernn", "reference"], default="ernn")
     ap.add_argument("--workload", default="rot256")
-    ap.add_argument("--cpu-sample-steps", type=int, default=100,
-                    help="time steps of the bounded CPU sample")
+    ap.add_argument("--cpu-sample-steps", type=int, default=200,
+                    help="time steps of the bounded CPU sample (reference arm steps; larger workloads)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nt", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--ckpt", type=int, default=None, help="override the checkpoint interval")
@@ -198,34 +200,61 @@ def _cpu_model() -> str:
     return "unknown"
 
 
+_STANDALONE = {}
+
+
+def standalone(name):
+    """Load <package>/<name>.py (configs, sources: numpy / torch only) by file
+    path, without importing the package, so the reference arm's process never
+    maps libernn_gb300.so."""
+    if name not in _STANDALONE:
+        import importlib.util
+        path = os.path.join(ROOT, "elastodynamics-encoded-rnn_gb300", name + ".py")
+        spec = importlib.util.spec_from_file_location("ernn_standalone_" + name, path)
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[spec.name] = mod  # dataclasses resolve annotations through sys.modules
+        spec.loader.exec_module(mod)
+        _STANDALONE[name] = mod
+    return _STANDALONE[name]
+
+
+def library_mapped():
+    """Whether this process has mapped libernn_gb300.so (Linux /proc maps)."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libernn_gb300" in line for line in f)
+    except OSError:
+        return None
+
+
 def cpu_sample(workload, nt_sample, iters=2):
     """The reference path (PyTorch restatement, autograd) on the host cores:
     forward (receiver traces) -> misfit -> backward -> Adam, truncated to
     nt_sample steps of the same grid.  Returns (Gcell-steps/s, threads, sample)."""
-    import ernn_gb300.harness as Hn
+    Wk, Src = standalone("configs"), standalone("sources")
     from oracle import torch_ref
 
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    w = Hn.WORKLOADS[workload]()
+    w = Wk.WORKLOADS[workload]()
     dev = torch.device("cpu")
     if w.extra.get("fields"):
         t = fields_reference_iteration(w, nt_sample, dev, iters)
         return (w.nx * w.ny * nt_sample / t / 1e9, threads,
                 f"{workload} grid, {nt_sample} of {w.nt} steps, six constant fields, best of {iters}")
-    sig = torch.tensor(Hn.sources.hann_burst_signal(nt_sample, Hn.DT, w.f0, 5, w.amplitude),
+    sig = torch.tensor(Src.hann_burst_signal(nt_sample, Wk.DT, w.f0, 5, w.amplitude),
                        dtype=torch.float32)[None].repeat(w.nshots, 1)
-    pos = [Hn.sources.cell_position(i, j, w.nx, w.ny, Hn.H) for (i, j) in w.src_cells]
-    load = Hn.sources.point_load_maps(w.nx, w.ny, Hn.H, pos, w.gaussian_param, device=dev)
+    pos = [Src.cell_position(i, j, w.nx, w.ny, Wk.H) for (i, j) in w.src_cells]
+    load = Src.point_load_maps(w.nx, w.ny, Wk.H, pos, w.gaussian_param, device=dev)
     rec = torch.tensor([[i * w.ny + j for (i, j) in w.rec_cells]] * w.nshots, dtype=torch.int32)
-    rho = torch.tensor(Hn.RHO)
-    theta = torch.nn.Parameter(torch.tensor(Hn.initial_guess(w) / Hn.scales(w.C_true), dtype=torch.float32))
-    sc = torch.tensor(Hn.scales(w.C_true), dtype=torch.float32)
+    rho = torch.tensor(Wk.RHO)
+    theta = torch.nn.Parameter(torch.tensor(Wk.initial_guess(w) / Wk.scales(w.C_true), dtype=torch.float32))
+    sc = torch.tensor(Wk.scales(w.C_true), dtype=torch.float32)
     opt = torch.optim.Adam([theta], lr=1e-2)
     with torch.no_grad():  # the observations: also the forward-only timing
         Ct = [torch.tensor(float(c)) for c in w.C_true]
         t0 = time.perf_counter()
-        ox, oy = torch_ref.propagate(Ct, rho, w.nx, w.ny, nt_sample, Hn.H, Hn.DT, sig, load, 1, rec)
+        ox, oy = torch_ref.propagate(Ct, rho, w.nx, w.ny, nt_sample, Wk.H, Wk.DT, sig, load, 1, rec)
         t_fwd = time.perf_counter() - t0
     _CPU_EXTRA["forward_only"] = round(w.nshots * w.nx * w.ny * nt_sample / t_fwd / 1e9, 6)
     _CPU_EXTRA["cpu_model"] = _cpu_model()
@@ -234,8 +263,8 @@ def cpu_sample(workload, nt_sample, iters=2):
         t0 = time.perf_counter()
         opt.zero_grad()
         C = theta * sc
-        px, py = torch_ref.propagate([C[i] for i in range(6)], rho, w.nx, w.ny, nt_sample, Hn.H,
-                                     Hn.DT, sig, load, 1, rec)
+        px, py = torch_ref.propagate([C[i] for i in range(6)], rho, w.nx, w.ny, nt_sample, Wk.H,
+                                     Wk.DT, sig, load, 1, rec)
         loss = ((px.double() - ox.double()) ** 2).mean() + ((py.double() - oy.double()) ** 2).mean()
         loss.backward()
         opt.step()
@@ -250,10 +279,9 @@ def fields_reference_iteration(w, nt, dev, iters):
     per-cell constant fields, autograd): forward with dense history every
     `stride` steps, 5:1 misfit on every 2nd frame + TV, backward, Adam.
     Returns the best time of `iters` iterations in seconds."""
-    import ernn_gb300.harness as Hn
-    from ernn_gb300 import sources as Src
+    Src = standalone("sources")
     from oracle import torch_ref
-    c = Hn.FIELDS301
+    c = standalone("configs").FIELDS301
     h = c["L"] / (w.nx - 1)
     dt = c["total_time"] / (c["nt"] - 1)
     X, Y = Src.centered_grid(w.nx, w.ny, h, device=dev)
@@ -463,9 +491,14 @@ def run_ernn(args, dist):
         "loss": float((pre(), inv.step())[1].item()),
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        v, thr, sample = cpu_sample(args.workload, args.cpu_sample_steps)
+        # the whole iteration when it is about 20 s of host work or less
+        # (rot256, plate128), else a bounded sample of its steps
+        full = w.cell_steps <= CPU_FULL_CELL_STEPS and not w.extra.get("fields")
+        v, thr, sample = cpu_sample(args.workload, w.nt if full else args.cpu_sample_steps,
+                                    iters=1 if full else 2)
         rec["cpu_baseline"] = {"value": round(v, 6), "unit": "Gcell-steps/s", "cores": thr,
-                               "kind": "port", "sample": sample + " (PyTorch restatement of the reference path, autograd)",
+                               "kind": "port", "same_config": full,
+                               "sample": sample + " (PyTorch restatement of the reference path, autograd)",
                                **_CPU_EXTRA}
     return rec
 
@@ -734,8 +767,7 @@ def run_reference(args, dist):
         return None
     if args.workload in ("fem301", "multi64"):
         return run_reference_other(args)
-    import ernn_gb300.harness as Hn
-    w = Hn.WORKLOADS[args.workload]()
+    w = standalone("configs").WORKLOADS[args.workload]()
     nts = args.cpu_sample_steps
     for _ in range(max(args.warmup, 0)):
         cpu_sample(args.workload, min(nts, 20), iters=1)
@@ -756,7 +788,9 @@ def run_reference(args, dist):
         "config": {"workload": f"{w.name}: {w.nx}x{w.ny} grid, {w.nt} steps (sampled {nts}), "
                                f"{w.nshots} shot(s), {len(w.rec_cells)} receivers"},
         "cpu_baseline": {"value": round(value, 6), "unit": "Gcell-steps/s", "cores": thr,
-                         "kind": "port", "sample": sample, **_CPU_EXTRA},
+                         "kind": "port", "same_config": nts >= w.nt,
+                         "sample": sample + " (PyTorch restatement of the reference path, autograd)",
+                         **_CPU_EXTRA},
         "e2e": {"value": round(value, 6), "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -767,6 +801,9 @@ def run_reference(args, dist):
                                    "value": round(w.nx * w.ny * w.nt / t / 1e9, 5), "unit": "Gcell-steps/s"}
         else:
             rec["gpu_autograd"] = gpu_autograd(args, w)
+    # evidence that this arm ran nothing of the library: its process never
+    # mapped libernn_gb300.so
+    rec["native_library_mapped"] = library_mapped()
     return rec
 
 
@@ -810,26 +847,26 @@ def run_reference_other(args):
 def gpu_autograd(args, w, iters=3):
     """The same restated reference path on the GPU with autograd (the reference's
     plain form on the same device), full workload."""
-    import ernn_gb300.harness as Hn
+    Wk, Src = standalone("configs"), standalone("sources")
     from oracle import torch_ref
     dev = torch.device("cuda", 0)
-    sig = torch.tensor(Hn.sources.hann_burst_signal(w.nt, Hn.DT, w.f0, 5, w.amplitude),
+    sig = torch.tensor(Src.hann_burst_signal(w.nt, Wk.DT, w.f0, 5, w.amplitude),
                        dtype=torch.float32, device=dev)[None].repeat(w.nshots, 1)
-    pos = [Hn.sources.cell_position(i, j, w.nx, w.ny, Hn.H) for (i, j) in w.src_cells]
-    load = Hn.sources.point_load_maps(w.nx, w.ny, Hn.H, pos, w.gaussian_param, device=dev)
+    pos = [Src.cell_position(i, j, w.nx, w.ny, Wk.H) for (i, j) in w.src_cells]
+    load = Src.point_load_maps(w.nx, w.ny, Wk.H, pos, w.gaussian_param, device=dev)
     rec = torch.tensor([[i * w.ny + j for (i, j) in w.rec_cells]] * w.nshots, dtype=torch.int32, device=dev)
-    rho = torch.tensor(Hn.RHO, device=dev)
+    rho = torch.tensor(Wk.RHO, device=dev)
     with torch.no_grad():
         Ct = [torch.tensor(float(c), device=dev) for c in w.C_true]
-        ox, oy = torch_ref.propagate(Ct, rho, w.nx, w.ny, w.nt, Hn.H, Hn.DT, sig, load, 1, rec)
-    theta = torch.nn.Parameter(torch.tensor(Hn.initial_guess(w) / Hn.scales(w.C_true), dtype=torch.float32, device=dev))
-    sc = torch.tensor(Hn.scales(w.C_true), dtype=torch.float32, device=dev)
+        ox, oy = torch_ref.propagate(Ct, rho, w.nx, w.ny, w.nt, Wk.H, Wk.DT, sig, load, 1, rec)
+    theta = torch.nn.Parameter(torch.tensor(Wk.initial_guess(w) / Wk.scales(w.C_true), dtype=torch.float32, device=dev))
+    sc = torch.tensor(Wk.scales(w.C_true), dtype=torch.float32, device=dev)
     opt = torch.optim.Adam([theta], lr=1e-2)
 
     def it():
         opt.zero_grad()
         C = theta * sc
-        px, py = torch_ref.propagate([C[i] for i in range(6)], rho, w.nx, w.ny, w.nt, Hn.H, Hn.DT,
+        px, py = torch_ref.propagate([C[i] for i in range(6)], rho, w.nx, w.ny, w.nt, Wk.H, Wk.DT,
                                      sig, load, 1, rec)
         loss = ((px.double() - ox.double()) ** 2).mean() + ((py.double() - oy.double()) ** 2).mean()
         loss.backward()

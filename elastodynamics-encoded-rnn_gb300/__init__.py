@@ -12,11 +12,11 @@ Public surface:
       one application of the operator;
   series_misfit, parameter_loss, damage_loss
       the inverters' objectives as fused device passes (loss and adjoint source);
-  sources, materials, harness
+  sources, materials, configs, harness
       source signals and loads, in-plane rotation and stability, benchmark
-      configurations.
+      configurations (numpy only) and the inversion iteration built on them.
 """
-from . import _lib, autotune, fem, formats, materials, misfit, sources
+from . import _lib, autotune, configs, fem, formats, materials, misfit, sources
 from ._lib import PATH_AUTO, PATH_RESIDENT, PATH_STEP, PATH_TILED
 from .propagate import (MODE_DFIELD, MODE_FIELDS, MODE_SCALAR, RECORD_FIELDS,
                         RECORD_RECEIVERS, ErnnPropagate, Geometry, check_device_status,
@@ -30,7 +30,7 @@ __all__ = [
     "CFRPWaveSimulatorRicker", "SpatiallyVaryingAnisotropicSimulator", "ShotGatherSimulator",
     "DegradationSimulator", "damage_loss", "parameter_loss", "series_misfit",
     "total_variation_2d", "ErnnPropagate", "Geometry", "propagate", "elastic_operator_with_force",
-    "sources", "materials", "formats", "fem", "autotune", "misfit", "MODE_SCALAR", "MODE_DFIELD",
+    "sources", "materials", "configs", "formats", "fem", "autotune", "misfit", "MODE_SCALAR", "MODE_DFIELD",
     "MODE_FIELDS", "RECORD_FIELDS", "RECORD_RECEIVERS", "PATH_AUTO", "PATH_STEP",
     "PATH_RESIDENT", "PATH_TILED", "check_device_status", "load_library",
 ]

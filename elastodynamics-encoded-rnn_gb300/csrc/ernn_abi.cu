@@ -280,6 +280,9 @@ int resident_adjoint(const ErnnProblem& p, const Plan& pl, ResCommon& rc, const 
 }
 
 }  // namespace
+
+void record_last_path(int32_t path) { g_last_path.store(path, std::memory_order_relaxed); }
+
 }  // namespace ernn
 
 using namespace ernn;

@@ -138,6 +138,10 @@ cudaError_t tracked_launch(int cls, cudaStream_t st, const std::function<void()>
 inline double alg_bytes_forward(int mode) {
   return 24.0 + (mode == kModeDField ? 4.0 : mode == kModeFields ? 24.0 : 0.0);
 }
+// Record which kernels ran the time loop of the latest propagation call
+// (ernn_last_path).
+void record_last_path(int32_t path);
+
 inline double alg_bytes_adjoint(int mode) {
   return 32.0 + (mode == kModeDField ? 4.0 + 8.0 : mode == kModeFields ? 24.0 + 48.0 : 0.0);
 }

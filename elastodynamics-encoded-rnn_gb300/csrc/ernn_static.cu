@@ -69,6 +69,9 @@ extern "C" int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, f
   if ((size_t)p->src_bx * p->src_by > 0 && (in->src_map == nullptr || in->src_origin == nullptr))
     return ERNN_ERR_INVALID;
   if (p->record == kRecordReceivers && in->rec_idx == nullptr) return ERNN_ERR_INVALID;
+  // the per-step kernels are the only ones this entry runs: an explicit
+  // request for the resident or tiled kernels cannot be served
+  if (p->path != ERNN_PATH_AUTO && p->path != ERNN_PATH_STEP) return ERNN_ERR_UNSUPPORTED;
   // coefficient block(s), then two state levels of nshots x 2 x nx x ny floats
   const size_t N = (size_t)p->nx * p->ny;
   const size_t state_bytes = align_static((size_t)p->nshots * 2 * N * sizeof(float));
@@ -83,6 +86,7 @@ extern "C" int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, f
   float* A = reinterpret_cast<float*>(b + coef_bytes);
   float* B = reinterpret_cast<float*>(b + coef_bytes + state_bytes);
   cudaStream_t st = (cudaStream_t)stream;
+  record_last_path(ERNN_PATH_STEP);
   if (launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st, ncoef) != cudaSuccess) return ERNN_ERR_CUDA;
 
   const int nt_out = (p->nt + p->stride - 1) / p->stride;

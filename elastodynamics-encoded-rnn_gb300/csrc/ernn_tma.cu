@@ -79,6 +79,58 @@ __device__ __forceinline__ void bar_wait(uint64_t* b, uint32_t parity, int* err)
   }
 }
 
+// Error path of a tile pipeline.  A wait that gives up (its own time limit,
+// or an error another CTA of the launch already recorded) marks the CTA
+// failed: from then on no further tile loads are issued (the launch's
+// outputs are invalid anyway), and before the CTA exits one thread waits,
+// again with a time limit, for the loads it had already issued, so no copy
+// is still writing into the shared memory of a CTA that has ended.
+struct PipeGuard {
+  int failed;  // a wait of this CTA gave up
+  int issued;  // tiles 0 .. issued-1 of this CTA had their loads issued
+};
+
+__device__ __forceinline__ void pipe_init(PipeGuard* g) {
+  g->failed = 0;
+  g->issued = 0;
+}
+__device__ __forceinline__ bool pipe_failed(const PipeGuard* g) {
+  return *reinterpret_cast<const volatile int*>(&g->failed) != 0;
+}
+__device__ __forceinline__ void pipe_issued(PipeGuard* g, int k) { atomicMax(&g->issued, k + 1); }
+
+// bar_wait that reports whether the phase completed (false: timed out, or an
+// error of the launch was already recorded); a false marks the CTA failed
+__device__ __forceinline__ bool bar_wait_ok(uint64_t* b, uint32_t parity, int* err, PipeGuard* g) {
+  if (bar_try(b, parity)) return true;
+  if (*(volatile int*)err == 0) {
+    const long long t0 = clock64();
+    for (;;) {
+      for (int k = 0; k < 64; ++k)
+        if (bar_try(b, parity)) return true;
+      if (clock64() - t0 > kWaitLimitCycles) {
+        atomicExch(err, kDeviceTimeout);
+        break;
+      }
+    }
+  }
+  *reinterpret_cast<volatile int*>(&g->failed) = 1;
+  __threadfence_block();
+  return false;
+}
+
+// After a failed CTA's tile loop (one thread): wait, each with a time limit,
+// for the phases of the last `ns` issued tiles (tile k: stage k % ns, phase
+// parity (k / ns) & 1).  A phase that already completed returns at once.
+__device__ __forceinline__ void pipe_drain(uint64_t* bar, int ns, const PipeGuard* g) {
+  const int issued = *reinterpret_cast<const volatile int*>(&g->issued);
+  for (int k = issued - ns < 0 ? 0 : issued - ns; k < issued; ++k) {
+    const long long t0 = clock64();
+    while (!bar_try(&bar[k % ns], (uint32_t)(k / ns) & 1u))
+      if (clock64() - t0 > kWaitLimitCycles) break;
+  }
+}
+
 // 3D tile load (columns, rows, component planes) into shared memory.
 __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
                                           uint64_t* b) {
@@ -353,12 +405,14 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   const uint32_t bytes = (uint32_t)(F::kHalo + (has_prev ? F::kOwn : 0)) * 4u;
   grid_dep_trigger();
   __shared__ int done[2];
+  __shared__ PipeGuard guard;
   if (tid == 0) {
     prefetch_map(&cur_map);
     prefetch_map(&prev_map);
     bar_init(&bar[0]);
     bar_init(&bar[1]);
     done[0] = done[1] = 0;
+    pipe_init(&guard);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   grid_dep_wait();  // the state of the previous step is complete from here on
@@ -378,7 +432,8 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   const bool has_src = a.bx > 0 && a.by > 0;
   auto issue = [&](int k) {  // loads of this CTA's k-th tile into stage k & 1
     const int t = blockIdx.x + k * gridDim.x;
-    if (t >= ntiles) return;
+    if (t >= ntiles || pipe_failed(&guard)) return;
+    pipe_issued(&guard, k);
     const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * kStage;
     fence_async();
@@ -418,7 +473,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
                      : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
-    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
+    bar_wait_ok(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err, &guard);
     const float* hb = sm + (k & 1) * kStage;
     const float* pb = hb + F::kHalo;
     float* out = a.out + (size_t)id.shot * 2 * N;
@@ -481,6 +536,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
     }
     release(done, k, [&] { issue(k + 2); });
   }
+  if (tid == 0 && pipe_failed(&guard)) pipe_drain(bar, 2, &guard);
 }
 
 // ------------------------------------------------------- two-step forward
@@ -543,12 +599,14 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   const uint32_t bytes = (uint32_t)(F::kCur + (has_prev ? F::kPrev : 0)) * 4u;
   grid_dep_trigger();
   __shared__ int done[2];
+  __shared__ PipeGuard guard;
   if (tid == 0) {
     prefetch_map(&cur_map);
     prefetch_map(&prev_map);
     bar_init(&bar[0]);
     bar_init(&bar[1]);
     done[0] = done[1] = 0;
+    pipe_init(&guard);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -556,7 +614,8 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   const bool has_src = a.bx > 0 && a.by > 0;
   auto issue = [&](int k) {  // loads of this CTA's k-th tile into stage k & 1
     const int t = blockIdx.x + k * gridDim.x;
-    if (t >= ntiles) return;
+    if (t >= ntiles || pipe_failed(&guard)) return;
+    pipe_issued(&guard, k);
     const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * F::kStage;
     fence_async();
@@ -584,7 +643,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     const float amp1 = sig[a.i] * K->kappa, amp2 = sig[a.i + 1] * K->kappa;
     const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
     const float* smap = has_src ? a.src_map + (size_t)id.shot * a.bx * a.by : nullptr;
-    bar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err);
+    bar_wait_ok(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err, &guard);
     const float* cb = sm + (k & 1) * F::kStage;           // u^i: rows -2 .. kTR+1
     const float* pb = cb + F::kCur;                        // u^{i-1}: rows -1 .. kTR
     float* mid = sm + 2 * F::kStage + (k & 1) * F::kMid;  // u^{i+1}: rows -1 .. kTR
@@ -683,6 +742,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     }
     release(done, k, [&] { issue(k + 2); });
   }
+  if (tid == 0 && pipe_failed(&guard)) pipe_drain(bar, 2, &guard);
 }
 
 // ----------------------------------------------------------------- adjoint
@@ -740,6 +800,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
                                         : L::kHalo + L::kBHa * kBW + (has_u ? L::kHalo : 0)) * 4u;
   grid_dep_trigger();
   __shared__ int done[NS];
+  __shared__ PipeGuard guard;
   if (tid == 0) {
     prefetch_map(&cur_map);
     prefetch_map(MODE == kModeScalar ? &prev_map : &d_map);
@@ -748,6 +809,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       bar_init(&bar[q]);
       done[q] = 0;
     }
+    pipe_init(&guard);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -765,7 +827,8 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   const int t_step = chunked ? 1 : (int)gridDim.x;
   auto issue = [&](int k) {
     const int t = t_first + k * t_step;
-    if (t >= t_end) return;
+    if (t >= t_end || pipe_failed(&guard)) return;
+    pipe_issued(&guard, k);
     const TileId id = tile_of<L::kTR>(t, tiles_x, tiles_y);
     const int sg = k % NS;
     float* st = sm + sg * L::kStage;
@@ -859,7 +922,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       }
     }
     const int stage = k % NS;
-    bar_wait(&bar[stage], (uint32_t)(k / NS) & 1u, err);
+    bar_wait_ok(&bar[stage], (uint32_t)(k / NS) & 1u, err, &guard);
     float* hb = sm + stage * L::kStage;
     float* pb = hb + L::kPrev;
     const float* ub = hb + L::kU;
@@ -1015,6 +1078,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     }
     release_stage(done, stage, [&] { issue(k + NS); });
   }
+  if (tid == 0 && pipe_failed(&guard)) pipe_drain(bar, NS, &guard);
   if (MODE != kModeScalar || !has_u) return;
   flush(per_shot ? acc_shot : 0);
 }

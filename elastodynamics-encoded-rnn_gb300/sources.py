@@ -102,13 +102,6 @@ def hann_burst_signal(nt, dt, f0=1e6, cycles=5, amplitude=1.0):
     return tone_burst(signal_times(nt, dt), f0, cycles, amplitude)
 
 
-def top_edge_positions(n, nx, margin=0):
-    """n cell indices along x evenly spaced on [margin, nx-1-margin]."""
-    if n == 1:
-        return [nx // 2]
-    return [int(round(v)) for v in np.linspace(margin, nx - 1 - margin, n)]
-
-
 def courant_number(c_max, rho, h, dt):
     """v_p dt / h with v_p = sqrt(c_max / rho)."""
     return math.sqrt(c_max / rho) * dt / h

@@ -63,8 +63,10 @@ enum {
                              distributed shared memory for all steps (scalar constants,
                              ny % 4 == 0, state small enough); ERNN_ERR_UNSUPPORTED otherwise */
   ERNN_PATH_TILED = 3     /* one launch per time step of persistent CTAs that stream
-                             64 x 32 tiles through TMA loads (scalar constants,
-                             ny % 4 == 0); ERNN_ERR_UNSUPPORTED otherwise */
+                             64-column tiles (16 rows; 32 for the degradation-map
+                             adjoint) through TMA loads (scalar constants or a
+                             degradation map, ny % 4 == 0); ERNN_ERR_UNSUPPORTED
+                             otherwise */
 };
 
 /* Problem flags. */

@@ -1,7 +1,9 @@
 """Generate the golden vectors in tests/golden/ from the reference module itself.
 
-Run in a container that has the reference checked out (default path below, or
-pass it as the first argument).  The reference is imported unmodified:
+Run where the reference is checked out, giving its location as the first
+argument or in the ERNN_REFERENCE environment variable:
+  python tests/golden/make_golden.py <reference checkout>
+The reference is imported unmodified:
   * Parameter_inversion/Inversion_adam.py is imported as a module with stub
     modules for matplotlib and h5py (absent here, unused on this path);
   * Parameter_inversion/FEM_generate_data.py likewise (its solver runs on the
@@ -27,7 +29,9 @@ from unittest import mock
 import numpy as np
 import torch
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ERNN_REFERENCE")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: make_golden.py <reference checkout>  (or set ERNN_REFERENCE)")
 OUT = os.path.dirname(os.path.abspath(__file__))
 sys.dont_write_bytecode = True
 

@@ -96,6 +96,38 @@ def test_stability_check():
     assert abs(E.materials.check_stability(one, 1.0, 1.0, 0.5) - 0.25) < 1e-12
 
 
+def test_numpy_stability_number_equals_the_library_check():
+    # the benchmark's reference arm draws its initial guesses with the numpy
+    # restatement (it must not load the library): both must accept and reject
+    # the same materials
+    rng = np.random.default_rng(5)
+    base = E.materials.rotate(E.materials.orthotropic_xz(130e9, 12e9, 6e9, 5.5e9), 30.0)
+    for k in range(40):
+        c = base * rng.uniform(0.5, 1.5, size=6)
+        dt = rng.choice([5e-9, 9e-9, 14e-9])
+        number, indefinite = E.configs.stability_number(c, 1560.0, 1e-4, dt)
+        try:
+            v = E.materials.check_stability(c, 1560.0, 1e-4, dt)
+            assert not indefinite and number <= 1.0
+            assert abs(v - number) <= 1e-12 * v
+        except ValueError:
+            assert indefinite or number > 1.0
+
+
+def test_reference_arm_loads_no_library():
+    # bench.py's reference arm builds its workload from the numpy-only
+    # configurations, loaded by file path in a fresh process
+    import subprocess
+    import sys
+    code = ("import bench; w = bench.standalone('configs').rot256(); "
+            "g = bench.standalone('configs').initial_guess(w); bench.standalone('sources'); "
+            "print(bench.library_mapped(), len(g))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(os.path.dirname(__file__)),
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == ["False", "6"]
+
+
 def test_rotation_properties():
     c = E.materials.orthotropic_xz(130e9, 12e9, 6e9, 5.5e9)
     assert np.allclose(E.materials.rotate(c, 0), c)

@@ -110,9 +110,10 @@ def test_resident_path_vs_fp64_oracle(name):
     assert rel(gg, rg) <= GRAD_TOL, rel(gg, rg)
 
 
-# scalar-constant cases with ny % 4 == 0 on the tiled (TMA) per-step kernels:
-# tiles of 64 columns x 32 rows, ragged edges in both directions, tile
-# boundaries through the source box and through receiver cells
+# cases with ny % 4 == 0 on the tiled (TMA) per-step kernels: tiles of 64
+# columns x 16 rows (32 rows in the degradation-map adjoint), ragged edges in
+# both directions, tile boundaries through the source box and through
+# receiver cells
 TILED_CASES = {
     "dense_ragged": dict(nx=45, ny=76),
     "receivers_multishot": dict(nx=70, ny=132, record=O.RECORD_RECEIVERS, S=3, nrec=40),
