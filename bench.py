@@ -36,6 +36,7 @@ import numpy as np  # noqa: E402
 import torch  # noqa: E402
 
 L2_BYTES = 129 * 1024 * 1024
+H_STEP, DT_STEP = 1e-4, 5e-9  # grid spacing and time step of every benchmark workload
 # the CPU baseline times the whole iteration up to this many cell-steps
 CPU_FULL_CELL_STEPS = 2.0e8
 FLUSH_BYTES = 256 * 1024 * 1024
@@ -54,6 +55,8 @@ def parse(argv=None):
     ap.add_argument("--cpu-sample-steps", type=int, default=200,
                     help="time steps of the bounded CPU sample (reference arm steps; larger workloads)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--err-instances", type=int, default=16,
+                    help="multi64: instances whose gradient is checked against the FP64 oracle")
     ap.add_argument("--nt", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--ckpt", type=int, default=None, help="override the checkpoint interval")
     ap.add_argument("--path", choices=list(PATHS), default="auto",
@@ -62,6 +65,9 @@ def parse(argv=None):
                     help="launch every iteration from the host instead of replaying a CUDA graph")
     ap.add_argument("--no-overlap", action="store_true",
                     help="launch consecutive step kernels without programmatic dependent launch")
+    ap.add_argument("--grouped", action="store_true",
+                    help="multi64: the instances grouped by size, one call per group on 8 streams, "
+                         "instead of one canvas with a tile table")
     ap.add_argument("--plain", action="store_true",
                     help="only run warmup + steps iterations (no timing, no JSON): a profiling target")
     return ap.parse_args(argv)
@@ -500,7 +506,34 @@ def run_ernn(args, dist):
                                "kind": "port", "same_config": full,
                                "sample": sample + " (PyTorch restatement of the reference path, autograd)",
                                **_CPU_EXTRA}
+        rec["errors"] = config_errors(args, dev)
     return rec
+
+
+# the FP64 check of the benchmark line runs the whole workload up to this
+# many cell-steps (about 10 s of host work); larger ones keep their grids and
+# shots with fewer steps
+ERR_FULL_CELL_STEPS = 2.0e8
+ERR_SAMPLE_STEPS = 160
+
+
+def config_errors(args, dev):
+    """Forward-trace and gradient error of the benchmarked workload against
+    the FP64 run of the same scheme (oracle/accuracy.py, the checker): same
+    grid, shots, receivers, constants, checkpoint interval and kernel path."""
+    from oracle.accuracy import workload_errors
+    w = make_workload(args)
+    if w.extra.get("fields"):
+        return {"note": "not computed for the six-field workload (dense history, TV objective)"}
+    full = w.cell_steps <= ERR_FULL_CELL_STEPS
+    nt = None if full else min(w.nt, ERR_SAMPLE_STEPS)
+    ckpt = None if full else max(1, (nt or w.nt) // 8)
+    r = workload_errors(w, dev, nt=nt, ckpt_k=ckpt, path=w.path, fp32_floor=w.D_true is not None)
+    r["bound"] = 1e-4
+    r["scope"] = ("whole workload" if full else
+                  f"full grid and shots, {r['nt']} of {w.nt} steps, checkpoint every {r['ckpt_k']}")
+    r["against"] = "FP64 C oracle of the same scheme (checkpoint recompute), same observations"
+    return r
 
 
 def _dense_load(geom, dtype, device):
@@ -549,6 +582,55 @@ def multi_grad_errors(inv, max_side=128, count=3):
     return out
 
 
+def canvas_grad_errors(inv, dev, count=64):
+    """Per-instance trace and gradient error of the canvas iteration against
+    the FP64 C oracle (oracle/accuracy.py, the checker), every instance on
+    its own grid with its own steps, at the instances' current constants, for
+    the misfit of the canvas objective (S x mean over the padded traces) and
+    the same observations.  Instances are checked smallest first."""
+    from oracle import oracle as O
+    from oracle.accuracy import _rel
+    ws, S = inv.ws, len(inv.ws)
+    theta = inv.theta
+    theta.grad = None
+    with torch.enable_grad():
+        from ernn_gb300.propagate import propagate as _prop
+        from ernn_gb300.misfit import series_misfit
+        ux, uy = _prop(inv.params(), inv.rho, inv.geom)
+        series_misfit(ux, uy, inv.obs[0], inv.obs[1], float(S), float(S)).backward()
+    g32 = (theta.grad.detach().double() * inv.scale.double()).cpu().numpy()  # dL/dC
+    px32, py32 = ux.detach().double().cpu().numpy(), uy.detach().double().cpu().numpy()
+    C = inv.params().detach().cpu().numpy().astype(np.float64)
+    ox, oy = (o.detach().double().cpu().numpy() for o in inv.obs)
+    count_all = ox.size  # the canvas objective's mean counts the padded traces of all instances
+    sig = inv.geom.src_signal.detach().double().cpu().numpy()
+    smap = inv.geom.src_map.detach().double().cpu().numpy()
+    org = inv.geom.src_origin.detach().cpu().numpy()
+    rec = inv.geom.rec_idx.detach().cpu().numpy()
+    X, Y = inv.canvas
+    out, t0 = [], time.perf_counter()
+    for k in sorted(range(S), key=lambda k: ws[k].nx)[:count]:
+        w, nt = ws[k], inv.nts[k]
+        x0, y0 = inv.x0[k], inv.y0[k]
+        rk = ((rec[k] // Y - x0) * w.ny + (rec[k] % Y - y0)).astype(np.int32)
+        case = O.Case(w.nx, w.ny, nt, H_STEP, DT_STEP, float(inv.rho[k]), C[k].astype(np.float32).astype(np.float64),
+                      sig[k:k + 1, :nt], smap[k:k + 1], np.array([[org[k, 0] - x0, org[k, 1] - y0]], np.int32),
+                      record=O.RECORD_RECEIVERS, rec_idx=rk[None])
+        kk = max(1, int(round((2 * nt) ** 0.5)))
+        qx, qy, ck = O.forward_ckpt(case, kk, "f64")
+        gx = 2.0 * S * (qx - ox[k:k + 1, :nt]) / count_all
+        gy = 2.0 * S * (qy - oy[k:k + 1, :nt]) / count_all
+        gC, _ = O.adjoint_ckpt(case, kk, ck, gx, gy, "f64")
+        s = inv.scale[k].detach().double().cpu().numpy()
+        out.append({"instance": k, "side": w.nx, "nt": nt,
+                    "fwd_rel_err": round(max(_rel(px32[k:k + 1, :nt], qx), _rel(py32[k:k + 1, :nt], qy)), 9),
+                    "grad_rel_err": round(_rel(g32[k] * s, gC * s), 9)})
+    worst = max(out, key=lambda r: r["grad_rel_err"]) if out else None
+    return {"instances": len(out), "max_fwd_rel_err": max(r["fwd_rel_err"] for r in out),
+            "max_grad_rel_err": worst["grad_rel_err"], "worst": worst, "oracle_s": round(time.perf_counter() - t0, 1),
+            "per_instance": out}
+
+
 def multi_plain_autograd(inv, dev, nt=100, count=8):
     """The restated reference path with autograd on the GPU (FP32), looped over
     `count` instances spread over the sizes, `nt` steps each: cell-steps per
@@ -591,9 +673,16 @@ def run_multi(args, dist):
     lib = E.load_library()
     ws = Hn.multi_instances(64)
     t0 = time.perf_counter()
-    # configuration 5: kernel path per group from the autotuner, unless one is forced
-    tuned = args.path in ("auto", "tuned")
-    inv = Hn.MultiInversion(ws, dev, tuned=tuned, path=None if tuned else PATHS[args.path])
+    tuned = False
+    if args.grouped:
+        # instances grouped by size, each group one call with per-shot
+        # constants; kernel path per group from the autotuner unless forced
+        tuned = args.path in ("auto", "tuned")
+        inv = Hn.MultiInversion(ws, dev, tuned=tuned, path=None if tuned else PATHS[args.path])
+    else:
+        # configuration 5 as one propagation: every instance a region of one
+        # canvas, one launch per time step over the running instances' tiles
+        inv = Hn.CanvasInversion(ws, dev, nt=args.nt)
     setup_s = time.perf_counter() - t0
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(max(args.warmup, 0)):
@@ -629,7 +718,7 @@ def run_multi(args, dist):
     for k in range(args.steps):
         flush.zero_()
         e2e[k][0].record()
-        loss = inv.step(obs=[o.to(dev, non_blocking=True) for o in obs_h])
+        loss = inv.step([o.to(dev, non_blocking=True) for o in obs_h])
         out_h.copy_(torch.cat([loss.reshape(1), inv.gradient().double()]), non_blocking=True)
         e2e[k][1].record()
     torch.cuda.synchronize()
@@ -637,13 +726,16 @@ def run_multi(args, dist):
     sides = [w.nx for w in ws]
     # library kernels of one iteration (an eager iteration: replays make no host calls)
     n_eager = lib.ernn_launch_count()
-    inv._eager_step()
+    (inv._eager_step if args.grouped else inv.step_eager)()
     torch.cuda.synchronize()
     per_iter = lib.ernn_launch_count() - n_eager
     extra = {}
     if dist.rank == 0 and not args.no_cpu_baseline:
-        extra["grad_error_vs_fp64"] = multi_grad_errors(inv)
-        extra["plain_autograd_loop"] = multi_plain_autograd(inv, dev)
+        if args.grouped:
+            extra["grad_error_vs_fp64"] = multi_grad_errors(inv)
+            extra["plain_autograd_loop"] = multi_plain_autograd(inv, dev)
+        else:
+            extra["grad_error_vs_fp64"] = canvas_grad_errors(inv, dev, count=args.err_instances)
     return {
         "metric": "Gcell-steps/s fwd+adj (hand adjoint, one Adam iteration)",
         "value": round(value, 4), "unit": "Gcell-steps/s", "n_gpus": dist.world,
@@ -651,9 +743,12 @@ def run_multi(args, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded instances and observations)",
         "config": {"workload": f"multi64: 64 inversions, side {min(sides)}..{max(sides)}, nt = 5.2 side, "
-                               f"one CUDA-graph-captured Adam iteration over all instances; "
-                               f"{len(inv.groups)} groups of equal instances, each one call with "
-                               f"per-shot constants, on 8 streams",
+                               f"one CUDA-graph-captured Adam iteration over all instances; " +
+                               (f"{len(inv.groups)} groups of equal instances, each one call with "
+                                f"per-shot constants, on 8 streams" if args.grouped else
+                                f"one {inv.canvas[0]}x{inv.canvas[1]} canvas, one launch per step over "
+                                f"a tile table of the running instances (checkpoint every "
+                                f"{inv.geom.ckpt_k})"),
                    "cell_steps_per_iter": inv.cell_steps,
                    "path_choice": "measured per group (autotune)" if tuned else args.path,
                    "l2": "flushed between timed iterations (256 MiB write)"},

@@ -14,6 +14,7 @@ MODE_SCALAR, MODE_DFIELD, MODE_FIELDS = 0, 1, 2
 RECORD_FIELDS, RECORD_RECEIVERS = 0, 1
 PATH_AUTO, PATH_STEP, PATH_RESIDENT, PATH_TILED = 0, 1, 2, 3
 FLAG_SHOT_CONSTANTS = 1
+FLAG_INSTANCES = 2
 
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "workspace too small", 3: "CUDA runtime error",
@@ -37,6 +38,12 @@ class ErnnInputs(ctypes.Structure):
     """Mirror of struct ErnnInputs (include/ernn.h); every field is a device pointer."""
     _fields_ = [(n, ctypes.c_void_p) for n in
                 ("C", "D", "rho", "src_signal", "src_map", "src_origin", "rec_idx")]
+
+
+class ErnnInstances(ctypes.Structure):
+    """Mirror of struct ErnnInstances (include/ernn.h); the arrays are host int32."""
+    _fields_ = [("count", ctypes.c_int32)] + [(n, ctypes.POINTER(ctypes.c_int32)) for n in
+                                               ("x0", "y0", "nx", "ny", "nt")]
 
 
 class ErnnFemProblem(ctypes.Structure):
@@ -78,6 +85,12 @@ SIGNATURES = {
     "ernn_operator": (ctypes.c_int, [ctypes.c_int32] * 4 + [ctypes.c_double] + [_P] * 10),
     "ernn_forward": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
                                     _P, _P, _P, ctypes.c_size_t, ctypes.c_int, _P]),
+    "ernn_forward_instances": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
+                                              ctypes.POINTER(ErnnInstances), _P, _P, _P, ctypes.c_size_t,
+                                              ctypes.c_int, _P]),
+    "ernn_adjoint_instances": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
+                                              ctypes.POINTER(ErnnInstances), _P, _P, _P, ctypes.c_size_t,
+                                              _P, ctypes.c_size_t, _P, _P]),
     "ernn_adjoint": (ctypes.c_int, [ctypes.POINTER(ErnnProblem), ctypes.POINTER(ErnnInputs),
                                     _P, _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, _P,
                                     _P]),

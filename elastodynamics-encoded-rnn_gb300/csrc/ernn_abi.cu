@@ -2,6 +2,7 @@
 // host-side time-loop driver: step schedule, checkpoint/recompute plan,
 // workspace layout.  Every launch goes on the caller's stream; nothing here
 // synchronises the host or allocates device memory.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstddef>
@@ -31,7 +32,17 @@ struct Plan {
   size_t t_coef, t_A, t_B, t_store, t_total_tape, t_total_notape;
   // adjoint scratch
   size_t s_coef, s_LA, s_LB, s_seg, s_lbuf, s_gacc, s_part, s_tflags, s_total;
+  // instances on a canvas: tile table (tape and scratch), a zero state (scratch)
+  bool inst;
+  size_t inst_bytes, t_inst, s_inst, s_zero;
 };
+
+// Upper bound of the tile-table entries of any placement of S instances on
+// an nx x ny canvas (each instance's tiling has at most one partial tile row
+// and column).
+inline size_t inst_table_bound(int nx, int ny, int S) {
+  return ((size_t)(nx + kInstTileRows - 1) / kInstTileRows + S) * ((size_t)(ny + 63) / 64 + S);
+}
 
 Plan make_plan(const ErnnProblem& p) {
   Plan pl{};
@@ -41,12 +52,18 @@ Plan make_plan(const ErnnProblem& p) {
   pl.store_all = (pl.nseg == 1);
   pl.nt_out = (p.nt + p.stride - 1) / p.stride;
   pl.N = (size_t)p.nx * p.ny;
-  pl.state_bytes = align_up((size_t)p.nshots * 2 * pl.N * sizeof(float));
-  const dim3 g = step_grid(p.nx, p.ny, p.nshots);
+  pl.inst = (p.flags & ERNN_FLAG_INSTANCES) != 0;
+  // instances share the canvas's one state plane
+  pl.state_bytes = align_up((size_t)(pl.inst ? 1 : p.nshots) * 2 * pl.N * sizeof(float));
+  const dim3 g = step_grid(p.nx, p.ny, pl.inst ? 1 : p.nshots);
   pl.nblocks = (int)(g.x * g.y * g.z);
-  pl.ncoef = (p.flags & ERNN_FLAG_SHOT_CONSTANTS) ? p.nshots : 1;
+  pl.ncoef = (p.flags & (ERNN_FLAG_SHOT_CONSTANTS | ERNN_FLAG_INSTANCES)) ? p.nshots : 1;
+  pl.inst_bytes = pl.inst ? align_up(inst_table_bound(p.nx, p.ny, p.nshots) * sizeof(int4)) +
+                                align_up((size_t)2 * p.nshots * sizeof(int4))
+                          : 0;
   size_t off = 0;
   pl.t_coef = off; off += align_up((size_t)pl.ncoef * sizeof(Coef));
+  pl.t_inst = off; off += pl.inst_bytes;
   pl.t_A = off; off += pl.state_bytes;
   pl.t_B = off; off += pl.state_bytes;
   pl.t_total_notape = off;
@@ -56,15 +73,18 @@ Plan make_plan(const ErnnProblem& p) {
   pl.t_total_tape = off;
   off = 0;
   pl.s_coef = off; off += align_up((size_t)pl.ncoef * sizeof(Coef));
+  pl.s_inst = off; off += pl.inst_bytes;
+  pl.s_zero = off; if (pl.inst) off += pl.state_bytes;  // u^0 = u^{-1} = 0 of the first segment
   pl.s_LA = off; off += pl.state_bytes;
   pl.s_LB = off; off += pl.state_bytes;
   // two recompute segments: the cluster-resident path recomputes segment j-1
   // while the adjoint consumes segment j
-  pl.s_seg = off; if (!pl.store_all) off += (size_t)2 * pl.k * pl.state_bytes;
+  // (instances: the tiled path only, one segment)
+  pl.s_seg = off; if (!pl.store_all) off += (size_t)(pl.inst ? 1 : 2) * pl.k * pl.state_bytes;
   // lam buffers of the resident reverse pass: two segments of kres steps,
   // only where that path can run
   pl.kres = pl.store_all ? (p.nt < kResStoreAllSegment ? p.nt : kResStoreAllSegment) : pl.k;
-  if (!resident_possible(p.mode, p.nx, p.ny)) pl.kres = 0;
+  if (!resident_possible(p.mode, p.nx, p.ny) || pl.inst) pl.kres = 0;
   pl.s_lbuf = off; off += (size_t)2 * pl.kres * pl.state_bytes;
   pl.s_gacc = off;
   if (p.mode == kModeDField) off += align_up((size_t)p.nshots * pl.N * sizeof(float));
@@ -79,7 +99,8 @@ Plan make_plan(const ErnnProblem& p) {
   // receiver table of the tiled adjoint: one byte per (shot, tile), sized for
   // its smallest tiles (64 x 16)
   pl.s_tflags = off;
-  if (p.record == kRecordReceivers) off += align_up(tma_tiles(p.nx, p.ny, p.nshots, 16));
+  if (p.record == kRecordReceivers)
+    off += align_up(pl.inst ? inst_table_bound(p.nx, p.ny, p.nshots) : tma_tiles(p.nx, p.ny, p.nshots, 16));
   pl.s_total = off;
   return pl;
 }
@@ -96,8 +117,12 @@ int validate(const ErnnProblem* p) {
   if (p->src_comp != 0 && p->src_comp != 1) return ERNN_ERR_INVALID;
   if (p->src_bx < 0 || p->src_by < 0) return ERNN_ERR_INVALID;
   if (p->path < ERNN_PATH_AUTO || p->path > ERNN_PATH_TILED) return ERNN_ERR_INVALID;
-  if ((p->flags & ~ERNN_FLAG_SHOT_CONSTANTS) != 0) return ERNN_ERR_INVALID;
+  if ((p->flags & ~(ERNN_FLAG_SHOT_CONSTANTS | ERNN_FLAG_INSTANCES)) != 0) return ERNN_ERR_INVALID;
   if ((p->flags & ERNN_FLAG_SHOT_CONSTANTS) && p->mode != kModeScalar) return ERNN_ERR_INVALID;
+  if ((p->flags & ERNN_FLAG_INSTANCES) &&
+      (p->mode != kModeScalar || p->record != kRecordReceivers || p->nshots > kMaxInstances ||
+       p->nx >= 65536 || p->ny >= 65536))
+    return ERNN_ERR_INVALID;
   if (!(p->h > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->h) || !std::isfinite(p->dt))
     return ERNN_ERR_INVALID;
   return ERNN_OK;
@@ -279,6 +304,63 @@ int resident_adjoint(const ErnnProblem& p, const Plan& pl, ResCommon& rc, const 
   return ERNN_OK;
 }
 
+// Instances of a canvas problem (ERNN_FLAG_INSTANCES), checked and ordered
+// by decreasing step count; upto[g] = tiles of the first g of that order.
+struct InstPlan {
+  InstDesc d;
+  int upto[kMaxInstances + 1];
+  // tiles of forward (or recompute) step i: instances with nt > i
+  int fwd_tiles(int i) const {
+    int g = 0;
+    while (g < d.count && d.nt[g] > i) ++g;
+    return upto[g];
+  }
+  // tiles of adjoint step m: instances with nt >= m
+  int adj_tiles(int m) const {
+    int g = 0;
+    while (g < d.count && d.nt[g] >= m) ++g;
+    return upto[g];
+  }
+};
+
+int plan_instances(const ErnnProblem& p, const ErnnInstances* in, InstPlan* ip) {
+  if (!(p.flags & ERNN_FLAG_INSTANCES) || in == nullptr || in->count != p.nshots || in->x0 == nullptr ||
+      in->y0 == nullptr || in->nx == nullptr || in->ny == nullptr || in->nt == nullptr)
+    return ERNN_ERR_INVALID;
+  const int S = in->count;
+  for (int k = 0; k < S; ++k) {
+    const int x0 = in->x0[k], y0 = in->y0[k], nx = in->nx[k], ny = in->ny[k], nt = in->nt[k];
+    if (x0 < 0 || y0 < 0 || nx < 1 || ny < 4 || y0 % 4 != 0 || ny % 4 != 0 || x0 + nx > p.nx ||
+        y0 + ny > p.ny || nt < 1 || nt > p.nt)
+      return ERNN_ERR_INVALID;
+  }
+  // regions at least one cell apart: those cells stay zero, the instances'
+  // ghost rings
+  for (int a = 0; a < S; ++a)
+    for (int b = a + 1; b < S; ++b) {
+      const bool apart = in->x0[a] + in->nx[a] + 1 <= in->x0[b] || in->x0[b] + in->nx[b] + 1 <= in->x0[a] ||
+                         in->y0[a] + in->ny[a] + 1 <= in->y0[b] || in->y0[b] + in->ny[b] + 1 <= in->y0[a];
+      if (!apart) return ERNN_ERR_INVALID;
+    }
+  int order[kMaxInstances];
+  for (int k = 0; k < S; ++k) order[k] = k;
+  std::stable_sort(order, order + S, [&](int u, int v) { return in->nt[u] > in->nt[v]; });
+  ip->d.count = S;
+  ip->upto[0] = 0;
+  for (int g = 0; g < S; ++g) {
+    const int k = order[g];
+    ip->d.id[g] = k;
+    ip->d.x0[g] = in->x0[k];
+    ip->d.y0[g] = in->y0[k];
+    ip->d.nx[g] = in->nx[k];
+    ip->d.ny[g] = in->ny[k];
+    ip->d.nt[g] = in->nt[k];
+    ip->d.base[g] = ip->upto[g];
+    ip->upto[g + 1] = ip->upto[g] + inst_tiles(in->nx[k], in->ny[k]);
+  }
+  return ERNN_OK;
+}
+
 }  // namespace
 
 void record_last_path(int32_t path) { g_last_path.store(path, std::memory_order_relaxed); }
@@ -362,19 +444,40 @@ int ernn_operator(int32_t nshots, int32_t nx, int32_t ny, int32_t mode, double h
   return ERNN_OK;
 }
 
-int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, float* out_uy,
-                 void* tape, size_t tape_bytes, int with_tape, void* stream) {
+// The forward time loop of ernn_forward and, with an instance plan `ip`, of
+// ernn_forward_instances.
+static int forward_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPlan* ip, float* out_ux,
+                        float* out_uy, void* tape, size_t tape_bytes, int with_tape, void* stream) {
   int rc = validate(p);
   if (rc) return rc;
   if ((rc = validate_inputs(p, in))) return rc;
   if (out_ux == nullptr || out_uy == nullptr || tape == nullptr) return ERNN_ERR_INVALID;
+  if ((ip != nullptr) != ((p->flags & ERNN_FLAG_INSTANCES) != 0)) return ERNN_ERR_INVALID;
   const Plan pl = make_plan(*p);
   if (tape_bytes < (with_tape ? pl.t_total_tape : pl.t_total_notape)) return ERNN_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
   Coef* coef = reinterpret_cast<Coef*>(at(tape, pl.t_coef));
   ERNN_CUDA(launch_coef(p->mode, in->C, in->rho, p->h, p->dt, coef, st, pl.ncoef));
 
-  if (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT) {
+  InstTiles itab{nullptr, nullptr, 0};
+  if (ip != nullptr) {
+    // instances: the tiled kernels over the tile table only; every state
+    // buffer starts at zero (cells between the regions are never written:
+    // the instances' ghost rings), trace frames past an instance's steps too
+    if (p->path != ERNN_PATH_AUTO && p->path != ERNN_PATH_TILED) return ERNN_ERR_UNSUPPORTED;
+    if (!tma_eligible(p->mode, p->nx, p->ny, 1)) return ERNN_ERR_UNSUPPORTED;
+    itab.tiles = reinterpret_cast<int4*>(at(tape, pl.t_inst));
+    itab.box = reinterpret_cast<int4*>(at(tape, pl.t_inst + align_up(inst_table_bound(p->nx, p->ny, p->nshots) *
+                                                                       sizeof(int4))));
+    ERNN_CUDA(launch_inst_table(ip->d, const_cast<int4*>(itab.tiles), const_cast<int4*>(itab.box), st));
+    const size_t zero_to = with_tape ? pl.t_total_tape : pl.t_total_notape;
+    ERNN_CUDA(cudaMemsetAsync(at(tape, pl.t_A), 0, zero_to - pl.t_A, st));
+    const size_t tr_bytes = (size_t)p->nshots * pl.nt_out * p->nrec * sizeof(float);
+    ERNN_CUDA(cudaMemsetAsync(out_ux, 0, tr_bytes, st));
+    ERNN_CUDA(cudaMemsetAsync(out_uy, 0, tr_bytes, st));
+  }
+
+  if (ip == nullptr && (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT)) {
     ResCommon res;
     if (pick_resident(*p, *in, coef, res)) {
       g_last_path.store(ERNN_PATH_RESIDENT, std::memory_order_relaxed);
@@ -383,7 +486,8 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
     if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;
   }
   int tiled = 0;
-  if ((rc = use_tiled(*p, &tiled))) return rc;
+  if (ip != nullptr) tiled = 1;
+  else if ((rc = use_tiled(*p, &tiled))) return rc;
   g_last_path.store(tiled ? ERNN_PATH_TILED : ERNN_PATH_STEP, std::memory_order_relaxed);
   auto fwd_step = [&](const FwdStep& s) {
     return tiled ? launch_tma_fwd(p->mode, s, &coef->err, st) : launch_fwd_step(p->mode, s, st);
@@ -398,6 +502,7 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
   };
   const bool receivers = (p->record == kRecordReceivers);
   FwdStep a = base_fwd(*p, *in, coef, pl.nt_out);
+  a.inst = itab;
   const float* last = nullptr;
   for (int i = 0; i < p->nt; ++i) {
     if (store_all) {
@@ -408,6 +513,11 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
       a.out = (i % 2 == 0) ? A : B;
       a.cur = i == 0 ? nullptr : ((i % 2 == 0) ? B : A);
       a.prev = i <= 1 ? nullptr : a.out;
+    }
+    if (ip != nullptr) {
+      // u^0 = 0: B (zeroed, first written at step 1) stands for it
+      if (a.cur == nullptr) a.cur = B;
+      a.inst.ntiles = ip->fwd_tiles(i);
     }
     a.i = i;
     a.copy0 = a.copy1 = nullptr;
@@ -428,17 +538,35 @@ int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, floa
   }
   if (receivers && (p->nt - 1) % p->stride == 0) {
     ERNN_CUDA(launch_gather(last, p->nx, p->ny, p->nshots, in->rec_idx, p->nrec,
-                            (p->nt - 1) / p->stride, pl.nt_out, out_ux, out_uy, st));
+                            (p->nt - 1) / p->stride, pl.nt_out, out_ux, out_uy, st, itab.box, p->nt));
   }
   return ERNN_OK;
 }
 
-int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
-                 const float* g_uy, const void* tape_c, size_t tape_bytes, void* scratch,
-                 size_t scratch_bytes, double* grad_C, float* grad_field, void* stream) {
+int ernn_forward(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, float* out_uy,
+                 void* tape, size_t tape_bytes, int with_tape, void* stream) {
+  return forward_impl(p, in, nullptr, out_ux, out_uy, tape, tape_bytes, with_tape, stream);
+}
+
+int ernn_forward_instances(const ErnnProblem* p, const ErnnInputs* in, const ErnnInstances* inst,
+                           float* out_ux, float* out_uy, void* tape, size_t tape_bytes, int with_tape,
+                           void* stream) {
+  int rc = validate(p);
+  if (rc) return rc;
+  InstPlan ip;
+  if ((rc = plan_instances(*p, inst, &ip))) return rc;
+  return forward_impl(p, in, &ip, out_ux, out_uy, tape, tape_bytes, with_tape, stream);
+}
+
+// The adjoint of ernn_adjoint and, with an instance plan `ip`, of
+// ernn_adjoint_instances.
+static int adjoint_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPlan* ip, const float* g_ux,
+                        const float* g_uy, const void* tape_c, size_t tape_bytes, void* scratch,
+                        size_t scratch_bytes, double* grad_C, float* grad_field, void* stream) {
   int rc = validate(p);
   if (rc) return rc;
   if ((rc = validate_inputs(p, in))) return rc;
+  if ((ip != nullptr) != ((p->flags & ERNN_FLAG_INSTANCES) != 0)) return ERNN_ERR_INVALID;
   if (g_ux == nullptr || g_uy == nullptr || tape_c == nullptr || scratch == nullptr)
     return ERNN_ERR_INVALID;
   if (p->mode == kModeScalar && grad_C == nullptr) return ERNN_ERR_INVALID;
@@ -461,7 +589,22 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   if (p->mode != kModeScalar) ERNN_CUDA(cudaMemsetAsync(gacc, 0, pl.s_part - pl.s_gacc, st));
   else ERNN_CUDA(cudaMemsetAsync(partials, 0, pl.s_tflags - pl.s_part, st));
 
-  if (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT) {
+  InstTiles itab{nullptr, nullptr, 0};
+  if (ip != nullptr) {
+    // instances: the tiled kernels over the tile table only; the zero state
+    // and the recompute segment start at zero (cells between the regions are
+    // never written: the instances' ghost rings)
+    if (p->path != ERNN_PATH_AUTO && p->path != ERNN_PATH_TILED) return ERNN_ERR_UNSUPPORTED;
+    if (!tma_eligible(p->mode, p->nx, p->ny, 1)) return ERNN_ERR_UNSUPPORTED;
+    itab.tiles = reinterpret_cast<int4*>(at(scratch, pl.s_inst));
+    itab.box = reinterpret_cast<int4*>(at(scratch, pl.s_inst + align_up(inst_table_bound(p->nx, p->ny, p->nshots) *
+                                                                          sizeof(int4))));
+    ERNN_CUDA(launch_inst_table(ip->d, const_cast<int4*>(itab.tiles), const_cast<int4*>(itab.box), st));
+    ERNN_CUDA(cudaMemsetAsync(at(scratch, pl.s_zero), 0, pl.state_bytes, st));
+    if (!pl.store_all) ERNN_CUDA(cudaMemsetAsync(at(scratch, pl.s_seg), 0, (size_t)pl.k * pl.state_bytes, st));
+  }
+
+  if (ip == nullptr && (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT)) {
     ResCommon res;
     if (pick_resident(*p, *in, coef, res)) {
       g_last_path.store(ERNN_PATH_RESIDENT, std::memory_order_relaxed);
@@ -477,12 +620,14 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     if (p->path == ERNN_PATH_RESIDENT) return ERNN_ERR_UNSUPPORTED;
   }
   int tiled = 0;
-  if ((rc = use_tiled(*p, &tiled))) return rc;
+  if (ip != nullptr) tiled = 1;
+  else if ((rc = use_tiled(*p, &tiled))) return rc;
   g_last_path.store(tiled ? ERNN_PATH_TILED : ERNN_PATH_STEP, std::memory_order_relaxed);
 
   auto stored = [&](int n) { return fat(tape, pl.t_store + (size_t)(n - 1) * pl.state_bytes); };
+  const float* zero_state = ip != nullptr ? fat(scratch, pl.s_zero) : nullptr;
   auto ck = [&](int j, int lev) -> const float* {
-    if (j == 0) return nullptr;
+    if (j == 0) return lev == 0 ? zero_state : nullptr;  // u^0 = 0 (given as a state with instances)
     if (lev == 1 && j * pl.k - 1 == 0) return nullptr;  // u^0 = 0 (k == 1)
     return fat(tape, pl.t_store + ((size_t)(j - 1) * 2 + lev) * pl.state_bytes);
   };
@@ -499,9 +644,14 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   b.partials = partials;
   b.gacc = gacc;
   b.tile_flags = nullptr;
+  b.inst = itab;
   if (tiled && p->record == kRecordReceivers) {
     uint8_t* flags = reinterpret_cast<uint8_t*>(at(scratch, pl.s_tflags));
-    ERNN_CUDA(launch_tile_flags(p->mode, in->rec_idx, p->nshots, p->nrec, p->nx, p->ny, flags, st));
+    if (ip != nullptr)
+      ERNN_CUDA(launch_inst_tile_flags(in->rec_idx, p->nshots, p->nrec, p->ny, itab.box, flags,
+                                       ip->upto[ip->d.count], st));
+    else
+      ERNN_CUDA(launch_tile_flags(p->mode, in->rec_idx, p->nshots, p->nrec, p->nx, p->ny, flags, st));
     b.tile_flags = flags;
   }
 
@@ -522,6 +672,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
   auto adj_step = [&](int m, const float* um) -> int {
     const int idx = p->nt - m;
     b.m = m;
+    if (ip != nullptr) b.inst.ntiles = ip->adj_tiles(m);
     b.out = (idx % 2 == 0) ? LA : LB;
     b.cur = (idx % 2 == 0) ? LB : LA;
     b.prev = b.out;
@@ -538,6 +689,7 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
       if ((rc = adj_step(m, stored(m)))) return rc;
   } else {
     FwdStep a = base_fwd(*p, *in, coef, pl.nt_out);
+    a.inst = itab;
     for (int j = pl.nseg - 1; j >= 0; --j) {
       const int i0 = j * pl.k, i1 = (j + 1) * pl.k < p->nt ? (j + 1) * pl.k : p->nt;
       // recompute u^{i0+1} .. u^{i1} into the segment buffer; u^{nt} is never
@@ -551,7 +703,13 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
         a.prev = (i == i0) ? ck(j, 1) : (i == i0 + 1 ? ck(j, 0) : seg(i - i0 - 2));
         a.chained = chained ? 1 : 0;
         chained = true;
-        a.out2 = (tiled && i + 1 < iend) ? seg(i + 1 - i0) : nullptr;
+        if (ip != nullptr) a.inst.ntiles = ip->fwd_tiles(i);
+        // (a pair of steps takes the tiles of the first step: an instance
+        // ending after step i runs both of them, one ending at i + 1 takes
+        // the pair only when it has step i + 1)
+        a.out2 = (tiled && i + 1 < iend && (ip == nullptr || ip->fwd_tiles(i + 1) == a.inst.ntiles))
+                     ? seg(i + 1 - i0)
+                     : nullptr;
         if (a.out2 != nullptr && tma_fwd2_would_run(p->mode, a)) {
           ERNN_CUDA(launch_tma_fwd2(p->mode, a, &coef->err, st));
           i += 2;
@@ -576,6 +734,24 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
     ERNN_CUDA(launch_finalize_fields(p->mode, gacc, p->nshots, (int)pl.N, coef, grad_field, st));
   }
   return ERNN_OK;
+}
+
+int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
+                 const float* g_uy, const void* tape_c, size_t tape_bytes, void* scratch,
+                 size_t scratch_bytes, double* grad_C, float* grad_field, void* stream) {
+  return adjoint_impl(p, in, nullptr, g_ux, g_uy, tape_c, tape_bytes, scratch, scratch_bytes, grad_C,
+                      grad_field, stream);
+}
+
+int ernn_adjoint_instances(const ErnnProblem* p, const ErnnInputs* in, const ErnnInstances* inst,
+                           const float* g_ux, const float* g_uy, const void* tape, size_t tape_bytes,
+                           void* scratch, size_t scratch_bytes, double* grad_C, void* stream) {
+  int rc = validate(p);
+  if (rc) return rc;
+  InstPlan ip;
+  if ((rc = plan_instances(*p, inst, &ip))) return rc;
+  return adjoint_impl(p, in, &ip, g_ux, g_uy, tape, tape_bytes, scratch, scratch_bytes, grad_C, nullptr,
+                      stream);
 }
 
 uint64_t ernn_launch_count(void) { return launches(); }

@@ -528,17 +528,22 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
 }
 
 // --------------------------------------------------------------------------
+// With instances (inst_box != nullptr) every shot reads the one canvas
+// plane, and an instance whose step count is below `step` (the state index
+// recorded) gets zeros: its frames end earlier.
 __global__ void gather_kernel(const float* __restrict__ state, int N, int S,
                               const int32_t* __restrict__ rec_idx, int nrec, int frame,
-                              int nt_out, float* __restrict__ tr_x, float* __restrict__ tr_y) {
+                              int nt_out, float* __restrict__ tr_x, float* __restrict__ tr_y,
+                              const int4* __restrict__ inst_box, int step) {
   const int total = S * nrec;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int s = e / nrec, r = e - s * nrec;
     const int32_t idx = rec_idx[e];
     const size_t o = ((size_t)s * nt_out + frame) * nrec + r;
-    const bool ok = idx >= 0 && idx < N;  // out of range: 0
-    tr_x[o] = ok ? state[(size_t)s * 2 * N + idx] : 0.f;
-    tr_y[o] = ok ? state[(size_t)s * 2 * N + N + idx] : 0.f;
+    const size_t plane = inst_box ? 0 : (size_t)s * 2 * N;
+    const bool ok = idx >= 0 && idx < N && (inst_box == nullptr || step <= inst_box[2 * s + 1].z);
+    tr_x[o] = ok ? state[plane + idx] : 0.f;
+    tr_y[o] = ok ? state[plane + N + idx] : 0.f;
   }
 }
 
@@ -734,10 +739,10 @@ cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st) {
 
 cudaError_t launch_gather(const float* state, int nx, int ny, int S, const int32_t* rec_idx,
                           int nrec, int frame, int nt_out, float* tr_x, float* tr_y,
-                          cudaStream_t st) {
+                          cudaStream_t st, const int4* inst_box, int step) {
   return tracked(kProfOther, st, [&] {
     gather_kernel<<<small_grid((size_t)S * nrec, 256), 256, 0, st>>>(
-        state, nx * ny, S, rec_idx, nrec, frame, nt_out, tr_x, tr_y);
+        state, nx * ny, S, rec_idx, nrec, frame, nt_out, tr_x, tr_y, inst_box, step);
   });
 }
 

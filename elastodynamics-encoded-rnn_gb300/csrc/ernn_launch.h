@@ -12,6 +12,17 @@
 
 namespace ernn {
 
+// Instances on one canvas (ERNN_FLAG_INSTANCES): the tiled kernels walk a
+// tile table instead of the grid's tiling.  Entry t of the table is
+// (instance, x0, y0, 0) of one 64 x 16 tile; per instance k, box[2k] =
+// (x0, y0, x1, y1) of its region and box[2k + 1] = (first table entry of its
+// tiles, tiles per tile row, steps, 0).
+struct InstTiles {
+  const int4* tiles;   // the table, instances ordered by decreasing step count
+  const int4* box;     // per instance (region, tiling and step count)
+  int ntiles;          // entries of this launch: the prefix of running instances
+};
+
 // Per-step arguments of the forward kernel: computes u^{i+1} from u^i, u^{i-1}.
 // State buffers are laid out [shot][component][cell] with N = nx*ny cells.
 struct FwdStep {
@@ -39,6 +50,7 @@ struct FwdStep {
   const int32_t* src_origin;
   int bx, by, src_comp;
   int chained;  // previous launch on the stream is a step kernel of the same loop
+  InstTiles inst;  // instances: tile table (inst.tiles == nullptr otherwise)
 };
 
 // Per-step arguments of the adjoint kernel: computes lam^m from lam^{m+1},
@@ -63,6 +75,7 @@ struct AdjStep {
   // receiver, or nullptr (every tile scans the receivers)
   const uint8_t* tile_flags;
   int chained;  // previous launch on the stream is a step kernel of the same loop
+  InstTiles inst;  // instances: tile table (inst.tiles == nullptr otherwise)
 };
 
 dim3 step_grid(int nx, int ny, int S);
@@ -74,7 +87,7 @@ cudaError_t launch_fwd_step(int mode, const FwdStep& a, cudaStream_t st);
 cudaError_t launch_adj_step(int mode, const AdjStep& a, cudaStream_t st);
 cudaError_t launch_gather(const float* state, int nx, int ny, int S, const int32_t* rec_idx,
                           int nrec, int frame, int nt_out, float* tr_x, float* tr_y,
-                          cudaStream_t st);
+                          cudaStream_t st, const int4* inst_box = nullptr, int step = 0);
 cudaError_t launch_gscale(const float* gx, const float* gy, size_t n, Coef* coef,
                           cudaStream_t st, int ncoef = 1);
 // ngrad gradients of 6: gradient s sums partial rows [s nblocks, (s+1) nblocks).

@@ -454,6 +454,208 @@ __device__ __forceinline__ void ring_step(const Tile& T, const KSr& ks, const St
   }
 }
 
+// ------------------------------------------------- register-resident step
+// The step roles' fast form, for grids whose CTAs split into full chunks of
+// RC rows (every thread one unit of exactly RC rows).  A thread's unit
+// (column quad, RC consecutive rows) is fixed for the launch, so the thread
+// keeps its own cells of the current and the previous level in registers
+// from one step to the next: per step it reads from shared memory only the
+// left and right neighbours of its rows and the rows just above and below
+// its chunk, and writes its new cells (for the neighbours' windows of the
+// next step and the state copies); the previous level never comes back from
+// shared memory.  The three-level ring in shared memory stays complete
+// (every cell is stored every step), so halo pushes, bulk state copies,
+// trace recording and the final lam pair read it as before.  Receiver
+// residuals (adjoint role) are added by the threads owning the receiver
+// cells, in registers.
+struct RegUnit {
+  bool active;       // the thread has a unit (a chunk inside the CTA's rows)
+  int j;             // first column of the quad
+  int ra;            // rows ra .. ra+RC-1 (local)
+  bool top_ext;      // row ra is the CTA's first row (its upper row is a halo row)
+  bool bot_ext;      // row ra+RC-1 is the CTA's last row
+  uint32_t src_rows; // bit k: row ra+k meets the source box (forward role)
+  uint32_t rmask;    // bit 4k+q: cell (ra+k, j+q) holds a receiver (adjoint role)
+};
+
+// The thread's own cells of a level: rows ra .. ra+RC-1 of the quad at j.
+template <int RC>
+__device__ __forceinline__ void own_load(const Tile& T, const float* level, const RegUnit& U,
+                                         float (&vx)[RC][4], float (&vy)[RC][4]) {
+#pragma unroll
+  for (int k = 0; k < RC; ++k) {
+    const float4 a = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(level), 0) + T.at(U.ra + k + 1, U.j));
+    const float4 b = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(level), 1) + T.at(U.ra + k + 1, U.j));
+    vx[k][0] = a.x; vx[k][1] = a.y; vx[k][2] = a.z; vx[k][3] = a.w;
+    vy[k][0] = b.x; vy[k][1] = b.y; vy[k][2] = b.z; vy[k][3] = b.w;
+  }
+}
+
+// A row window as register references: left neighbour, the four cells, right
+// neighbour (columns j-1 .. j+4).
+struct RowRef {
+  const float& l;
+  const float (&c)[4];
+  const float& r;
+};
+
+// One component's stencil sums of the four cells from the rows above (u0),
+// at (u1) and below (u2): the terms of comp_stencils in the same order and
+// rounding.
+__device__ __forceinline__ void ref_stencils(const RowRef& u0, const RowRef& u1, const RowRef& u2,
+                                             float xx[4], float yy[4], float xy[4]) {
+  auto at = [](const RowRef& u, int k) -> float { return k == 0 ? u.l : k == 5 ? u.r : u.c[k - 1]; };
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int k = 2 * p + 1;
+    const float2 m0 = make_float2(at(u0, k), at(u0, k + 1));
+    const float2 m1 = make_float2(at(u1, k), at(u1, k + 1));
+    const float2 m2 = make_float2(at(u2, k), at(u2, k + 1));
+    put(xx, p, __ffma2_rn(dup2(-2.f), m1, __fadd2_rn(m0, m2)));
+    put(yy, p, __ffma2_rn(dup2(-2.f), m1, make_float2(at(u1, k - 1) + at(u1, k + 1), at(u1, k) + at(u1, k + 2))));
+    const float2 a = make_float2(at(u2, k + 1) + at(u0, k - 1), at(u2, k + 2) + at(u0, k));
+    const float2 b = make_float2(at(u2, k - 1) + at(u0, k + 1), at(u2, k) + at(u0, k + 2));
+    put(xy, p, __fadd2_rn(a, neg2(b)));
+  }
+}
+
+// New values of one own row (local row lr): px, py hold the previous level
+// on entry and the new level on return.  The new row is stored into the
+// next level and, on the CTA's first and last row, pushed into the
+// neighbours' halo rows.  Same terms, order and rounding as row_step.
+template <bool LAM, bool DENSE>
+__device__ __forceinline__ void reg_row(const Tile& T, const KSr& ks, const StepCtx& x, const Rhs& rhs,
+                                        int lr, int j, bool src_row, const RowRef& ax, const RowRef& ay,
+                                        const RowRef& bx, const RowRef& by, const RowRef& dx,
+                                        const RowRef& dy, float (&px)[4], float (&py)[4]) {
+  const int ny = x.ny;
+  const int s = lr + 1;
+  Quad st;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    st.cx[q] = bx.c[q];
+    st.cy[q] = by.c[q];
+  }
+  ref_stencils(ax, bx, dx, st.xx_x, st.yy_x, st.xy_x);
+  ref_stencils(ay, by, dy, st.xx_y, st.yy_y, st.xy_y);
+  float2 v2x[2], v2y[2];
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    float2 lx, ly;
+    lq2(ks, st, p, lx, ly);
+    v2x[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cx, p), neg2(pair(px, p))), lx);
+    v2y[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cy, p), neg2(pair(py, p))), ly);
+  }
+  if (!LAM) {
+    if (src_row) {
+      const float4 fl = *reinterpret_cast<const float4*>(rhs.F + lr * ny + j);
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const float2 fz = __fmul2_rn(dup2(rhs.amp), pair4(fl, p));
+        if (rhs.src_comp == 0) v2x[p] = __fadd2_rn(v2x[p], fz); else v2y[p] = __fadd2_rn(v2y[p], fz);
+      }
+    }
+  } else if (DENSE && rhs.gx != nullptr) {
+    const float4 a4 = *reinterpret_cast<const float4*>(rhs.gx + (size_t)lr * ny + j);
+    const float4 b4 = *reinterpret_cast<const float4*>(rhs.gy + (size_t)lr * ny + j);
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      v2x[p] = __ffma2_rn(dup2(rhs.gs), pair4(a4, p), v2x[p]);
+      v2y[p] = __ffma2_rn(dup2(rhs.gs), pair4(b4, p), v2y[p]);
+    }
+  }
+  put(px, 0, v2x[0]);
+  put(px, 1, v2x[1]);
+  put(py, 0, v2y[0]);
+  put(py, 1, v2y[1]);
+  const float4 nvx = f4(px), nvy = f4(py);
+  *reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j)) = nvx;
+  *reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j)) = nvy;
+  if (lr == 0 && x.up_base) {  // into rank-1's bottom halo row
+    const uint32_t o = x.nxt_off_b + 4u * (uint32_t)T.at(x.R + 1, j);
+    st_async16(x.up_base + o, nvx, x.up_bar);
+    st_async16(x.up_base + o + 4u * (uint32_t)T.plane, nvy, x.up_bar);
+  }
+  if (lr == x.rows - 1 && x.dn_base) {  // into rank+1's top halo row
+    const uint32_t o = x.nxt_off_b + 4u * (uint32_t)T.at(0, j);
+    st_async16(x.dn_base + o, nvx, x.dn_bar);
+    st_async16(x.dn_base + o + 4u * (uint32_t)T.plane, nvy, x.dn_bar);
+  }
+}
+
+// Window [j-1 .. j+4] of a shared-memory row as (left, quad, right).
+struct HaloRow {
+  float l, c[4], r;
+};
+__device__ __forceinline__ void load_halo(const float* __restrict__ p, int j, int ny, HaloRow& h) {
+  const float4 m = *reinterpret_cast<const float4*>(p + j);
+  h.l = (j >= 1) ? p[j - 1] : 0.f;
+  h.c[0] = m.x;
+  h.c[1] = m.y;
+  h.c[2] = m.z;
+  h.c[3] = m.w;
+  h.r = (j + 4 < ny) ? p[j + 4] : 0.f;
+}
+
+// One ring step of the register-resident form.  (cx, cy): the thread's cells
+// of cur; (px, py): of prev on entry, of nxt on return.  The rows that read
+// a neighbour CTA's halo row (the CTA's first and last rows) run after the
+// bounded wait for it, every other row before; threads with neither row do
+// not wait.
+template <bool LAM, bool DENSE, int RC>
+__device__ __forceinline__ void reg_step(const Tile& T, const KSr& ks, const StepCtx& x, const Rhs& rhs,
+                                         uint64_t* cur_bar, uint32_t parity, bool wait, int* err,
+                                         const RegUnit& U, const float (&cx)[RC][4],
+                                         const float (&cy)[RC][4], float (&px)[RC][4],
+                                         float (&py)[RC][4]) {
+  const int ny = x.ny, j = U.j, a = U.ra;
+  const float* cur0 = T.comp(const_cast<float*>(x.cur), 0);
+  const float* cur1 = T.comp(const_cast<float*>(x.cur), 1);
+  float lx[RC], rx[RC], ly[RC], ry[RC];
+#pragma unroll
+  for (int k = 0; k < RC; ++k) {
+    const int o = T.at(a + k + 1, 0);
+    lx[k] = j >= 1 ? cur0[o + j - 1] : 0.f;
+    ly[k] = j >= 1 ? cur1[o + j - 1] : 0.f;
+    rx[k] = j + 4 < ny ? cur0[o + j + 4] : 0.f;
+    ry[k] = j + 4 < ny ? cur1[o + j + 4] : 0.f;
+  }
+  HaloRow tx, ty, bx, by;  // rows a-1 and a+RC (halo coordinates a and a+RC+1)
+  if (!U.top_ext) {
+    load_halo(cur0 + T.at(a, 0), j, ny, tx);
+    load_halo(cur1 + T.at(a, 0), j, ny, ty);
+  }
+  if (!U.bot_ext) {
+    load_halo(cur0 + T.at(a + RC + 1, 0), j, ny, bx);
+    load_halo(cur1 + T.at(a + RC + 1, 0), j, ny, by);
+  }
+  auto row = [&](int k) {
+    const RowRef bxr{lx[k], cx[k], rx[k]}, byr{ly[k], cy[k], ry[k]};
+    const RowRef axr = k == 0 ? RowRef{tx.l, tx.c, tx.r} : RowRef{lx[k - 1], cx[k - 1], rx[k - 1]};
+    const RowRef ayr = k == 0 ? RowRef{ty.l, ty.c, ty.r} : RowRef{ly[k - 1], cy[k - 1], ry[k - 1]};
+    const RowRef dxr = k == RC - 1 ? RowRef{bx.l, bx.c, bx.r} : RowRef{lx[k + 1], cx[k + 1], rx[k + 1]};
+    const RowRef dyr = k == RC - 1 ? RowRef{by.l, by.c, by.r} : RowRef{ly[k + 1], cy[k + 1], ry[k + 1]};
+    reg_row<LAM, DENSE>(T, ks, x, rhs, a + k, j, (U.src_rows >> k) & 1u, axr, ayr, bxr, byr, dxr, dyr,
+                        px[k], py[k]);
+  };
+#pragma unroll
+  for (int k = 0; k < RC; ++k)
+    if (!(k == 0 && U.top_ext) && !(k == RC - 1 && U.bot_ext)) row(k);
+  if (U.top_ext || U.bot_ext) {
+    if (wait) halo_wait(cur_bar, parity, err);
+    if (U.top_ext) {
+      load_halo(cur0 + T.at(0, 0), j, ny, tx);
+      load_halo(cur1 + T.at(0, 0), j, ny, ty);
+    }
+    if (U.bot_ext) {
+      load_halo(cur0 + T.at(a + RC + 1, 0), j, ny, bx);
+      load_halo(cur1 + T.at(a + RC + 1, 0), j, ny, by);
+    }
+    if (U.top_ext) row(0);
+    if (U.bot_ext && (RC > 1 || !U.top_ext)) row(RC - 1);
+  }
+}
+
 // Row window [j-1 .. j+4] of row i of a global plane (zero outside the grid).
 __device__ __forceinline__ void load_grow6(const float* __restrict__ plane, int i, int j, int nx,
                                            int ny, float w[6]) {
@@ -553,7 +755,7 @@ __device__ void imaging_role(const ResCommon& c, const ResImg& g, int shot, int 
 }
 
 // ---------------------------------------------------------------- kernel
-template <bool DENSE>
+template <bool DENSE, int RC>
 __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommon c, const ResFwd f,
                                                                    const ResLam a, const ResImg g,
                                                                    const ResRoles roles) {
@@ -586,6 +788,9 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   int* rec_count = rec_list + 2 * kResMaxRec;
   uint64_t* bar = reinterpret_cast<uint64_t*>(rec_count + 4);  // [4], 8-byte aligned
   // bar[0..2]: halo rows of the ring levels; bar[3]: the initial state
+  int* inj = reinterpret_cast<int*>(bar + 4);  // [kResMaxRec] receivers by owner thread
+  int* inj_cnt = inj + kResMaxRec;             // [kResThreads]
+  int* inj_pos = inj_cnt + kResThreads;        // [kResThreads]
 
   const Coef* K = c.coef + (size_t)shot * c.coef_stride;
   const KSr ks{K->k11, K->k22, K->kq12, K->k16, K->k26, K->k66, K->k16h, K->k26h};
@@ -708,6 +913,33 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   };
   int t_last = -1;
 
+  // register-resident form of the adjoint role: the thread's own cells of
+  // the two latest levels (A and B swap roles from one step to the next)
+  constexpr int RCn = RC > 0 ? RC : 1;
+  float Ax[RCn][4], Ay[RCn][4], Bx[RCn][4], By[RCn][4];
+  RegUnit RU;
+  RU.active = false;
+  RU.j = 0;
+  RU.ra = 0;
+  RU.top_ext = RU.bot_ext = false;
+  RU.src_rows = 0u;
+  RU.rmask = 0u;
+  if (RC > 0) {
+    // units of exactly RC rows: thread tid takes column quad tid % (ny / 4)
+    // and rows [RC * (tid / (ny / 4)), + RC); the host launches this form only
+    // when every CTA's rows split into such chunks
+    const int ncq = ny / 4, ch = tid / ncq;
+    RU.j = 4 * (tid - ch * ncq);
+    RU.ra = ch * RCn;
+    RU.active = RU.ra < rows;
+    RU.top_ext = RU.ra == 0;
+    RU.bot_ext = RU.ra + RCn == rows;
+    if (RU.active && !is_fwd) {
+      own_load<RCn>(T, Lv(0), RU, Ax, Ay);  // cur of the first step
+      own_load<RCn>(T, Lv(2), RU, Bx, By);  // prev of the first step
+    }
+  }
+
   if (is_fwd) {
     // ================================================================ FWD role
     const float* sig = c.src_signal + (size_t)shot * c.nt;
@@ -719,7 +951,9 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     const int ck_k = f.ckpt != nullptr ? f.ck_k : 1;
     int c1_r = (f.i0 + 1) % ck_k, c1_q = (f.i0 + 1) / ck_k;
     int c2_r = (f.i0 + 2) % ck_k, c2_q = (f.i0 + 2) / ck_k;
-    for (int i = f.i0; i < f.i1; ++i) {
+    // (the step as a lambda called from one loop: measured 8 % faster on
+    // rot256 than the same body written inline in the loop)
+    auto fwd_step = [&](int i) {
       const int t = i - f.i0;
       set_levels(t);
       expect_next(t);
@@ -767,14 +1001,15 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
           f.tr_y[o] = T.comp(x.nxt, 1)[off];
         }
       }
-    }
+    };
+    for (int i = f.i0; i < f.i1; ++i) fwd_step(i);
   } else {
     // ================================================================ LAM role
     const float gs = c.coef->gscale;  // one scale for every shot
     // residuals of the receivers this thread injects (entries tid + h * kResThreads),
     // loaded one recording step ahead when the launch's frames are not staged
-    // in shared memory (below)
-    constexpr int kRecPerThread = (kResMaxRec + kResThreads - 1) / kResThreads;
+    // in shared memory (below); generic form only
+    constexpr int kRecPerThread = RC > 0 ? 1 : (kResMaxRec + kResThreads - 1) / kResThreads;
     float gnx[kRecPerThread], gny[kRecPerThread];
 #pragma unroll
     for (int h = 0; h < kRecPerThread; ++h) { gnx[h] = 0.f; gny[h] = 0.f; }
@@ -806,8 +1041,55 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
         F[2 * idx + 1] = a.g_y[go];
       }
       __syncthreads();
-    } else if (!DENSE && next_src >= a.m_lo + 1) {
+    } else if (RC == 0 && !DENSE && next_src >= a.m_lo + 1) {
       load_g(next_src);
+    }
+    // Register-resident form: the receivers of this CTA sorted by the thread
+    // that owns their cell (counting sort), so that each owner adds its
+    // cells' residuals to its own registers; entry (cell bit << 16) | e.
+    int inj_beg = 0, inj_end = 0;
+    if (RC > 0 && !DENSE && nloc > 0) {
+      const int ncq = ny / 4;
+      auto owner_of = [&](int e, int& bit) {
+        const int off = rec_list[2 * e];
+        const int s = off / ny, jj = off - s * ny;  // halo row s = local row + 1
+        const int lr = s - 1, ch = lr / RCn;
+        bit = 4 * (lr - ch * RCn) + (jj & 3);
+        return ch * ncq + (jj >> 2);
+      };
+      for (int k = tid; k < kResThreads; k += kResThreads) inj_cnt[k] = 0;
+      __syncthreads();
+      for (int e = tid; e < nloc; e += kResThreads) {
+        int bit;
+        atomicAdd(&inj_cnt[owner_of(e, bit)], 1);
+      }
+      __syncthreads();
+      if (tid == 0) {  // exclusive prefix sum (once per launch)
+        int s = 0;
+        for (int k = 0; k < kResThreads; ++k) {
+          const int v = inj_cnt[k];
+          inj_pos[k] = s;
+          s += v;
+        }
+      }
+      __syncthreads();
+      inj_beg = inj_pos[tid];
+      inj_end = inj_beg + inj_cnt[tid];
+      __syncthreads();
+      for (int e = tid; e < nloc; e += kResThreads) {
+        int bit;
+        const int o = owner_of(e, bit);
+        inj[atomicAdd(&inj_pos[o], 1)] = (bit << 16) | e;
+      }
+      __syncthreads();
+      // each owner sorts its few entries by cell and marks its cells
+      for (int p = inj_beg + 1; p < inj_end; ++p) {
+        const int v = inj[p];
+        int q = p - 1;
+        while (q >= inj_beg && inj[q] > v) { inj[q + 1] = inj[q]; --q; }
+        inj[q + 1] = v;
+      }
+      for (int p = inj_beg; p < inj_end; ++p) RU.rmask |= 1u << (inj[p] >> 16);
     }
     // lam^{m_hi+1} is the imaging partner of u^{m_hi}: store it first
     if (tid == 0 && a.lbuf && a.store_init) {
@@ -819,16 +1101,42 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     Rhs rhs{nullptr, 0.f, 0, nullptr, nullptr, gs};
     // (m - 1) % stride and (m - 1) / stride as counters stepping down with m
     int sm_r = (a.m_hi - 1) % c.stride, sm_q = (a.m_hi - 1) / c.stride;
-    for (int m = a.m_hi; m >= a.m_lo + 1; --m) {
+    auto lam_step = [&](int m, const float (&Cx)[RCn][4], const float (&Cy)[RCn][4], float (&Px)[RCn][4],
+                        float (&Py)[RCn][4]) {
       const int t = a.m_hi - m;  // cur = lam^{m+1}, prev = lam^{m+2}, nxt = lam^m
       set_levels(t);
       expect_next(t);
       const bool src_step = sm_r == 0;
       const int frame = sm_q;
       if (sm_r == 0) { sm_r = c.stride - 1; --sm_q; } else { --sm_r; }
-      if (!DENSE && src_step) {
-        // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: subtract g from the own
-        // copy of lam^{m+2}, which only the owning thread reads this step
+      if (RC > 0 && !DENSE && src_step && RU.rmask != 0u) {
+        // lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g: the owner subtracts g
+        // from its register copy of lam^{m+2} (every receiver of a cell summed)
+        int p = inj_beg;
+#pragma unroll
+        for (int cb = 0; cb < 4 * RCn; ++cb) {
+          if ((RU.rmask >> cb) & 1u) {
+            float gxs = 0.f, gys = 0.f;
+            while (p < inj_end && (inj[p] >> 16) == cb) {
+              const int e = inj[p] & 0xffff;
+              if (staged) {
+                const int si = (frame - f_lo) * nloc + e;
+                gxs += F[2 * si];
+                gys += F[2 * si + 1];
+              } else {
+                const size_t go = ((size_t)shot * c.nt_out + frame) * c.nrec + rec_list[2 * e + 1];
+                gxs += a.g_x[go];
+                gys += a.g_y[go];
+              }
+              ++p;
+            }
+            Px[cb >> 2][cb & 3] += -gs * gxs;
+            Py[cb >> 2][cb & 3] += -gs * gys;
+          }
+        }
+      } else if (RC == 0 && !DENSE && src_step) {
+        // generic form: subtract g from the own copy of lam^{m+2} in shared
+        // memory, which only the owning thread reads this step
 #pragma unroll
         for (int h = 0; h < kRecPerThread; ++h) {
           const int e = tid + h * kResThreads;
@@ -852,7 +1160,12 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
         rhs.gy = a.g_y + ((size_t)shot * c.nt_out + frame) * N + (size_t)r0 * ny;
       }
       const bool w = step_wait(t);
-      ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err, U);
+      if (RC > 0) {
+        if (RU.active)
+          reg_step<true, DENSE, RCn>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err,
+                                     RU, Cx, Cy, Px, Py);
+      } else
+        ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err, U);
       if (w) parity_bits ^= 1u << (t % 3);
       if (tid == 0) bulk_wait_read_all();
       __syncthreads();
@@ -863,6 +1176,16 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
                     (ptrdiff_t)N);
         bulk_commit();
       }
+    };
+    if constexpr (RC > 0) {
+      int m = a.m_hi;
+      for (; m - 1 >= a.m_lo + 1; m -= 2) {
+        lam_step(m, Ax, Ay, Bx, By);      // cur A, prev B -> B holds lam^m
+        lam_step(m - 1, Bx, By, Ax, Ay);  // cur B, prev A -> A holds lam^{m-1}
+      }
+      if (m >= a.m_lo + 1) lam_step(m, Ax, Ay, Bx, By);
+    } else {
+      for (int m = a.m_hi; m >= a.m_lo + 1; --m) lam_step(m, Ax, Ay, Bx, By);
     }
   }
   // The neighbours' last pushes land in this CTA's level of step t_last + 1:
@@ -901,7 +1224,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
 // ---------------------------------------------------------------- host side
 size_t resident_smem_bytes(const ResCommon& c) {
   const size_t level = 2 * (size_t)(c.R + 2) * c.ny * sizeof(float);
-  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 4 * sizeof(uint64_t) + 16;
+  const size_t tail = (2 * kResMaxRec + 4) * sizeof(int) + 4 * sizeof(uint64_t) +
+                      (kResMaxRec + 2 * kResThreads) * sizeof(int) + 16;
   return 3 * level + (size_t)c.R * c.ny * sizeof(float) + tail;
 }
 
@@ -980,8 +1304,32 @@ bool resident_feasible(const ResCommon& c, bool dense) {
   return ok;
 }
 
+// Rows per chunk of the register-resident form for this problem (the same
+// split as unit_of for a CTA of R rows): 1, 2 or 4, or 0 when a thread would
+// hold more than one unit or more than four rows (the generic form runs).
+static int resident_rc(const ResCommon& c) {
+  const int ncq = c.ny / 4;
+  if (ncq < 1 || ncq > kResThreads) return 0;
+  const int nchunk = kResThreads / ncq;
+  const int rc = (c.R + nchunk - 1) / nchunk;
+  // (4-row chunks measured slower in this form than in the generic one:
+  // rot256 adjoint launches 214 vs 161 us)
+  if (rc != 1 && rc != 2) return 0;
+  // every CTA's rows (R, and the last CTA's remainder) in whole chunks
+  const int last = c.nx - (c.CL - 1) * c.R;
+  return (c.R % rc == 0 && last % rc == 0) ? rc : 0;
+}
+
+static const void* resident_fn(bool dense, int rc) {
+  switch (rc) {
+    case 1: return dense ? (const void*)resident_kernel<true, 1> : (const void*)resident_kernel<false, 1>;
+    case 2: return dense ? (const void*)resident_kernel<true, 2> : (const void*)resident_kernel<false, 2>;
+    default: return dense ? (const void*)resident_kernel<true, 0> : (const void*)resident_kernel<false, 0>;
+  }
+}
+
 static bool feasible_uncached(const ResCommon& c, bool dense, size_t smem) {
-  const void* fn = dense ? (const void*)resident_kernel<true> : (const void*)resident_kernel<false>;
+  const void* fn = resident_fn(dense, resident_rc(c));
   if (configure(fn, smem) != cudaSuccess) {
     cudaGetLastError();
     return false;
@@ -1009,7 +1357,8 @@ cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResLam& a
                             bool run_fwd, bool run_lam, bool run_img, bool dense, cudaStream_t st) {
   if (!run_fwd && !run_lam && !run_img) return cudaSuccess;
   const size_t smem = resident_smem_bytes(c);
-  const void* fn = dense ? (const void*)resident_kernel<true> : (const void*)resident_kernel<false>;
+  const int rcf = resident_rc(c);
+  const void* fn = resident_fn(dense, rcf);
   cudaError_t e = configure(fn, smem);
   if (e != cudaSuccess) return e;
   ResRoles roles{-1, -1, -1, 0};
@@ -1040,8 +1389,14 @@ cudaError_t launch_resident(const ResCommon& c, const ResFwd& f, const ResLam& a
                (run_lam ? 24.0 * (a.m_hi - a.m_lo) : 0.0) +   // lam recursion: 3 x 8 B
                (run_img ? 16.0 * (g.n_hi - g.n_lo + 1) : 0.0));  // imaging: read lam, u
   return tracked_launch(cls, st, [&] {
-    if (dense) cudaLaunchKernelEx(&cfg, resident_kernel<true>, c, f, a, g, roles);
-    else cudaLaunchKernelEx(&cfg, resident_kernel<false>, c, f, a, g, roles);
+    switch (rcf * 2 + (dense ? 1 : 0)) {
+      case 2: cudaLaunchKernelEx(&cfg, resident_kernel<false, 1>, c, f, a, g, roles); break;
+      case 3: cudaLaunchKernelEx(&cfg, resident_kernel<true, 1>, c, f, a, g, roles); break;
+      case 4: cudaLaunchKernelEx(&cfg, resident_kernel<false, 2>, c, f, a, g, roles); break;
+      case 5: cudaLaunchKernelEx(&cfg, resident_kernel<true, 2>, c, f, a, g, roles); break;
+      case 1: cudaLaunchKernelEx(&cfg, resident_kernel<true, 0>, c, f, a, g, roles); break;
+      default: cudaLaunchKernelEx(&cfg, resident_kernel<false, 0>, c, f, a, g, roles); break;
+    }
   }, bytes);
 }
 

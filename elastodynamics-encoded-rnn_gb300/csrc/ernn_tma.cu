@@ -316,9 +316,39 @@ __device__ __forceinline__ void leap4(const Coefs& k, const Sums4& s, const floa
   }
 }
 
+// A tile: its state plane (shot), origin, and the instance it belongs to
+// with that instance's region [xs, xe) x [ys, ye) (the shot and the whole
+// grid unless the problem has instances on a canvas).
 struct TileId {
   int shot, x0, y0;
+  int inst, xs, ys, xe, ye;
 };
+
+// The grid's own tile as a TileId of its shot.
+__device__ __forceinline__ TileId grid_tile(TileId id, int nx, int ny) {
+  id.inst = id.shot;
+  id.xs = 0;
+  id.ys = 0;
+  id.xe = nx;
+  id.ye = ny;
+  return id;
+}
+
+// Entry t of an instance tile table (canvas plane 0).
+__device__ __forceinline__ TileId table_tile(const InstTiles& in, int t) {
+  const int4 e = in.tiles[t];
+  const int4 b = in.box[2 * e.x];
+  TileId id;
+  id.shot = 0;
+  id.x0 = e.y;
+  id.y0 = e.z;
+  id.inst = e.x;
+  id.xs = b.x;
+  id.ys = b.y;
+  id.xe = b.z;
+  id.ye = b.w;
+  return id;
+}
 
 // The tiles t = first, first + stride, ... of a CTA, walked in (shot, row
 // block, column block) coordinates: the stride is split once into the same
@@ -339,7 +369,7 @@ struct TileWalk {
     dx = r / ty;
     dy = r - dx * ty;
   }
-  __device__ __forceinline__ TileId id() const { return TileId{shot, xt * TR, yt * kTY}; }
+  __device__ __forceinline__ TileId id() const { return TileId{shot, xt * TR, yt * kTY, shot, 0, 0, 0, 0}; }
   __device__ __forceinline__ void next() {
     yt += dy;
     if (yt >= tiles_y) { yt -= tiles_y; ++xt; }
@@ -401,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
-  const int ntiles = a.S * tiles_x * tiles_y;
+  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(F::kHalo + (has_prev ? F::kOwn : 0)) * 4u;
   grid_dep_trigger();
   __shared__ int done[2];
@@ -423,9 +453,12 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
       const int s = e / a.nrec, r = e - s * a.nrec;
       const int32_t idx = a.rec_idx[e];
       const size_t o = ((size_t)s * a.nt_out + a.gframe) * a.nrec + r;
-      const bool ok = a.cur != nullptr && idx >= 0 && (size_t)idx < N;
-      a.tr_x[o] = ok ? a.cur[(size_t)s * 2 * N + idx] : 0.f;
-      a.tr_y[o] = ok ? a.cur[(size_t)s * 2 * N + N + idx] : 0.f;
+      // instances: one canvas plane; an instance past its last step records zeros
+      const size_t plane = a.inst.tiles ? 0 : (size_t)s * 2 * N;
+      const bool ok = a.cur != nullptr && idx >= 0 && (size_t)idx < N &&
+                      (a.inst.tiles == nullptr || a.i <= a.inst.box[2 * s + 1].z);
+      a.tr_x[o] = ok ? a.cur[plane + idx] : 0.f;
+      a.tr_y[o] = ok ? a.cur[plane + N + idx] : 0.f;
     }
   }
   __syncthreads();
@@ -434,7 +467,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles || pipe_failed(&guard)) return;
     pipe_issued(&guard, k);
-    const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
+    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : tile_of<F::kTR>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
@@ -453,14 +486,14 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = walk.id();
+    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : grid_tile(walk.id(), nx, ny);
     walk.next();
     // per-tile scalars, loaded before the wait (coefficients per shot with
     // per-shot constants)
-    const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
+    const Coef* K = a.coef + (size_t)id.inst * a.coef_stride;
     const Coefs ks = a.coef_stride != 0 ? coefs(K) : ks0;
-    const float amp = a.src_signal[(size_t)id.shot * a.nt + a.i] * K->kappa;
-    const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
+    const float amp = a.src_signal[(size_t)id.inst * a.nt + a.i] * K->kappa;
+    const int ox = has_src ? a.src_origin[2 * id.inst] : 0, oy = has_src ? a.src_origin[2 * id.inst + 1] : 0;
     const int gj = id.y0 + j;
     const int r0 = F::kRT * rg;  // tile row r0 + q2 -> box row r0 + q2 + 1
     float4 w4[F::kRT];
@@ -506,12 +539,12 @@ __global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
         for (int q = 0; q < 4; ++q) {
           const int sb = gj + q - oy;
           if ((unsigned)sb < (unsigned)a.by) {
-            const float f = amp * a.src_map[((size_t)id.shot * a.bx + sa) * a.by + sb];
+            const float f = amp * a.src_map[((size_t)id.inst * a.bx + sa) * a.by + sb];
             if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
           }
         }
       }
-      if (gi < nx && gj < ny) {
+      if (gi < id.xe && gj < id.ye) {
         const float4 nvx = make_float4(vx[0], vx[1], vx[2], vx[3]);
         const float4 nvy = make_float4(vy[0], vy[1], vy[2], vy[3]);
         const size_t o = (size_t)gi * ny + gj;
@@ -595,7 +628,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
-  const int ntiles = a.S * tiles_x * tiles_y;
+  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(F::kCur + (has_prev ? F::kPrev : 0)) * 4u;
   grid_dep_trigger();
   __shared__ int done[2];
@@ -616,7 +649,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles || pipe_failed(&guard)) return;
     pipe_issued(&guard, k);
-    const TileId id = tile_of<F::kTR>(t, tiles_x, tiles_y);
+    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : tile_of<F::kTR>(t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * F::kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
@@ -635,14 +668,14 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = walk.id();
+    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : grid_tile(walk.id(), nx, ny);
     walk.next();
-    const Coef* K = a.coef + (size_t)id.shot * a.coef_stride;
+    const Coef* K = a.coef + (size_t)id.inst * a.coef_stride;
     const Coefs ks = a.coef_stride != 0 ? coefs(K) : ks0;
-    const float* sig = a.src_signal + (size_t)id.shot * a.nt;
+    const float* sig = a.src_signal + (size_t)id.inst * a.nt;
     const float amp1 = sig[a.i] * K->kappa, amp2 = sig[a.i + 1] * K->kappa;
-    const int ox = has_src ? a.src_origin[2 * id.shot] : 0, oy = has_src ? a.src_origin[2 * id.shot + 1] : 0;
-    const float* smap = has_src ? a.src_map + (size_t)id.shot * a.bx * a.by : nullptr;
+    const int ox = has_src ? a.src_origin[2 * id.inst] : 0, oy = has_src ? a.src_origin[2 * id.inst + 1] : 0;
+    const float* smap = has_src ? a.src_map + (size_t)id.inst * a.bx * a.by : nullptr;
     bar_wait_ok(&bar[k & 1], (uint32_t)(k >> 1) & 1u, err, &guard);
     const float* cb = sm + (k & 1) * F::kStage;           // u^i: rows -2 .. kTR+1
     const float* pb = cb + F::kCur;                        // u^{i-1}: rows -1 .. kTR
@@ -675,7 +708,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
         pvy = *reinterpret_cast<const float4*>(pb + F::kBH1 * kBW + m * kBW + b);
       }
       const int gi = id.x0 + m - 1, gj = id.y0 - 4 + b;  // ny % 4 == 0: a quad is in or out
-      const bool inside = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+      const bool inside = gi >= id.xs && gi < id.xe && gj >= id.ys && gj < id.ye;
       float vx[4], vy[4];
       leap4<false>(ks, st, st.cx, st.cy, pvx, pvy, pvx, vx, vy);
 #pragma unroll
@@ -734,7 +767,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
           }
         }
       }
-      if (gi < nx && gj < ny) {
+      if (gi < id.xe && gj < id.ye) {
         const size_t o = (size_t)gi * ny + gj;
         *reinterpret_cast<float4*>(out2 + o) = make_float4(vx[0], vx[1], vx[2], vx[3]);
         *reinterpret_cast<float4*>(out2 + N + o) = make_float4(vy[0], vy[1], vy[2], vy[3]);
@@ -794,7 +827,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
-  const int ntiles = a.S * tiles_x * tiles_y;
+  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(MODE == kModeScalar
                                         ? L::kHalo + L::kOwn + (has_u ? L::kOwn : 0)
                                         : L::kHalo + L::kBHa * kBW + (has_u ? L::kHalo : 0)) * 4u;
@@ -829,7 +862,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     const int t = t_first + k * t_step;
     if (t >= t_end || pipe_failed(&guard)) return;
     pipe_issued(&guard, k);
-    const TileId id = tile_of<L::kTR>(t, tiles_x, tiles_y);
+    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : tile_of<L::kTR>(t, tiles_x, tiles_y);
     const int sg = k % NS;
     float* st = sm + sg * L::kStage;
     fence_async();
@@ -898,13 +931,13 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
   for (int k = 0;; ++k) {
     const int t = t_first + k * t_step;
     if (t >= t_end) break;
-    const TileId id = walk.id();
+    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : grid_tile(walk.id(), nx, ny);
     walk.next();
-    if (MODE == kModeScalar && per_shot && has_u && id.shot != acc_shot) {
+    if (MODE == kModeScalar && per_shot && has_u && id.inst != acc_shot) {
       if (acc_shot >= 0) flush(acc_shot);
-      acc_shot = id.shot;
+      acc_shot = id.inst;
     }
-    const Coefs ks = per_shot ? coefs(a.coef + (size_t)id.shot * a.coef_stride) : ks0;
+    const Coefs ks = per_shot ? coefs(a.coef + (size_t)id.inst * a.coef_stride) : ks0;
     const int gj = id.y0 + j;
     const int r0 = L::kRT * rg;
     // receivers in this tile (uniform over the CTA): the injection and its
@@ -931,11 +964,11 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
     // tile's copy of lam^{m+2} (lam^m = ... - lam^{m+2} + ... + g)
     if (MODE == kModeScalar && tile_inject) {
       for (int rr = tid; rr < a.nrec; rr += kThreads) {
-        const int32_t idx = a.rec_idx[(size_t)id.shot * a.nrec + rr];
+        const int32_t idx = a.rec_idx[(size_t)id.inst * a.nrec + rr];
         if (idx < 0 || (size_t)idx >= N) continue;
         const int gi = idx / ny, gjj = idx - gi * ny;
         if (gi >= id.x0 && gi < id.x0 + L::kTR && gjj >= id.y0 && gjj < id.y0 + kTY) {
-          const size_t go = ((size_t)id.shot * a.nt_out + a.frame) * a.nrec + rr;
+          const size_t go = ((size_t)id.inst * a.nt_out + a.frame) * a.nrec + rr;
           atomicAdd(&pb[(gi - id.x0) * kTY + (gjj - id.y0)], -gs * a.g_x[go]);
           atomicAdd(&pb[L::kTR * kTY + (gi - id.x0) * kTY + (gjj - id.y0)], -gs * a.g_y[go]);
         }
@@ -975,7 +1008,9 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       Sums4 st;
       sums4(wx, wy, st);
       const int gi = id.x0 + r;
-      const bool in = gi < nx && gj < ny;
+      // the cells of the tile inside its instance's region (the whole grid
+      // without instances; ny % 4 == 0: a quad is in or out)
+      const bool in = gi < id.xe && gj < id.ye;
       // unweighted lam^{m+1} at the 4 cells (zero outside the grid, so the
       // imaging products of those cells vanish without a guard)
       float c1x[4], c1y[4];
@@ -1021,8 +1056,11 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
       }
       if (MODE == kModeScalar && has_u) {
         // transposed imaging: u^m at the cell times the stencils of lam^{m+1}
-        const float4 u4x = *reinterpret_cast<const float4*>(ub + r * kTY + j);
-        const float4 u4y = *reinterpret_cast<const float4*>(ub + L::kTR * kTY + r * kTY + j);
+        // (cells of a tile beyond its instance's region take no part: on a
+        // canvas they may hold another instance's state)
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 u4x = in ? *reinterpret_cast<const float4*>(ub + r * kTY + j) : zero4;
+        const float4 u4y = in ? *reinterpret_cast<const float4*>(ub + L::kTR * kTY + r * kTY + j) : zero4;
 #pragma unroll
         for (int p = 0; p < 2; ++p) {  // each sum as a chain of fused multiply-adds, two cells per op
           const float2 ux = pair4(u4x, p), uy = pair4(u4y, p);
@@ -1219,6 +1257,53 @@ cudaError_t launch_tile_flags(int mode, const int32_t* rec_idx, int S, int nrec,
   });
 }
 
+namespace {
+// Block b writes the tiles of instance d.id[b] (entry base[b] + xt * tiles_y
+// + yt for the tile at rows x0 + 16 xt, columns y0 + 64 yt) and its box.
+__global__ void inst_table_kernel(const InstDesc d, int4* __restrict__ tiles, int4* __restrict__ box) {
+  const int b = blockIdx.x;
+  const int k = d.id[b];
+  const int tiles_y = (d.ny[b] + 63) / 64;
+  const int n = inst_tiles(d.nx[b], d.ny[b]);
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const int xt = t / tiles_y, yt = t - xt * tiles_y;
+    tiles[d.base[b] + t] = make_int4(k, d.x0[b] + kInstTileRows * xt, d.y0[b] + 64 * yt, 0);
+  }
+  if (threadIdx.x == 0) {
+    box[2 * k] = make_int4(d.x0[b], d.y0[b], d.x0[b] + d.nx[b], d.y0[b] + d.ny[b]);
+    box[2 * k + 1] = make_int4(d.base[b], tiles_y, d.nt[b], 0);
+  }
+}
+
+__global__ void inst_tile_flags_kernel(const int32_t* __restrict__ rec_idx, int S, int nrec, int ny,
+                                       const int4* __restrict__ box, uint8_t* __restrict__ flags) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= S * nrec) return;
+  const int s = e / nrec;
+  const int32_t idx = rec_idx[e];
+  if (idx < 0) return;
+  const int gi = idx / ny, gj = idx - gi * ny;
+  const int4 r = box[2 * s], m = box[2 * s + 1];
+  if (gi < r.x || gi >= r.z || gj < r.y || gj >= r.w) return;
+  flags[m.x + ((gi - r.x) / kInstTileRows) * m.y + (gj - r.y) / 64] = 1;
+}
+}  // namespace
+
+cudaError_t launch_inst_table(const InstDesc& d, int4* tiles, int4* box, cudaStream_t st) {
+  if (d.count < 1) return cudaSuccess;
+  return tracked_launch(kProfOther, st, [&] { inst_table_kernel<<<d.count, 256, 0, st>>>(d, tiles, box); });
+}
+
+cudaError_t launch_inst_tile_flags(const int32_t* rec_idx, int S, int nrec, int ny, const int4* box,
+                                   uint8_t* flags, int ntiles, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)ntiles, st);
+  if (e != cudaSuccess) return e;
+  const int n = S * nrec;
+  return tracked_launch(kProfOther, st, [&] {
+    inst_tile_flags_kernel<<<(n + 255) / 256, 256, 0, st>>>(rec_idx, S, nrec, ny, box, flags);
+  });
+}
+
 bool tma_eligible(int mode, int nx, int ny, int S) {
   (void)nx;
   (void)S;
@@ -1256,13 +1341,14 @@ bool tma_fwd2_would_run(int mode, const FwdStep& a) {
 cudaError_t launch_tma_fwd2(int mode, const FwdStep& a, int* err, cudaStream_t st) {
   using F = Fwd2Layout;
   CUtensorMap cur_map, prev_map;
-  if (!tma_fwd2_would_run(mode, a) || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, F::kBH2) ||
-      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, a.S, kBW, F::kBH1))
+  const int planes = a.inst.tiles ? 1 : a.S;  // instances share one canvas plane
+  if (!tma_fwd2_would_run(mode, a) || !make_map(&cur_map, a.cur, a.nx, a.ny, planes, kBW, F::kBH2) ||
+      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, planes, kBW, F::kBH1))
     return cudaErrorNotSupported;
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + F::kTR - 1) / F::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
-  const int ntiles = a.S * tiles_x * tiles_y;
+  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   int grid = num_sms() * F::kCtasPerSm;
   if (grid > ntiles) grid = ntiles;
   const int hp = a.prev ? 1 : 0;
@@ -1270,7 +1356,7 @@ cudaError_t launch_tma_fwd2(int mode, const FwdStep& a, int* err, cudaStream_t s
   return tracked_launch(kProfForward, st, [&] {
     launch_step_kernel(tma_fwd2_kernel<kModeScalar>, dim3(grid), dim3(kThreads), kFwd2Smem, st, chained, a,
                        cur_map, prev_map, tiles_x, tiles_y, hp, err);
-  }, 2.0 * (double)a.S * a.nx * a.ny * 16.0);
+  }, 2.0 * (a.inst.tiles ? (double)a.inst.ntiles * F::kTR * kTY : (double)a.S * a.nx * a.ny) * 16.0);
 }
 
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st) {
@@ -1278,16 +1364,17 @@ cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st
                   a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) && al16(a.copy0) &&
                   al16(a.copy1) && (a.frame < 0 || (al16(a.hist_x) && al16(a.hist_y)));
   CUtensorMap cur_map, prev_map;
-  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, a.S, kBW, FwdLayout::kBHa) ||
-      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, a.S, kTY, FwdLayout::kTR))
-    return launch_fwd_step(mode, a, st);
+  const int planes = a.inst.tiles ? 1 : a.S;  // instances share one canvas plane
+  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, planes, kBW, FwdLayout::kBHa) ||
+      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, planes, kTY, FwdLayout::kTR))
+    return a.inst.tiles ? cudaErrorNotSupported : launch_fwd_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + FwdLayout::kTR - 1) / FwdLayout::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
-  const int ntiles = a.S * tiles_x * tiles_y;
+  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   int grid = num_sms() * FwdLayout::kCtasPerSm;
   if (grid > ntiles) grid = ntiles;
-  const double cells = (double)a.S * a.nx * a.ny;
+  const double cells = a.inst.tiles ? (double)a.inst.ntiles * FwdLayout::kTR * kTY : (double)a.S * a.nx * a.ny;
   const int hp = a.prev ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfForward, st, [&] {
@@ -1308,9 +1395,10 @@ bool adj_maps(int mode, const AdjStep& a, CUtensorMap* cur_map, CUtensorMap* pre
                   a.cur != nullptr && a.prev != nullptr && al16(a.cur) && al16(a.prev) && al16(a.out) &&
                   al16(a.u) && (a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
   const int tr = tma_adj_tile_rows(mode), bh = tr + 2;
-  return ok && make_map(cur_map, a.cur, a.nx, a.ny, a.S, kBW, bh) &&
-         make_map(prev_map, a.prev, a.nx, a.ny, a.S, kTY, tr) &&
-         make_map(u_map, a.u ? a.u : a.cur, a.nx, a.ny, a.S, dfield ? kBW : kTY, dfield ? bh : tr) &&
+  const int planes = a.inst.tiles ? 1 : a.S;  // instances share one canvas plane
+  return ok && make_map(cur_map, a.cur, a.nx, a.ny, planes, kBW, bh) &&
+         make_map(prev_map, a.prev, a.nx, a.ny, planes, kTY, tr) &&
+         make_map(u_map, a.u ? a.u : a.cur, a.nx, a.ny, planes, dfield ? kBW : kTY, dfield ? bh : tr) &&
          make_map2(d_map, dfield ? a.field : a.cur, a.nx, a.ny, kBW, bh);
 }
 }  // namespace
@@ -1323,16 +1411,17 @@ bool tma_adj_would_run(int mode, const AdjStep& a) {
 cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st) {
   const bool dfield = mode == kModeDField;
   CUtensorMap cur_map, prev_map, u_map, d_map;
-  if (!adj_maps(mode, a, &cur_map, &prev_map, &u_map, &d_map)) return launch_adj_step(mode, a, st);
+  if (!adj_maps(mode, a, &cur_map, &prev_map, &u_map, &d_map))
+    return a.inst.tiles ? cudaErrorNotSupported : launch_adj_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tr = tma_adj_tile_rows(mode);
   const int tiles_x = (a.nx + tr - 1) / tr, tiles_y = (a.ny + kTY - 1) / kTY;
-  const int ntiles = a.S * tiles_x * tiles_y;
+  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   int grid = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm : AdjLayout<kModeScalar>::kCtasPerSm);
   if (grid > ntiles) grid = ntiles;
   if (grid > kTiledRowsPerShot) grid = kTiledRowsPerShot;
-  const double cells = (double)a.S * a.nx * a.ny;
+  const double cells = a.inst.tiles ? (double)a.inst.ntiles * tr * kTY : (double)a.S * a.nx * a.ny;
   const int hu = a.u ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfAdjoint, st, [&] {

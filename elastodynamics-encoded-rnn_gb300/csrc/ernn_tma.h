@@ -1,5 +1,5 @@
 // Tiled per-step kernels (ernn_tma.cu): one launch per time step, persistent
-// CTAs streaming 64 x 32 tiles through TMA loads.  Internal to the library.
+// CTAs streaming 64-column tiles through TMA loads.  Internal to the library.
 #pragma once
 
 #include "ernn_launch.h"
@@ -34,6 +34,28 @@ bool tma_adj_would_run(int mode, const AdjStep& a);
 // (tma_tiles(nx, ny, S, tma_adj_tile_rows(mode)) bytes at `flags`).
 cudaError_t launch_tile_flags(int mode, const int32_t* rec_idx, int S, int nrec, int nx, int ny,
                               uint8_t* flags, cudaStream_t st);
+// Instances on a canvas (ERNN_FLAG_INSTANCES).  The instance table passed
+// by value to the kernel that writes the tile table: instances in the order
+// of decreasing step count, each with its caller-side index.
+constexpr int kMaxInstances = 256;
+constexpr int kInstTileRows = 16;  // tile rows of every instance kernel (scalar constants)
+struct InstDesc {
+  int count;
+  int id[kMaxInstances], x0[kMaxInstances], y0[kMaxInstances], nx[kMaxInstances];
+  int ny[kMaxInstances], nt[kMaxInstances], base[kMaxInstances];
+};
+// Tiles of one instance of nx x ny cells.
+__host__ __device__ inline int inst_tiles(int nx, int ny) {
+  return ((nx + kInstTileRows - 1) / kInstTileRows) * ((ny + 63) / 64);
+}
+// Writes the tile table (sum of inst_tiles entries, in the order of d) and
+// the per-instance boxes (2 x S int4) described in InstTiles.
+cudaError_t launch_inst_table(const InstDesc& d, int4* tiles, int4* box, cudaStream_t st);
+// Receiver table of the instance tile table: flags[t] = 1 where the tile's
+// instance has a receiver in it (ntiles bytes).
+cudaError_t launch_inst_tile_flags(const int32_t* rec_idx, int S, int nrec, int ny, const int4* box,
+                                   uint8_t* flags, int ntiles, cudaStream_t st);
+
 // Runs one bounded wait that cannot complete and copies the error word it
 // records into *status_host; synchronises `st`.
 cudaError_t wait_selftest(int* status_host, cudaStream_t st);

@@ -159,7 +159,14 @@ class Inversion(_GraphedIteration):
 
 class DamageInversion(_GraphedIteration):
     """One inversion iteration of the degradation-map workload: D(x) trained by
-    Adam with C(x) = (1 - D(x)) C0 (initial guess D = 0)."""
+    Adam with C(x) = (1 - D(x)) C0 (initial guess D = 0).
+
+    The objective is the trace MSE divided by its value at the initial guess
+    (a fixed factor, one pass of the same fused misfit).  The plain MSE of
+    these displacements is about 1e-11 and its gradient per cell about
+    1e-13, far below Adam's eps = 1e-8: Adam would then move D by a few
+    millionths of lr per step.  Normalised, the objective starts at 1 and
+    the steps are of order lr, as for the scalar constants."""
 
     def __init__(self, w: Workload, device, lr=1e-2, seed=0, nt=None, graph=False):
         if w.D_true is None:
@@ -172,6 +179,9 @@ class DamageInversion(_GraphedIteration):
         self.C0 = torch.tensor(w.C_true, dtype=torch.float32, device=device)
         self.D = torch.nn.Parameter(torch.zeros((w.nx, w.ny), device=device))
         self.opt = FusedAdam([self.D], lr=lr)
+        with torch.no_grad():
+            ux, uy = propagate(self.C0, self.rho, self.geom, D=self.D.detach())
+            self.loss_scale = float(1.0 / trace_misfit(ux, uy, self.obs[0], self.obs[1]))
         if graph:
             self.capture()
 
@@ -179,7 +189,7 @@ class DamageInversion(_GraphedIteration):
         obs = self.obs
         self.opt.zero_grad(set_to_none=False)
         ux, uy = propagate(self.C0, self.rho, self.geom, D=self.D)
-        loss = trace_misfit(ux, uy, obs[0], obs[1])
+        loss = series_misfit(ux, uy, obs[0], obs[1], self.loss_scale, self.loss_scale)
         loss.backward()
         self.opt.step()
         return loss
@@ -432,3 +442,125 @@ class MultiInversion:
 
     def relative_errors(self):
         return np.stack([inv.relative_errors() for inv in self.invs])
+
+
+def canvas_layout(ws, gap_rows=1, gap_cols=4):
+    """Shelf packing of the instances' grids on one canvas: largest first,
+    shelves of the canvas width (about square overall), regions gap_rows
+    rows and gap_cols columns apart (the cells between them stay zero: the
+    instances' ghost rings).  Returns (X, Y, x0, y0) with x0, y0 per
+    instance in the order of `ws`."""
+    area = sum((w.nx + gap_rows) * (w.ny + gap_cols) for w in ws)
+    width = max(max(w.ny for w in ws) + gap_cols, int(np.ceil(np.sqrt(area) / 64.0)) * 64)
+    order = sorted(range(len(ws)), key=lambda k: (-ws[k].nx, -ws[k].ny, k))
+    x0, y0 = [0] * len(ws), [0] * len(ws)
+    shelf_x, shelf_h, col = 0, 0, 0
+    for k in order:
+        w = ws[k]
+        if col + w.ny > width:
+            shelf_x += shelf_h + gap_rows
+            shelf_h, col = 0, 0
+        x0[k], y0[k] = shelf_x, col
+        col += w.ny + gap_cols
+        shelf_h = max(shelf_h, w.nx)
+    X = shelf_x + shelf_h
+    Y = width
+    return X, Y, x0, y0
+
+
+class CanvasInversion(_GraphedIteration):
+    """Many independent scalar-constant inversions of uneven grid sizes and
+    step counts advanced as ONE propagation: the instances are regions of a
+    canvas (canvas_layout) and every time step is one launch of the tiled
+    kernels over the table of all running instances' tiles (instances drop
+    out of the table as their step counts end); each instance keeps its own
+    constants, source, receivers, observations and gradient; one fused Adam
+    launch updates every instance; the whole iteration is one CUDA graph.
+
+    Traces are (S, max nt_out, R), zero past each instance's own frames (the
+    observations likewise), and the objective is S times their mean square
+    residual: the sum of the instances' misfits up to a factor per instance
+    that Adam's per-parameter step normalisation ignores."""
+
+    def __init__(self, ws, device, lr=1e-2, seed=0, graph=True, nt=None):
+        from .propagate import Instances, choose_ckpt_k
+        self.ws = ws
+        self.device = device
+        S = len(ws)
+        nts = [w.nt if nt is None else min(w.nt, nt) for w in ws]
+        X, Y, x0, y0 = canvas_layout(ws)
+        self.canvas = (X, Y)
+        self.x0, self.y0, self.nts = x0, y0, nts
+        nt_max = max(nts)
+        sig = np.zeros((S, nt_max), np.float32)
+        maps, origins = [], []
+        for k, w in enumerate(ws):
+            sig[k, :nts[k]] = sources.hann_burst_signal(nts[k], DT, w.f0, 5, w.amplitude).astype(np.float32)
+            (si, sj), = w.src_cells
+            dense = sources.point_load_maps(w.nx, w.ny, H, [sources.cell_position(si, sj, w.nx, w.ny, H)],
+                                            w.gaussian_param, device=device)
+            m, o = sources.crop_box(dense)
+            maps.append(m[0])
+            origins.append((int(o[0, 0]) + x0[k], int(o[0, 1]) + y0[k]))
+        bx = max(m.shape[0] for m in maps)
+        by = max(m.shape[1] for m in maps)
+        smap = torch.zeros((S, bx, by), dtype=torch.float32, device=device)
+        for k, m in enumerate(maps):
+            smap[k, :m.shape[0], :m.shape[1]] = m
+        nrec = len(ws[0].rec_cells)
+        if any(len(w.rec_cells) != nrec for w in ws):
+            raise ValueError("every instance needs the same number of receivers")
+        rec = torch.tensor([[(x0[k] + i) * Y + (y0[k] + j) for (i, j) in w.rec_cells]
+                            for k, w in enumerate(ws)], dtype=torch.int32, device=device)
+        inst = Instances(x0, y0, [w.nx for w in ws], [w.ny for w in ws], nts)
+        self.geom = Geometry(nx=X, ny=Y, nt=nt_max, h=H, dt=DT, src_signal=torch.tensor(sig, device=device),
+                             src_map=smap, src_origin=torch.tensor(origins, dtype=torch.int32, device=device),
+                             stride=1, src_comp=1, rec_idx=rec, instances=inst)
+        from ._lib import FLAG_INSTANCES
+        self.geom.ckpt_k = choose_ckpt_k(self.geom, 0, device, flags=FLAG_INSTANCES)
+        self.rho = torch.full((S,), RHO, dtype=torch.float32, device=device)
+        # observations: the same propagation at the true constants plus
+        # Gaussian noise of 0.5 % of each instance's trace RMS (seeded)
+        Ct = torch.tensor(np.stack([w.C_true for w in ws]), dtype=torch.float32, device=device)
+        with torch.no_grad():
+            ox, oy = propagate(Ct, self.rho, self.geom)
+        g = torch.Generator(device=device).manual_seed(seed)
+        self.obs = []
+        for o in (ox, oy):
+            rms = o.double().pow(2).mean(dim=(1, 2), keepdim=True).sqrt().float()
+            noisy = o + 0.005 * rms * torch.randn(o.shape, generator=g, device=device)
+            valid = torch.zeros_like(o)
+            for k in range(S):
+                valid[k, :nts[k]] = 1.0
+            self.obs.append((noisy * valid).contiguous())
+        C0 = np.stack([initial_guess(w, seed + k) for k, w in enumerate(ws)])
+        sc = np.stack([scales(w.C_true) for w in ws])
+        self.scale = torch.tensor(sc, dtype=torch.float32, device=device)
+        self.theta = torch.nn.Parameter(torch.tensor(C0 / sc, dtype=torch.float32, device=device))
+        self.opt = FusedAdam([self.theta], lr=lr)
+        self.cell_steps = sum(w.nx * w.ny * n for w, n in zip(ws, nts))
+        if graph:
+            self.capture()
+
+    def params(self):
+        return self.theta * self.scale
+
+    def step_eager(self):
+        obs = self.obs
+        self.opt.zero_grad(set_to_none=False)
+        ux, uy = propagate(self.params(), self.rho, self.geom)
+        S = float(len(self.ws))
+        loss = series_misfit(ux, uy, obs[0], obs[1], S, S)
+        loss.backward()
+        self.opt.step()
+        return loss
+
+    def forward_only(self):
+        with torch.no_grad():
+            return propagate(self.params().detach(), self.rho, self.geom)
+
+    def gradient(self):
+        return self.theta.grad.reshape(-1)
+
+    def constants(self):
+        return self.params().detach().double().cpu().numpy()

@@ -29,6 +29,33 @@ def _stream():
 
 
 @dataclass
+class Instances:
+    """Independent instances on one canvas: instance k occupies rows
+    [x0[k], x0[k] + nx[k]) and columns [y0[k], y0[k] + ny[k]) of the canvas
+    grid and runs nt[k] steps (y0 and ny multiples of 4, regions at least one
+    cell apart).  With it a Geometry's grid is the canvas, its shots are the
+    instances (sources and receivers in canvas cells), nt is max(nt) and the
+    constants are (S, 6) with rho (S,)."""
+    x0: list
+    y0: list
+    nx: list
+    ny: list
+    nt: list
+
+    def __post_init__(self):
+        self._arrays = [(ctypes.c_int32 * len(v))(*[int(x) for x in v])
+                        for v in (self.x0, self.y0, self.nx, self.ny, self.nt)]
+
+    @property
+    def count(self) -> int:
+        return len(self.nt)
+
+    def c_struct(self) -> _lib.ErnnInstances:
+        P = ctypes.POINTER(ctypes.c_int32)
+        return _lib.ErnnInstances(self.count, *[ctypes.cast(a, P) for a in self._arrays])
+
+
+@dataclass
 class Geometry:
     """Static description of one propagation: grid, time axis, sources, receivers.
 
@@ -55,6 +82,7 @@ class Geometry:
     rec_idx: torch.Tensor | None = None
     ckpt_k: int | None = None
     path: int = _lib.PATH_AUTO
+    instances: Instances | None = None
     _checked: bool = field(default=False, repr=False)
 
     @property
@@ -106,7 +134,10 @@ class Geometry:
             lo, hi = int(r.min()), int(r.max())
             if lo < 0 or hi >= self.nx * self.ny:
                 raise ValueError("receiver index outside the grid")
-        rc = _lib.load().ernn_validate(ctypes.byref(self.problem(MODE_SCALAR)))
+        if self.instances is not None and self.instances.count != S:
+            raise ValueError("one instance per shot")
+        flags = _lib.FLAG_INSTANCES if self.instances is not None else 0
+        rc = _lib.load().ernn_validate(ctypes.byref(self.problem(MODE_SCALAR, flags)))
         _lib.check("ernn_validate", rc)
         self._checked = True
 
@@ -224,7 +255,10 @@ class ErnnPropagate(torch.autograd.Function):
         dev = C.device
         per_shot = D is None and C.dim() == 2 and C.shape[-1] == 6
         mode = MODE_SCALAR if per_shot else _mode_of(C, D)
-        flags = _lib.FLAG_SHOT_CONSTANTS if per_shot else 0
+        inst = geom.instances
+        if inst is not None and not per_shot:
+            raise ValueError("instances take (S, 6) constants with rho (S,)")
+        flags = _lib.FLAG_INSTANCES if inst is not None else (_lib.FLAG_SHOT_CONSTANTS if per_shot else 0)
         C = C.detach().to(torch.float32).contiguous()
         D = None if D is None else D.detach().to(torch.float32).contiguous()
         rho = rho.detach().to(torch.float32).reshape(-1).contiguous()
@@ -252,10 +286,17 @@ class ErnnPropagate(torch.autograd.Function):
             out_ux = torch.empty(geom.out_shape(), dtype=torch.float32, device=dev)
             out_uy = torch.empty(geom.out_shape(), dtype=torch.float32, device=dev)
             ins = _inputs(geom, C, D, rho)
-            rc = lib.ernn_forward(ctypes.byref(prob), ctypes.byref(ins), _ptr(out_ux),
-                                  _ptr(out_uy), _ptr(tape), ctypes.c_size_t(tape_bytes),
-                                  int(want_grad), _stream())
-            _lib.check("ernn_forward", rc)
+            if inst is not None:
+                ist = inst.c_struct()
+                rc = lib.ernn_forward_instances(ctypes.byref(prob), ctypes.byref(ins), ctypes.byref(ist),
+                                                _ptr(out_ux), _ptr(out_uy), _ptr(tape),
+                                                ctypes.c_size_t(tape_bytes), int(want_grad), _stream())
+                _lib.check("ernn_forward_instances", rc)
+            else:
+                rc = lib.ernn_forward(ctypes.byref(prob), ctypes.byref(ins), _ptr(out_ux),
+                                      _ptr(out_uy), _ptr(tape), ctypes.c_size_t(tape_bytes),
+                                      int(want_grad), _stream())
+                _lib.check("ernn_forward", rc)
             _STATUS.enqueue("ernn_forward", prob, tape, 0)
         ctx.geom = geom
         ctx.mode = mode
@@ -288,11 +329,19 @@ class ErnnPropagate(torch.autograd.Function):
             else:
                 grad_field = None
             ins = _inputs(geom, C, D, rho)
-            rc = lib.ernn_adjoint(ctypes.byref(prob), ctypes.byref(ins), _ptr(g_ux), _ptr(g_uy),
-                                  _ptr(ctx.tape), ctypes.c_size_t(ctx.tape.numel()),
-                                  _ptr(scratch), ctypes.c_size_t(scratch_bytes), _ptr(grad_C64),
-                                  _ptr(grad_field), _stream())
-            _lib.check("ernn_adjoint", rc)
+            if geom.instances is not None:
+                ist = geom.instances.c_struct()
+                rc = lib.ernn_adjoint_instances(ctypes.byref(prob), ctypes.byref(ins), ctypes.byref(ist),
+                                                _ptr(g_ux), _ptr(g_uy), _ptr(ctx.tape),
+                                                ctypes.c_size_t(ctx.tape.numel()), _ptr(scratch),
+                                                ctypes.c_size_t(scratch_bytes), _ptr(grad_C64), _stream())
+                _lib.check("ernn_adjoint_instances", rc)
+            else:
+                rc = lib.ernn_adjoint(ctypes.byref(prob), ctypes.byref(ins), _ptr(g_ux), _ptr(g_uy),
+                                      _ptr(ctx.tape), ctypes.c_size_t(ctx.tape.numel()),
+                                      _ptr(scratch), ctypes.c_size_t(scratch_bytes), _ptr(grad_C64),
+                                      _ptr(grad_field), _stream())
+                _lib.check("ernn_adjoint", rc)
             _STATUS.enqueue("ernn_adjoint", prob, scratch, 1)
         if mode == MODE_SCALAR:
             return grad_C64.to(torch.float32), None, None, None, None

@@ -74,7 +74,16 @@ enum {
   /* SCALAR mode: every shot has its own constants and density — C is
    * nshots x 6, rho nshots, grad_C nshots x 6 — so independent inversions
    * of one grid size and step count advance in the same launches */
-  ERNN_FLAG_SHOT_CONSTANTS = 1
+  ERNN_FLAG_SHOT_CONSTANTS = 1,
+  /* Independent instances of uneven grid sizes and step counts on one
+   * canvas (ernn_forward_instances / ernn_adjoint_instances): nx x ny is the
+   * canvas, holding ONE state plane; nshots is the number of instances, each
+   * a rectangular region of the canvas with its own constants (C nshots x 6,
+   * rho nshots, as ERNN_FLAG_SHOT_CONSTANTS), source (src_signal nshots x nt,
+   * src_map, src_origin in canvas cells), receivers (rec_idx: canvas cell
+   * indices) and step count; nt is the largest step count.  SCALAR mode,
+   * RECORD_RECEIVERS, tiled kernels (ERNN_PATH_AUTO or _TILED). */
+  ERNN_FLAG_INSTANCES = 2
 };
 
 /* One propagation problem.  Plain data; identical layout in C, C++, ctypes. */
@@ -185,6 +194,42 @@ int ernn_adjoint(const ErnnProblem* p, const ErnnInputs* in, const float* g_ux,
  * No counterpart in the reference. */
 int ernn_forward_static(const ErnnProblem* p, const ErnnInputs* in, float* out_ux, float* out_uy,
                         void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Many independent inversions of uneven grid sizes and step counts advancing
+ * in one launch sequence (a problem with ERNN_FLAG_INSTANCES).  The caller
+ * places each instance in a region of the canvas: regions at least one row
+ * and four columns apart (the cells between them, never written, are the
+ * instances' zero ghost rings), y0 and ny multiples of 4.  Every time step is
+ * one launch over a table of all instances' 64 x 16 tiles, ordered by step
+ * count, of which a step takes the prefix of instances still running: an
+ * instance with nt_k steps takes part in forward steps i < nt_k and adjoint
+ * steps m <= nt_k, on the same time axis, so checkpoint segments are shared.
+ * Instance k's trace frames beyond its own ceil(nt_k / stride) are zero.
+ * The reference runs one inversion per loop (batch of one,
+ * Parameter_inversion/Inversion_adam.py:252); no counterpart there. */
+#define ERNN_MAX_INSTANCES 256
+
+typedef struct ErnnInstances {
+  int32_t count;        /* instances: the problem's nshots (<= ERNN_MAX_INSTANCES) */
+  const int32_t* x0;    /* host: count first rows of the regions */
+  const int32_t* y0;    /* host: count first columns (multiples of 4) */
+  const int32_t* nx;    /* host: count region rows */
+  const int32_t* ny;    /* host: count region columns (multiples of 4) */
+  const int32_t* nt;    /* host: count step counts, 1 .. problem nt */
+} ErnnInstances;
+
+/* Forward time loop of every instance (tape: ernn_tape_bytes of the canvas
+ * problem).  Outputs: traces (nshots, nt_out, nrec) per component. */
+int ernn_forward_instances(const ErnnProblem* p, const ErnnInputs* in, const ErnnInstances* inst,
+                           float* out_ux, float* out_uy, void* tape, size_t tape_bytes, int with_tape,
+                           void* stream);
+
+/* Adjoint of every instance: grad_C nshots x 6 (each instance's constants),
+ * FP64 sums over its cells and steps. */
+int ernn_adjoint_instances(const ErnnProblem* p, const ErnnInputs* in, const ErnnInstances* inst,
+                           const float* g_ux, const float* g_uy, const void* tape, size_t tape_bytes,
+                           void* scratch, size_t scratch_bytes, double* grad_C, void* stream);
 
 /* ---------------------------------------------------------------------------
  * FEM data generator (the step before the ERNN path): the explicit

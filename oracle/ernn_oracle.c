@@ -26,6 +26,8 @@
 #define ORACLE_RECORD_RECEIVERS 1
 #define ORACLE_ERR_INVALID 1
 #define ORACLE_ERR_ALLOC 2
+/* fixed chunks of the imaging sums (order independent of the thread count) */
+#define ORACLE_CHUNKS 64
 
 /* Problem description; mirrors the fields of ErnnProblem that the oracle needs. */
 typedef struct {

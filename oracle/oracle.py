@@ -154,6 +154,60 @@ def adjoint(case: Case, states: np.ndarray, g_ux: np.ndarray, g_uy: np.ndarray,
     return gC, gD
 
 
+def forward_ckpt(case: Case, k: int, precision: str = "f64"):
+    """Forward loop keeping checkpoint pairs every k steps instead of every
+    state.  Returns (out_ux, out_uy, ckpt) for adjoint_ckpt."""
+    dt = np.float64 if precision == "f64" else np.float32
+    fn = getattr(_lib(), f"oracle_forward_ckpt_{precision}")
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(_Problem)] + [ctypes.c_void_p] * 6 + [real, ctypes.c_int] + \
+        [ctypes.c_void_p] * 3
+    C, D = _arr(case.C, dt), _arr(case.D, dt)
+    sig, smap = _arr(case.src_signal, dt), _arr(case.src_map, dt)
+    org = _arr(case.src_origin, np.int32)
+    rec = _arr(case.rec_idx, np.int32)
+    out_ux = np.zeros(case.out_shape(), dt)
+    out_uy = np.zeros(case.out_shape(), dt)
+    nseg = (case.nt + k - 1) // k
+    ckpt = np.zeros((nseg, case.nshots, 2, 2, case.nx, case.ny), dt)
+    p = case.problem()
+    rc = fn(ctypes.byref(p), _ptr(C), _ptr(D), _ptr(sig), _ptr(smap), _ptr(org), _ptr(rec),
+            real(case.rho), int(k), _ptr(out_ux), _ptr(out_uy), _ptr(ckpt))
+    if rc != 0:
+        raise ValueError(f"oracle_forward_ckpt failed with code {rc}")
+    return out_ux, out_uy, ckpt
+
+
+def adjoint_ckpt(case: Case, k: int, ckpt: np.ndarray, g_ux: np.ndarray, g_uy: np.ndarray,
+                 precision: str = "f64"):
+    """The exact discrete adjoint recomputing each k-step segment from the
+    checkpoints of forward_ckpt.  Returns what adjoint() returns."""
+    dt = np.float64 if precision == "f64" else np.float32
+    fn = getattr(_lib(), f"oracle_adjoint_ckpt_{precision}")
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(_Problem)] + [ctypes.c_void_p] * 6 + [real, ctypes.c_int] + \
+        [ctypes.c_void_p] * 5
+    C, D = _arr(case.C, dt), _arr(case.D, dt)
+    sig, smap = _arr(case.src_signal, dt), _arr(case.src_map, dt)
+    org = _arr(case.src_origin, np.int32)
+    rec = _arr(case.rec_idx, np.int32)
+    ck = _arr(ckpt, dt)
+    gx, gy = _arr(g_ux, dt), _arr(g_uy, dt)
+    if case.mode == MODE_FIELDS:
+        gC = np.zeros((6, case.nx, case.ny), np.float64)
+    else:
+        gC = np.zeros(6, np.float64)
+    gD = np.zeros((case.nx, case.ny), np.float64) if case.mode == MODE_DFIELD else None
+    p = case.problem()
+    rc = fn(ctypes.byref(p), _ptr(C), _ptr(D), _ptr(sig), _ptr(smap), _ptr(org), _ptr(rec),
+            real(case.rho), int(k), _ptr(ck), _ptr(gx), _ptr(gy), _ptr(gC), _ptr(gD))
+    if rc != 0:
+        raise ValueError(f"oracle_adjoint_ckpt failed with code {rc}")
+    return gC, gD
+
+
 def operator(nx, ny, h, C, ux, uy, fx=None, fy=None, rho=1.0, mode=MODE_SCALAR, D=None,
              precision="f64", ref_f32_sum=1):
     """One application of the elastic operator: returns (Lux, Luy) = ((A u + f) / rho)."""

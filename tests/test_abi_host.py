@@ -56,10 +56,29 @@ def test_validation_rejects_bad_problems():
     assert lib.ernn_validate(ctypes.byref(_problem())) == 0
     bad = [dict(nx=0), dict(nt=0), dict(stride=0), dict(mode=3), dict(record=2),
            dict(nrec=0), dict(src_comp=2), dict(h=0.0), dict(dt=-1.0), dict(ckpt_k=0),
-           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=4), dict(path=-1), dict(flags=2), dict(flags=1, mode=1)]
+           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=4), dict(path=-1), dict(flags=4),
+           dict(flags=1, mode=1),
+           # instances on a canvas: scalar constants, receiver traces, canvas < 65536
+           dict(flags=2, mode=1), dict(flags=2, record=0), dict(flags=2, nshots=257),
+           dict(flags=2, nx=70000, ny=16)]
     for kw in bad:
         assert lib.ernn_validate(ctypes.byref(_problem(**kw))) == 1, kw
     assert lib.ernn_validate(None) == 1
+
+
+def test_instance_workspace_holds_one_canvas_plane():
+    # with instances the state is one canvas plane, not one per shot, and the
+    # tape and scratch hold the tile table (and the scratch a zero state)
+    lib = E.load_library()
+    plain = _problem(flags=1, ckpt_k=100)
+    inst = _problem(flags=2, ckpt_k=100)
+    assert lib.ernn_validate(ctypes.byref(inst)) == 0
+    state1 = (2 * 64 * 48 * 4 + 255) // 256 * 256
+    t_plain = lib.ernn_tape_bytes(ctypes.byref(plain), 0)
+    t_inst = lib.ernn_tape_bytes(ctypes.byref(inst), 0)
+    # two state levels of two shots vs of one plane, plus the table
+    assert t_inst - 2 * state1 < t_plain - 2 * 2 * state1 + 256 * 1024
+    assert lib.ernn_adjoint_scratch_bytes(ctypes.byref(inst)) > 0
 
 
 def test_workspace_sizes_follow_checkpoint_plan():

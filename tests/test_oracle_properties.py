@@ -145,3 +145,25 @@ def test_invalid_problem_rejected():
     case.h = -1.0
     with pytest.raises(ValueError):
         O.forward(case)
+
+
+@pytest.mark.parametrize("mode,record,k", [(O.MODE_SCALAR, O.RECORD_RECEIVERS, 7),
+                                           (O.MODE_SCALAR, O.RECORD_FIELDS, 90),
+                                           (O.MODE_DFIELD, O.RECORD_RECEIVERS, 13),
+                                           (O.MODE_FIELDS, O.RECORD_FIELDS, 1)])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_checkpointed_oracle_equals_the_store_all_oracle(mode, record, k, precision):
+    # the checkpointed drivers replay the same steps in the same order: the
+    # outputs and gradients are bitwise those of the store-all drivers
+    case = make_case(mode=mode, record=record, S=2, nt=61)
+    rng = np.random.default_rng(2)
+    wx = rng.standard_normal(case.out_shape())
+    wy = rng.standard_normal(case.out_shape())
+    ax, ay, st = O.forward(case, precision, keep_states=True)
+    gA, dA = O.adjoint(case, st, wx, wy, precision)
+    bx, by, ck = O.forward_ckpt(case, k, precision)
+    gB, dB = O.adjoint_ckpt(case, k, ck, wx, wy, precision)
+    assert np.array_equal(ax, bx) and np.array_equal(ay, by)
+    assert np.array_equal(gA, gB)
+    if dA is not None:
+        assert np.array_equal(dA, dB)
