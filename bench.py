@@ -339,7 +339,7 @@ def run_ernn(args, dist):
             D = inv.D.detach() if damage else None
         tuned = autotune.tune(inv.geom, C, inv.rho, D=D)
         del C, D
-        inv.geom.path, inv.geom.ckpt_k = tuned
+        inv.geom.path, inv.geom.ckpt_k, inv.geom.tile_rows = tuned
         torch.cuda.synchronize()
         E.check_device_status()
     if not args.eager:  # the whole iteration as one CUDA graph, replayed per step
@@ -474,7 +474,8 @@ def run_ernn(args, dist):
                    "kernel_path": {0: "auto", 1: "step", 2: "resident", 3: "tiled"}[int(lib.ernn_last_path())],
                    "launch": ("one CUDA graph per iteration" if inv.graph is not None else "eager") +
                              ("" if args.no_overlap else ", step kernels overlapped (programmatic dependent launch)"),
-                   "path_choice": "measured (autotune)" if tuned else args.path,
+                   "path_choice": (f"measured (autotune): tiles 64x{inv.geom.tile_rows}" if tuned
+                                   else args.path),
                    "l2": "flushed between timed iterations (256 MiB write)",
                    **({"iterations": "each restarts from the initial guess (outside the timed region)"}
                       if w.extra.get("restart") else {}),

@@ -15,6 +15,7 @@ RECORD_FIELDS, RECORD_RECEIVERS = 0, 1
 PATH_AUTO, PATH_STEP, PATH_RESIDENT, PATH_TILED = 0, 1, 2, 3
 FLAG_SHOT_CONSTANTS = 1
 FLAG_INSTANCES = 2
+FLAG_TALL_TILES = 4
 
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "workspace too small", 3: "CUDA runtime error",

@@ -1,4 +1,4 @@
-"""Measured choice of the kernel path and checkpoint interval for a problem.
+"""Measured choice of the kernel path, tile geometry and checkpoint interval.
 
 `choose_ckpt_k` (propagate.py) sizes the checkpoint interval from memory;
 ERNN_PATH_AUTO picks the kernel path from static rules (cluster-resident when
@@ -6,11 +6,13 @@ the state fits a cluster, tiled when a step has >= 4 tiles per SM, plain
 otherwise).  The rules are right for one problem running alone; for problems
 that share the GPU with others (the streams of a multi-instance iteration) or
 sit near a threshold, `tune` times the candidates instead: every eligible
-path — and, when the tape does not fit, the memory-sized interval and half
-of it — on a short forward + adjoint of the same problem (`probe_steps` steps,
-the problem's own shots, grid and receivers), and keeps the fastest.  Results
-are cached per (device name, grid, shots, steps, mode, record, per-shot
-constants) for the process, and optionally in a JSON file.
+path — on the tiled path both tile geometries, 64 x 16 and 64 x 32 tiles
+(ERNN_FLAG_TALL_TILES) — and, when the tape does not fit, the memory-sized
+interval and half of it, on a short forward + adjoint of the same problem
+(`probe_steps` steps, the problem's own shots, grid and receivers), and
+keeps the fastest.  Results are cached per (device name, grid, shots, steps,
+mode, record, per-shot constants) for the process, and optionally in a JSON
+file.
 """
 from __future__ import annotations
 
@@ -50,9 +52,10 @@ def _time(geom: Geometry, C, rho, D, steps: int, reps: int) -> float:
 
 
 def tune(geom: Geometry, C: torch.Tensor, rho: torch.Tensor, D=None, probe_steps: int = 96,
-         reps: int = 2, cache_file: str | None = None) -> tuple[int, int]:
-    """(path, ckpt_k) for this problem, measured; sets neither on `geom`.  A
-    checkpoint interval already set on `geom` is kept (only the path is tuned)."""
+         reps: int = 2, cache_file: str | None = None) -> tuple[int, int, int]:
+    """(path, ckpt_k, tile_rows) for this problem, measured; sets none of them
+    on `geom`.  A checkpoint interval already set on `geom` is kept.
+    tile_rows: 32 for 64 x 32 tiles on the tiled path, else 16."""
     dev = C.device
     key = _key(geom, C, D, dev)
     if key not in _CACHE and cache_file and os.path.exists(cache_file):
@@ -73,20 +76,26 @@ def tune(geom: Geometry, C: torch.Tensor, rho: torch.Tensor, D=None, probe_steps
         ks = [k_mem] if k_mem >= geom.nt else sorted({max(1, k_mem // 2), k_mem})
     best = None
     for path in (_lib.PATH_RESIDENT, _lib.PATH_TILED, _lib.PATH_STEP):
-        for k in ks:
-            # the probe keeps the interval's ratio to the step count
-            k_probe = max(1, min(steps, round(k * steps / geom.nt)))
-            g = dataclasses.replace(geom, path=path, ckpt_k=k_probe, _checked=False)
-            try:
-                ms = _time(g, C, rho, D, steps, reps)
-            except _lib.ErnnError as e:
-                if e.code == 6:  # ERNN_ERR_UNSUPPORTED: path not eligible
-                    break
-                raise
-            if best is None or ms < best[0]:
-                best = (ms, path, k)
-    _CACHE[key] = (best[1], best[2])
+        rows = (16, 32) if path == _lib.PATH_TILED else (16,)
+        eligible = True
+        for tr in rows:
+            for k in ks:
+                # the probe keeps the interval's ratio to the step count
+                k_probe = max(1, min(steps, round(k * steps / geom.nt)))
+                g = dataclasses.replace(geom, path=path, ckpt_k=k_probe, tile_rows=tr, _checked=False)
+                try:
+                    ms = _time(g, C, rho, D, steps, reps)
+                except _lib.ErnnError as e:
+                    if e.code == 6:  # ERNN_ERR_UNSUPPORTED: path not eligible
+                        eligible = False
+                        break
+                    raise
+                if best is None or ms < best[0]:
+                    best = (ms, path, k, tr)
+            if not eligible:
+                break
+    _CACHE[key] = (best[1], best[2], best[3])
     if cache_file:
         with open(cache_file, "w") as f:
             json.dump(_CACHE, f)
-    return best[1], best[2]
+    return tuple(_CACHE[key])

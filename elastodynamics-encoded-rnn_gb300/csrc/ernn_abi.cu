@@ -117,7 +117,8 @@ int validate(const ErnnProblem* p) {
   if (p->src_comp != 0 && p->src_comp != 1) return ERNN_ERR_INVALID;
   if (p->src_bx < 0 || p->src_by < 0) return ERNN_ERR_INVALID;
   if (p->path < ERNN_PATH_AUTO || p->path > ERNN_PATH_TILED) return ERNN_ERR_INVALID;
-  if ((p->flags & ~(ERNN_FLAG_SHOT_CONSTANTS | ERNN_FLAG_INSTANCES)) != 0) return ERNN_ERR_INVALID;
+  if ((p->flags & ~(ERNN_FLAG_SHOT_CONSTANTS | ERNN_FLAG_INSTANCES | ERNN_FLAG_TALL_TILES)) != 0)
+    return ERNN_ERR_INVALID;
   if ((p->flags & ERNN_FLAG_SHOT_CONSTANTS) && p->mode != kModeScalar) return ERNN_ERR_INVALID;
   if ((p->flags & ERNN_FLAG_INSTANCES) &&
       (p->mode != kModeScalar || p->record != kRecordReceivers || p->nshots > kMaxInstances ||
@@ -503,6 +504,7 @@ static int forward_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPl
   const bool receivers = (p->record == kRecordReceivers);
   FwdStep a = base_fwd(*p, *in, coef, pl.nt_out);
   a.inst = itab;
+  a.tile_rows = (p->flags & ERNN_FLAG_TALL_TILES) ? 32 : 16;
   const float* last = nullptr;
   for (int i = 0; i < p->nt; ++i) {
     if (store_all) {
@@ -645,13 +647,15 @@ static int adjoint_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPl
   b.gacc = gacc;
   b.tile_flags = nullptr;
   b.inst = itab;
+  b.tile_rows = (p->flags & ERNN_FLAG_TALL_TILES) ? 32 : 16;
   if (tiled && p->record == kRecordReceivers) {
     uint8_t* flags = reinterpret_cast<uint8_t*>(at(scratch, pl.s_tflags));
     if (ip != nullptr)
       ERNN_CUDA(launch_inst_tile_flags(in->rec_idx, p->nshots, p->nrec, p->ny, itab.box, flags,
                                        ip->upto[ip->d.count], st));
     else
-      ERNN_CUDA(launch_tile_flags(p->mode, in->rec_idx, p->nshots, p->nrec, p->nx, p->ny, flags, st));
+      ERNN_CUDA(launch_tile_flags(p->mode, in->rec_idx, p->nshots, p->nrec, p->nx, p->ny, flags, st,
+                                  b.tile_rows));
     b.tile_flags = flags;
   }
 
@@ -690,6 +694,7 @@ static int adjoint_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPl
   } else {
     FwdStep a = base_fwd(*p, *in, coef, pl.nt_out);
     a.inst = itab;
+    a.tile_rows = b.tile_rows;
     for (int j = pl.nseg - 1; j >= 0; --j) {
       const int i0 = j * pl.k, i1 = (j + 1) * pl.k < p->nt ? (j + 1) * pl.k : p->nt;
       // recompute u^{i0+1} .. u^{i1} into the segment buffer; u^{nt} is never

@@ -51,6 +51,7 @@ struct FwdStep {
   int bx, by, src_comp;
   int chained;  // previous launch on the stream is a step kernel of the same loop
   InstTiles inst;  // instances: tile table (inst.tiles == nullptr otherwise)
+  int tile_rows;   // tiled kernels: 32 for 64 x 32 tiles, otherwise the default (16)
 };
 
 // Per-step arguments of the adjoint kernel: computes lam^m from lam^{m+1},
@@ -76,6 +77,7 @@ struct AdjStep {
   const uint8_t* tile_flags;
   int chained;  // previous launch on the stream is a step kernel of the same loop
   InstTiles inst;  // instances: tile table (inst.tiles == nullptr otherwise)
+  int tile_rows;   // tiled kernels: 32 for 64 x 32 tiles, otherwise the default (16)
 };
 
 dim3 step_grid(int nx, int ny, int S);

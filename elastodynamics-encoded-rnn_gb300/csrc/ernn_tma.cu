@@ -407,25 +407,29 @@ __device__ __forceinline__ float4 one_minus(const float4 d) {
 // Stage: halo box of u^i, own box of u^{i-1}.  DFIELD reads its 4 weights
 // per row straight from global memory (one plane shared by every shot, L2
 // resident).
-// 64 x 16 tiles, one row per thread.
-struct FwdLayout {
-  static constexpr int kTR = 16;         // tile rows
+// 64 x TR tiles, TR / 16 rows per thread: 16 rows by default (four CTAs per
+// SM), 32 rows as a measured alternative (three CTAs per SM, a tenth fewer
+// halo rows per cell).
+template <int TR>
+struct FwdLayoutT {
+  static constexpr int kTR = TR;         // tile rows
   static constexpr int kRT = kTR / 16;   // rows per thread
   static constexpr int kBHa = kTR + 2;   // halo box rows
   static constexpr int kHalo = 2 * kBHa * kBW;
   static constexpr int kOwn = 2 * kTR * kTY;
   static constexpr int kStage = (kHalo + kOwn + 31) / 32 * 32;  // 128-byte multiple
-  static constexpr int kCtasPerSm = 4;
+  static constexpr int kCtasPerSm = TR == 16 ? 4 : 3;
 };
+using FwdLayout = FwdLayoutT<16>;
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads, FwdLayout::kCtasPerSm)
+template <int MODE, int TR>
+__global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
     tma_fwd_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, int tiles_x, int tiles_y, int has_prev,
                    int* err) {
   extern __shared__ float sm_raw[];
   float* sm = aligned128(sm_raw);
-  using F = FwdLayout;
+  using F = FwdLayoutT<TR>;
   constexpr int kStage = F::kStage;
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * kStage);
   const int tid = threadIdx.x;
@@ -788,13 +792,14 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
 // Stage (DFIELD): halo boxes of lam^{m+1}, u^m and D (its imaging is per
 // cell, so u's stencils are needed); lam^{m+2} is read into registers
 // before the wait (keeps two CTAs per SM within shared memory).
-template <int MODE>
+template <int MODE, int TR = (MODE == kModeScalar ? 16 : 32)>
 struct AdjLayout {
   // SCALAR: 64 x 16 tiles, one row per thread (80 registers: three CTAs
-  // per SM).  DFIELD keeps 64 x 32 tiles and two rows per thread: with one
-  // row its three halo windows per output row (lam, u, D) cost more than the
-  // third CTA gains (24.4 vs 21.5 us per damage512 step)
-  static constexpr int kTR = (MODE == kModeScalar) ? 16 : 32;  // tile rows
+  // per SM), or 64 x 32 tiles (two rows per thread, two CTAs per SM) as a
+  // measured alternative.  DFIELD keeps 64 x 32 tiles and two rows per
+  // thread: with one row its three halo windows per output row (lam, u, D)
+  // cost more than the third CTA gains (24.4 vs 21.5 us per damage512 step)
+  static constexpr int kTR = TR;                               // tile rows
   static constexpr int kRT = kTR / 16;                         // rows per thread
   static constexpr int kBHa = kTR + 2;                         // halo box rows
   static constexpr int kHalo = 2 * kBHa * kBW;
@@ -810,15 +815,15 @@ struct AdjLayout {
   // two CTAs per SM measured slower for SCALAR (150 vs 114 us per shots1024
   // step): the kernel needs the third CTA's warps more than a deeper pipeline
   static constexpr int kStages = 2;
-  static constexpr int kCtasPerSm = (MODE == kModeScalar) ? 3 : 2;
+  static constexpr int kCtasPerSm = (MODE == kModeScalar && TR == 16) ? 3 : 2;
 };
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads, AdjLayout<MODE>::kCtasPerSm)
+template <int MODE, int TR>
+__global__ void __launch_bounds__(kThreads, AdjLayout<MODE, TR>::kCtasPerSm)
     tma_adj_kernel(const AdjStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap u_map,
                    const __grid_constant__ CUtensorMap d_map, int tiles_x, int tiles_y, int has_u, int* err) {
-  using L = AdjLayout<MODE>;
+  using L = AdjLayout<MODE, TR>;
   extern __shared__ float sm_raw[];
   float* sm = aligned128(sm_raw);
   constexpr int NS = L::kStages;
@@ -1201,11 +1206,15 @@ bool make_map2(CUtensorMap* m, const float* base, int nx, int ny, int bw, int bh
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-constexpr size_t kFwdSmem = 2 * (size_t)FwdLayout::kStage * 4 + 16 + 128;
+template <int TR>
+constexpr size_t fwd_smem() {
+  return 2 * (size_t)FwdLayoutT<TR>::kStage * 4 + 16 + 128;
+}
 constexpr size_t kFwd2Smem = (2 * (size_t)Fwd2Layout::kStage + 2 * (size_t)Fwd2Layout::kMid) * 4 + 16 + 128;
-template <int MODE>
+template <int MODE, int TR = (MODE == kModeScalar ? 16 : 32)>
 constexpr size_t adj_smem() {
-  return (size_t)AdjLayout<MODE>::kStages * AdjLayout<MODE>::kStage * 4 + 8 * AdjLayout<MODE>::kStages + 128;
+  using L = AdjLayout<MODE, TR>;
+  return (size_t)L::kStages * L::kStage * 4 + 8 * L::kStages + 128;
 }
 
 cudaError_t set_smem() {
@@ -1213,12 +1222,15 @@ cudaError_t set_smem() {
   static cudaError_t result = cudaSuccess;
   std::call_once(once, [] {
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e[5] = {
-        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar>, at, (int)kFwdSmem),
-        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField>, at, (int)kFwdSmem),
+    cudaError_t e[8] = {
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar, 16>, at, (int)fwd_smem<16>()),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField, 16>, at, (int)fwd_smem<16>()),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar, 32>, at, (int)fwd_smem<32>()),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField, 32>, at, (int)fwd_smem<32>()),
         cudaFuncSetAttribute(tma_fwd2_kernel<kModeScalar>, at, (int)kFwd2Smem),
-        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar>, at, (int)adj_smem<kModeScalar>()),
-        cudaFuncSetAttribute(tma_adj_kernel<kModeDField>, at, (int)adj_smem<kModeDField>())};
+        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar, 16>, at, (int)adj_smem<kModeScalar, 16>()),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar, 32>, at, (int)adj_smem<kModeScalar, 32>()),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeDField, 32>, at, (int)adj_smem<kModeDField, 32>())};
     for (cudaError_t x : e)
       if (x != cudaSuccess) result = x;
   });
@@ -1245,8 +1257,8 @@ cudaError_t wait_selftest(int* status_host, cudaStream_t st) {
 }
 
 cudaError_t launch_tile_flags(int mode, const int32_t* rec_idx, int S, int nrec, int nx, int ny,
-                              uint8_t* flags, cudaStream_t st) {
-  const int tr = tma_adj_tile_rows(mode);
+                              uint8_t* flags, cudaStream_t st, int tile_rows) {
+  const int tr = tma_adj_tile_rows(mode, tile_rows);
   const int tiles_x = (nx + tr - 1) / tr, tiles_y = (ny + kTY - 1) / kTY;
   cudaError_t e = cudaMemsetAsync(flags, 0, tma_tiles(nx, ny, S, tr), st);
   if (e != cudaSuccess) return e;
@@ -1314,8 +1326,8 @@ size_t tma_tiles(int nx, int ny, int S, int tile_rows) {
   return (size_t)S * ((nx + tile_rows - 1) / tile_rows) * ((ny + kTY - 1) / kTY);
 }
 
-int tma_adj_tile_rows(int mode) {
-  return mode == kModeScalar ? AdjLayout<kModeScalar>::kTR : AdjLayout<kModeDField>::kTR;
+int tma_adj_tile_rows(int mode, int tile_rows) {
+  return mode == kModeScalar ? (tile_rows == 32 ? 32 : 16) : AdjLayout<kModeDField>::kTR;
 }
 
 namespace {
@@ -1359,32 +1371,42 @@ cudaError_t launch_tma_fwd2(int mode, const FwdStep& a, int* err, cudaStream_t s
   }, 2.0 * (a.inst.tiles ? (double)a.inst.ntiles * F::kTR * kTY : (double)a.S * a.nx * a.ny) * 16.0);
 }
 
-cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st) {
+namespace {
+template <int TR>
+cudaError_t launch_tma_fwd_t(int mode, const FwdStep& a, int* err, cudaStream_t st) {
+  using F = FwdLayoutT<TR>;
   const bool ok = (mode == kModeScalar || (mode == kModeDField && al16(a.field))) && a.cur != nullptr &&
                   a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) && al16(a.copy0) &&
                   al16(a.copy1) && (a.frame < 0 || (al16(a.hist_x) && al16(a.hist_y)));
   CUtensorMap cur_map, prev_map;
   const int planes = a.inst.tiles ? 1 : a.S;  // instances share one canvas plane
-  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, planes, kBW, FwdLayout::kBHa) ||
-      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, planes, kTY, FwdLayout::kTR))
+  if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, planes, kBW, F::kBHa) ||
+      !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, planes, kTY, F::kTR))
     return a.inst.tiles ? cudaErrorNotSupported : launch_fwd_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
-  const int tiles_x = (a.nx + FwdLayout::kTR - 1) / FwdLayout::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
+  const int tiles_x = (a.nx + F::kTR - 1) / F::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
-  int grid = num_sms() * FwdLayout::kCtasPerSm;
+  int grid = num_sms() * F::kCtasPerSm;
   if (grid > ntiles) grid = ntiles;
-  const double cells = a.inst.tiles ? (double)a.inst.ntiles * FwdLayout::kTR * kTY : (double)a.S * a.nx * a.ny;
+  const double cells = a.inst.tiles ? (double)a.inst.ntiles * F::kTR * kTY : (double)a.S * a.nx * a.ny;
   const int hp = a.prev ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfForward, st, [&] {
     if (mode == kModeScalar)
-      launch_step_kernel(tma_fwd_kernel<kModeScalar>, grid, dim3(kThreads), kFwdSmem, st, chained,
+      launch_step_kernel(tma_fwd_kernel<kModeScalar, TR>, grid, dim3(kThreads), fwd_smem<TR>(), st, chained,
                          a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
     else
-      launch_step_kernel(tma_fwd_kernel<kModeDField>, grid, dim3(kThreads), kFwdSmem, st, chained,
+      launch_step_kernel(tma_fwd_kernel<kModeDField, TR>, grid, dim3(kThreads), fwd_smem<TR>(), st, chained,
                          a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
   }, cells * alg_bytes_forward(mode));
+}
+}  // namespace
+
+cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st) {
+  // the instance tile table holds 16-row tiles
+  if (a.tile_rows == 32 && a.inst.tiles == nullptr) return launch_tma_fwd_t<32>(mode, a, err, st);
+  return launch_tma_fwd_t<16>(mode, a, err, st);
 }
 
 namespace {
@@ -1394,7 +1416,7 @@ bool adj_maps(int mode, const AdjStep& a, CUtensorMap* cur_map, CUtensorMap* pre
   const bool ok = (mode == kModeScalar || (dfield && al16(a.field) && al16(a.gacc))) && a.ny % 4 == 0 &&
                   a.cur != nullptr && a.prev != nullptr && al16(a.cur) && al16(a.prev) && al16(a.out) &&
                   al16(a.u) && (a.record != kRecordFields || (al16(a.g_x) && al16(a.g_y)));
-  const int tr = tma_adj_tile_rows(mode), bh = tr + 2;
+  const int tr = tma_adj_tile_rows(mode, a.inst.tiles ? 16 : a.tile_rows), bh = tr + 2;
   const int planes = a.inst.tiles ? 1 : a.S;  // instances share one canvas plane
   return ok && make_map(cur_map, a.cur, a.nx, a.ny, planes, kBW, bh) &&
          make_map(prev_map, a.prev, a.nx, a.ny, planes, kTY, tr) &&
@@ -1415,21 +1437,26 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
     return a.inst.tiles ? cudaErrorNotSupported : launch_adj_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
-  const int tr = tma_adj_tile_rows(mode);
+  const int tr = tma_adj_tile_rows(mode, a.inst.tiles ? 16 : a.tile_rows);
   const int tiles_x = (a.nx + tr - 1) / tr, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
-  int grid = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm : AdjLayout<kModeScalar>::kCtasPerSm);
+  int grid = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm
+                                 : (tr == 32 ? AdjLayout<kModeScalar, 32>::kCtasPerSm
+                                             : AdjLayout<kModeScalar, 16>::kCtasPerSm));
   if (grid > ntiles) grid = ntiles;
   if (grid > kTiledRowsPerShot) grid = kTiledRowsPerShot;
   const double cells = a.inst.tiles ? (double)a.inst.ntiles * tr * kTY : (double)a.S * a.nx * a.ny;
   const int hu = a.u ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfAdjoint, st, [&] {
-    if (!dfield)
-      launch_step_kernel(tma_adj_kernel<kModeScalar>, grid, dim3(kThreads), adj_smem<kModeScalar>(), st,
+    if (dfield)
+      launch_step_kernel(tma_adj_kernel<kModeDField, 32>, grid, dim3(kThreads), adj_smem<kModeDField, 32>(), st,
+                         chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+    else if (tr == 32)
+      launch_step_kernel(tma_adj_kernel<kModeScalar, 32>, grid, dim3(kThreads), adj_smem<kModeScalar, 32>(), st,
                          chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
     else
-      launch_step_kernel(tma_adj_kernel<kModeDField>, grid, dim3(kThreads), adj_smem<kModeDField>(), st,
+      launch_step_kernel(tma_adj_kernel<kModeScalar, 16>, grid, dim3(kThreads), adj_smem<kModeScalar, 16>(), st,
                          chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
   }, cells * alg_bytes_adjoint(mode));
 }

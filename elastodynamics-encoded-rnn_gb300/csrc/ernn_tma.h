@@ -15,8 +15,9 @@ bool tma_eligible(int mode, int nx, int ny, int S);
 constexpr int kTiledRowsPerShot = 1024;
 // Number of 64-column tiles of `tile_rows` rows of one step over all shots.
 size_t tma_tiles(int nx, int ny, int S, int tile_rows = 32);
-// Tile rows of the tiled adjoint for a mode (16 SCALAR, 32 DFIELD).
-int tma_adj_tile_rows(int mode);
+// Tile rows of the tiled adjoint for a mode: SCALAR 16, or 32 when
+// tile_rows == 32 (ERNN_FLAG_TALL_TILES); DFIELD 32.
+int tma_adj_tile_rows(int mode, int tile_rows = 0);
 // Same contract as launch_fwd_step / launch_adj_step (SCALAR or DFIELD
 // mode); `err` is the call's device error word.
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st);
@@ -31,9 +32,9 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
 // back to the plain kernel.
 bool tma_adj_would_run(int mode, const AdjStep& a);
 // Per-call receiver table of the tiled adjoint of `mode`
-// (tma_tiles(nx, ny, S, tma_adj_tile_rows(mode)) bytes at `flags`).
+// (tma_tiles(nx, ny, S, tma_adj_tile_rows(mode, tile_rows)) bytes at `flags`).
 cudaError_t launch_tile_flags(int mode, const int32_t* rec_idx, int S, int nrec, int nx, int ny,
-                              uint8_t* flags, cudaStream_t st);
+                              uint8_t* flags, cudaStream_t st, int tile_rows = 0);
 // Instances on a canvas (ERNN_FLAG_INSTANCES).  The instance table passed
 // by value to the kernel that writes the tile table: instances in the order
 // of decreasing step count, each with its caller-side index.

@@ -325,7 +325,8 @@ class _InstanceGroup:
         if tuned:  # measured kernel path at the memory-sized interval (autotune keeps a fixed one)
             from . import autotune
             C = torch.stack([inv.params() for inv in invs]).detach() if S > 1 else invs[0].params().detach()
-            self.geom.path, self.geom.ckpt_k = autotune.tune(self.geom, C, self.rho if S > 1 else self.rho[0])
+            self.geom.path, self.geom.ckpt_k, self.geom.tile_rows = autotune.tune(
+                self.geom, C, self.rho if S > 1 else self.rho[0])
 
     def loss(self):
         if len(self.invs) == 1:

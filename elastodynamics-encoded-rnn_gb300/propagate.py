@@ -68,6 +68,8 @@ class Geometry:
     path:       PATH_AUTO (cluster-resident when the problem fits, else the
                 tiled TMA kernels when eligible, else one plain kernel per
                 step), PATH_STEP, PATH_RESIDENT or PATH_TILED.
+    tile_rows:  tile rows of the tiled kernels, 16 or 32 (autotune.tune
+                measures both).
     """
     nx: int
     ny: int
@@ -83,6 +85,7 @@ class Geometry:
     ckpt_k: int | None = None
     path: int = _lib.PATH_AUTO
     instances: Instances | None = None
+    tile_rows: int = 16  # tiled kernels: 16 (64 x 16 tiles) or 32 (64 x 32, ERNN_FLAG_TALL_TILES)
     _checked: bool = field(default=False, repr=False)
 
     @property
@@ -99,6 +102,8 @@ class Geometry:
 
     def problem(self, mode: int, flags: int = 0) -> _lib.ErnnProblem:
         nrec = 0 if self.rec_idx is None else int(self.rec_idx.shape[1])
+        if self.tile_rows == 32:
+            flags |= _lib.FLAG_TALL_TILES
         k = self.ckpt_k if self.ckpt_k is not None else self.nt
         return _lib.ErnnProblem(self.nshots, self.nx, self.ny, self.nt, self.stride, mode,
                                 self.record, nrec, self.src_comp, int(self.src_map.shape[1]),

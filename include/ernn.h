@@ -83,7 +83,12 @@ enum {
    * src_map, src_origin in canvas cells), receivers (rec_idx: canvas cell
    * indices) and step count; nt is the largest step count.  SCALAR mode,
    * RECORD_RECEIVERS, tiled kernels (ERNN_PATH_AUTO or _TILED). */
-  ERNN_FLAG_INSTANCES = 2
+  ERNN_FLAG_INSTANCES = 2,
+  /* Tiled kernels: 64 x 32 tiles for the forward steps and the scalar
+   * adjoint instead of 64 x 16 (a tenth fewer halo rows per cell, one CTA
+   * fewer per SM); a tile geometry the autotuner measures.  Results are the
+   * same up to FP32 rounding of the imaging sums' grouping. */
+  ERNN_FLAG_TALL_TILES = 4
 };
 
 /* One propagation problem.  Plain data; identical layout in C, C++, ctypes. */

@@ -56,7 +56,7 @@ def test_validation_rejects_bad_problems():
     assert lib.ernn_validate(ctypes.byref(_problem())) == 0
     bad = [dict(nx=0), dict(nt=0), dict(stride=0), dict(mode=3), dict(record=2),
            dict(nrec=0), dict(src_comp=2), dict(h=0.0), dict(dt=-1.0), dict(ckpt_k=0),
-           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=4), dict(path=-1), dict(flags=4),
+           dict(nshots=0), dict(nx=70000, ny=70000), dict(path=4), dict(path=-1), dict(flags=8),
            dict(flags=1, mode=1),
            # instances on a canvas: scalar constants, receiver traces, canvas < 65536
            dict(flags=2, mode=1), dict(flags=2, record=0), dict(flags=2, nshots=257),

@@ -84,10 +84,35 @@ def test_autotune_picks_an_eligible_path_and_caches():
     geom = to_geometry(case, None, E.PATH_AUTO)
     C = torch.tensor(case.C, dtype=torch.float32, device=DEV)
     rho = torch.tensor(case.rho, dtype=torch.float32, device=DEV)
-    path, k = autotune.tune(geom, C, rho, probe_steps=40)
+    path, k, rows = autotune.tune(geom, C, rho, probe_steps=40)
     assert path in (E.PATH_STEP, E.PATH_RESIDENT, E.PATH_TILED) and 1 <= k <= case.nt
-    assert autotune.tune(geom, C, rho) == (path, k)  # cached
-    geom.path, geom.ckpt_k = path, k
+    assert rows in (16, 32) and (rows == 16 or path == E.PATH_TILED)
+    assert autotune.tune(geom, C, rho) == (path, k, rows)  # cached
+    geom.path, geom.ckpt_k, geom.tile_rows = path, k, rows
     with torch.no_grad():
         E.propagate(C, rho, geom)
     assert E._lib.load().ernn_last_path() == path
+
+
+@pytest.mark.parametrize("per_shot", [False, True])
+def test_tall_tiles_match_default_tiles(per_shot):
+    # 64 x 32 tiles (ERNN_FLAG_TALL_TILES) against the default 64 x 16 on the
+    # tiled path: the same forward states (same arithmetic per cell) and the
+    # gradient up to the grouping of the FP32 imaging sums
+    case = random_case(nx=70, ny=132, nt=90, S=2, record=O.RECORD_RECEIVERS, nrec=9)
+    rho = torch.tensor(case.rho, dtype=torch.float32, device=DEV)
+    out = []
+    for rows in (16, 32):
+        geom = to_geometry(case, 30, E.PATH_TILED)
+        geom.tile_rows = rows
+        C = torch.tensor(case.C, dtype=torch.float32, device=DEV)
+        r = rho
+        if per_shot:
+            C, r = C[None].repeat(2, 1) * torch.tensor([[1.0], [1.05]], device=DEV), rho.reshape(1).repeat(2)
+        C = C.clone().requires_grad_(True)
+        ux, uy = E.propagate(C, r, geom)
+        (ux.double().square().sum() + uy.double().square().sum()).backward()
+        out.append((ux.detach().cpu().numpy(), uy.detach().cpu().numpy(), C.grad.double().cpu().numpy()))
+    (ax, ay, ag), (bx, by, bg) = out
+    assert np.array_equal(ax, bx) and np.array_equal(ay, by)
+    assert rel(bg, ag) <= 1e-6, rel(bg, ag)
