@@ -153,7 +153,8 @@ FwdStep base_fwd(const ErnnProblem& p, const ErnnInputs& in, const Coef* coef, i
   a.nx = p.nx; a.ny = p.ny; a.S = p.nshots; a.nt = p.nt;
   a.frame = -1; a.gframe = -1; a.nt_out = nt_out;
   a.coef = coef;
-  a.coef_stride = (p.flags & ERNN_FLAG_SHOT_CONSTANTS) ? 1 : 0;
+  // one coefficient block per shot (per-shot constants) or per instance
+  a.coef_stride = (p.flags & (ERNN_FLAG_SHOT_CONSTANTS | ERNN_FLAG_INSTANCES)) ? 1 : 0;
   a.field = (p.mode == kModeFields) ? in.C : in.D;
   a.src_signal = in.src_signal;
   a.src_map = in.src_map;
