@@ -599,7 +599,7 @@ def canvas_grad_errors(inv, dev, count=64):
         from ernn_gb300.misfit import series_misfit
         ux, uy = _prop(inv.params(), inv.rho, inv.geom)
         series_misfit(ux, uy, inv.obs[0], inv.obs[1], float(S), float(S)).backward()
-    g32 = (theta.grad.detach().double() * inv.scale.double()).cpu().numpy()  # dL/dC
+    g32 = (theta.grad.detach().double() / inv.scale.double()).cpu().numpy()  # dL/dC (C = theta x scale)
     px32, py32 = ux.detach().double().cpu().numpy(), uy.detach().double().cpu().numpy()
     C = inv.params().detach().cpu().numpy().astype(np.float64)
     ox, oy = (o.detach().double().cpu().numpy() for o in inv.obs)
@@ -725,11 +725,22 @@ def run_multi(args, dist):
     torch.cuda.synchronize()
     e2e_ms = dist.max(sum(a.elapsed_time(b) for a, b in e2e) / args.steps)
     sides = [w.nx for w in ws]
-    # library kernels of one iteration (an eager iteration: replays make no host calls)
+    # library kernels of one iteration (an eager iteration: replays make no
+    # host calls), timed per kernel class by the library's own events
+    E._lib.profile(True)
     n_eager = lib.ernn_launch_count()
     (inv._eager_step if args.grouped else inv.step_eager)()
     torch.cuda.synchronize()
     per_iter = lib.ernn_launch_count() - n_eager
+    prof = E._lib.profile_read()
+    E._lib.profile(False)
+    classes = {}
+    for c in ("forward", "adjoint", "other"):
+        t_ms, n_l, b_tot = prof[c]
+        if n_l:
+            classes[c] = {"launches": n_l, "ms_total": round(t_ms, 3), "us_per_launch": round(t_ms * 1e3 / n_l, 3),
+                          "achieved_gbs": round(b_tot / (t_ms * 1e-3) / 1e9, 1) if b_tot else None,
+                          "frac": round(b_tot / (t_ms * 1e-3) / 1e9 / peaks()[0], 4) if b_tot else None}
     extra = {}
     if dist.rank == 0 and not args.no_cpu_baseline:
         if args.grouped:
@@ -757,6 +768,7 @@ def run_multi(args, dist):
                 "unit": "Gcell-steps/s", "h2d_bytes_per_step": sum(o.numel() * 4 for o in obs_h),
                 "d2h_bytes_per_step": out_h.numel() * 8},
         "ms_per_iter": round(ms, 3), "graph_capture_setup_s": round(setup_s, 2),
+        "kernel_classes_eager": classes,
         "host_launch_calls_in_timed_region": int(launches),
         "gpu_launches": int(per_iter * args.steps),
         "clocks": clk, "loss": float(loss), **extra,
