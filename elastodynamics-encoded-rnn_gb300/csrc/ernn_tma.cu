@@ -390,6 +390,27 @@ __device__ __forceinline__ TileId tile_of(int t, int tiles_x, int tiles_y) {
   return id;
 }
 
+// Tile t of a step where a CTA issues its loads: an entry of the instance
+// table (INST) or tile t of the shot-major grid of tiles.
+template <bool INST, int TR>
+__device__ __forceinline__ TileId step_tile(const InstTiles& in, int t, int tiles_x, int tiles_y) {
+  if constexpr (INST) return table_tile(in, t);
+  else return tile_of<TR>(t, tiles_x, tiles_y);
+}
+
+// Tile t of a CTA's compute loop.  The grid of tiles is walked in step with
+// t (advanced here); the table needs no walk.
+template <bool INST, int TR>
+__device__ __forceinline__ TileId walk_tile(const InstTiles& in, int t, TileWalk<TR>& walk, int nx, int ny) {
+  if constexpr (INST) {
+    return table_tile(in, t);
+  } else {
+    const TileId id = grid_tile(walk.id(), nx, ny);
+    walk.next();
+    return id;
+  }
+}
+
 // 2D tile load (columns, rows) into shared memory: the degradation plane.
 __device__ __forceinline__ void tma_load2(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* b) {
   asm volatile(
@@ -422,7 +443,9 @@ struct FwdLayoutT {
 };
 using FwdLayout = FwdLayoutT<16>;
 
-template <int MODE, int TR>
+// INST: tiles from the instance table (one canvas plane, instance-bounded
+// stores); otherwise the shot-major grid of tiles, with no table lookups.
+template <int MODE, int TR, bool INST>
 __global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
     tma_fwd_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, int tiles_x, int tiles_y, int has_prev,
@@ -435,7 +458,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
-  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
+  const int ntiles = INST ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(F::kHalo + (has_prev ? F::kOwn : 0)) * 4u;
   grid_dep_trigger();
   __shared__ int done[2];
@@ -458,9 +481,8 @@ __global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
       const int32_t idx = a.rec_idx[e];
       const size_t o = ((size_t)s * a.nt_out + a.gframe) * a.nrec + r;
       // instances: one canvas plane; an instance past its last step records zeros
-      const size_t plane = a.inst.tiles ? 0 : (size_t)s * 2 * N;
-      const bool ok = a.cur != nullptr && idx >= 0 && (size_t)idx < N &&
-                      (a.inst.tiles == nullptr || a.i <= a.inst.box[2 * s + 1].z);
+      const size_t plane = INST ? 0 : (size_t)s * 2 * N;
+      const bool ok = a.cur != nullptr && idx >= 0 && (size_t)idx < N && (!INST || a.i <= a.inst.box[2 * s + 1].z);
       a.tr_x[o] = ok ? a.cur[plane + idx] : 0.f;
       a.tr_y[o] = ok ? a.cur[plane + N + idx] : 0.f;
     }
@@ -471,7 +493,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles || pipe_failed(&guard)) return;
     pipe_issued(&guard, k);
-    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : tile_of<F::kTR>(t, tiles_x, tiles_y);
+    const TileId id = step_tile<INST, F::kTR>(a.inst, t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
@@ -490,8 +512,7 @@ __global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : grid_tile(walk.id(), nx, ny);
-    walk.next();
+    const TileId id = walk_tile<INST>(a.inst, t, walk, nx, ny);
     // per-tile scalars, loaded before the wait (coefficients per shot with
     // per-shot constants)
     const Coef* K = a.coef + (size_t)id.inst * a.coef_stride;
@@ -620,7 +641,7 @@ __device__ __forceinline__ void win_lanes(const float* __restrict__ box, int r, 
   w[5] = right_ok ? from_right : (b + 4 < kBW ? p[4] : 0.f);
 }
 
-template <int MODE>
+template <int MODE, bool INST>
 __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     tma_fwd2_kernel(const FwdStep a, const __grid_constant__ CUtensorMap cur_map,
                     const __grid_constant__ CUtensorMap prev_map, int tiles_x, int tiles_y, int has_prev,
@@ -632,7 +653,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
-  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
+  const int ntiles = INST ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(F::kCur + (has_prev ? F::kPrev : 0)) * 4u;
   grid_dep_trigger();
   __shared__ int done[2];
@@ -653,7 +674,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles || pipe_failed(&guard)) return;
     pipe_issued(&guard, k);
-    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : tile_of<F::kTR>(t, tiles_x, tiles_y);
+    const TileId id = step_tile<INST, F::kTR>(a.inst, t, tiles_x, tiles_y);
     float* st = sm + (k & 1) * F::kStage;
     fence_async();
     bar_expect(&bar[k & 1], bytes);
@@ -672,8 +693,7 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : grid_tile(walk.id(), nx, ny);
-    walk.next();
+    const TileId id = walk_tile<INST>(a.inst, t, walk, nx, ny);
     const Coef* K = a.coef + (size_t)id.inst * a.coef_stride;
     const Coefs ks = a.coef_stride != 0 ? coefs(K) : ks0;
     const float* sig = a.src_signal + (size_t)id.inst * a.nt;
@@ -818,7 +838,7 @@ struct AdjLayout {
   static constexpr int kCtasPerSm = (MODE == kModeScalar && TR == 16) ? 3 : 2;
 };
 
-template <int MODE, int TR>
+template <int MODE, int TR, bool INST>
 __global__ void __launch_bounds__(kThreads, AdjLayout<MODE, TR>::kCtasPerSm)
     tma_adj_kernel(const AdjStep a, const __grid_constant__ CUtensorMap cur_map,
                    const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap u_map,
@@ -832,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE, TR>::kCtasPerSm)
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   const size_t N = (size_t)nx * ny;
-  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
+  const int ntiles = INST ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   const uint32_t bytes = (uint32_t)(MODE == kModeScalar
                                         ? L::kHalo + L::kOwn + (has_u ? L::kOwn : 0)
                                         : L::kHalo + L::kBHa * kBW + (has_u ? L::kHalo : 0)) * 4u;
@@ -867,7 +887,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE, TR>::kCtasPerSm)
     const int t = t_first + k * t_step;
     if (t >= t_end || pipe_failed(&guard)) return;
     pipe_issued(&guard, k);
-    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : tile_of<L::kTR>(t, tiles_x, tiles_y);
+    const TileId id = step_tile<INST, L::kTR>(a.inst, t, tiles_x, tiles_y);
     const int sg = k % NS;
     float* st = sm + sg * L::kStage;
     fence_async();
@@ -936,8 +956,7 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE, TR>::kCtasPerSm)
   for (int k = 0;; ++k) {
     const int t = t_first + k * t_step;
     if (t >= t_end) break;
-    const TileId id = a.inst.tiles ? table_tile(a.inst, t) : grid_tile(walk.id(), nx, ny);
-    walk.next();
+    const TileId id = walk_tile<INST>(a.inst, t, walk, nx, ny);
     if (MODE == kModeScalar && per_shot && has_u && id.inst != acc_shot) {
       if (acc_shot >= 0) flush(acc_shot);
       acc_shot = id.inst;
@@ -1222,15 +1241,18 @@ cudaError_t set_smem() {
   static cudaError_t result = cudaSuccess;
   std::call_once(once, [] {
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e[8] = {
-        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar, 16>, at, (int)fwd_smem<16>()),
-        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField, 16>, at, (int)fwd_smem<16>()),
-        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar, 32>, at, (int)fwd_smem<32>()),
-        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField, 32>, at, (int)fwd_smem<32>()),
-        cudaFuncSetAttribute(tma_fwd2_kernel<kModeScalar>, at, (int)kFwd2Smem),
-        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar, 16>, at, (int)adj_smem<kModeScalar, 16>()),
-        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar, 32>, at, (int)adj_smem<kModeScalar, 32>()),
-        cudaFuncSetAttribute(tma_adj_kernel<kModeDField, 32>, at, (int)adj_smem<kModeDField, 32>())};
+    cudaError_t e[11] = {
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar, 16, false>, at, (int)fwd_smem<16>()),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField, 16, false>, at, (int)fwd_smem<16>()),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar, 32, false>, at, (int)fwd_smem<32>()),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeDField, 32, false>, at, (int)fwd_smem<32>()),
+        cudaFuncSetAttribute(tma_fwd_kernel<kModeScalar, 16, true>, at, (int)fwd_smem<16>()),
+        cudaFuncSetAttribute(tma_fwd2_kernel<kModeScalar, false>, at, (int)kFwd2Smem),
+        cudaFuncSetAttribute(tma_fwd2_kernel<kModeScalar, true>, at, (int)kFwd2Smem),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar, 16, false>, at, (int)adj_smem<kModeScalar, 16>()),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar, 32, false>, at, (int)adj_smem<kModeScalar, 32>()),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeDField, 32, false>, at, (int)adj_smem<kModeDField, 32>()),
+        cudaFuncSetAttribute(tma_adj_kernel<kModeScalar, 16, true>, at, (int)adj_smem<kModeScalar, 16>())};
     for (cudaError_t x : e)
       if (x != cudaSuccess) result = x;
   });
@@ -1366,47 +1388,56 @@ cudaError_t launch_tma_fwd2(int mode, const FwdStep& a, int* err, cudaStream_t s
   const int hp = a.prev ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfForward, st, [&] {
-    launch_step_kernel(tma_fwd2_kernel<kModeScalar>, dim3(grid), dim3(kThreads), kFwd2Smem, st, chained, a,
-                       cur_map, prev_map, tiles_x, tiles_y, hp, err);
+    if (a.inst.tiles)
+      launch_step_kernel(tma_fwd2_kernel<kModeScalar, true>, dim3(grid), dim3(kThreads), kFwd2Smem, st, chained,
+                         a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+    else
+      launch_step_kernel(tma_fwd2_kernel<kModeScalar, false>, dim3(grid), dim3(kThreads), kFwd2Smem, st, chained,
+                         a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
   }, 2.0 * (a.inst.tiles ? (double)a.inst.ntiles * F::kTR * kTY : (double)a.S * a.nx * a.ny) * 16.0);
 }
 
 namespace {
-template <int TR>
+template <int TR, bool INST>
 cudaError_t launch_tma_fwd_t(int mode, const FwdStep& a, int* err, cudaStream_t st) {
   using F = FwdLayoutT<TR>;
+  if (INST && mode != kModeScalar) return cudaErrorNotSupported;
   const bool ok = (mode == kModeScalar || (mode == kModeDField && al16(a.field))) && a.cur != nullptr &&
                   a.ny % 4 == 0 && al16(a.cur) && al16(a.prev) && al16(a.out) && al16(a.copy0) &&
                   al16(a.copy1) && (a.frame < 0 || (al16(a.hist_x) && al16(a.hist_y)));
   CUtensorMap cur_map, prev_map;
-  const int planes = a.inst.tiles ? 1 : a.S;  // instances share one canvas plane
+  const int planes = INST ? 1 : a.S;  // instances share one canvas plane
   if (!ok || !make_map(&cur_map, a.cur, a.nx, a.ny, planes, kBW, F::kBHa) ||
       !make_map(&prev_map, a.prev ? a.prev : a.cur, a.nx, a.ny, planes, kTY, F::kTR))
-    return a.inst.tiles ? cudaErrorNotSupported : launch_fwd_step(mode, a, st);
+    return INST ? cudaErrorNotSupported : launch_fwd_step(mode, a, st);
   cudaError_t e = set_smem();
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + F::kTR - 1) / F::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
-  const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
+  const int ntiles = INST ? a.inst.ntiles : a.S * tiles_x * tiles_y;
   int grid = num_sms() * F::kCtasPerSm;
   if (grid > ntiles) grid = ntiles;
-  const double cells = a.inst.tiles ? (double)a.inst.ntiles * F::kTR * kTY : (double)a.S * a.nx * a.ny;
+  const double cells = INST ? (double)a.inst.ntiles * F::kTR * kTY : (double)a.S * a.nx * a.ny;
   const int hp = a.prev ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfForward, st, [&] {
-    if (mode == kModeScalar)
-      launch_step_kernel(tma_fwd_kernel<kModeScalar, TR>, grid, dim3(kThreads), fwd_smem<TR>(), st, chained,
-                         a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+    if constexpr (INST)  // scalar constants only (checked above)
+      launch_step_kernel(tma_fwd_kernel<kModeScalar, TR, true>, grid, dim3(kThreads), fwd_smem<TR>(), st,
+                         chained, a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+    else if (mode == kModeScalar)
+      launch_step_kernel(tma_fwd_kernel<kModeScalar, TR, false>, grid, dim3(kThreads), fwd_smem<TR>(), st,
+                         chained, a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
     else
-      launch_step_kernel(tma_fwd_kernel<kModeDField, TR>, grid, dim3(kThreads), fwd_smem<TR>(), st, chained,
-                         a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
+      launch_step_kernel(tma_fwd_kernel<kModeDField, TR, false>, grid, dim3(kThreads), fwd_smem<TR>(), st,
+                         chained, a, cur_map, prev_map, tiles_x, tiles_y, hp, err);
   }, cells * alg_bytes_forward(mode));
 }
 }  // namespace
 
 cudaError_t launch_tma_fwd(int mode, const FwdStep& a, int* err, cudaStream_t st) {
   // the instance tile table holds 16-row tiles
-  if (a.tile_rows == 32 && a.inst.tiles == nullptr) return launch_tma_fwd_t<32>(mode, a, err, st);
-  return launch_tma_fwd_t<16>(mode, a, err, st);
+  if (a.inst.tiles != nullptr) return launch_tma_fwd_t<16, true>(mode, a, err, st);
+  if (a.tile_rows == 32) return launch_tma_fwd_t<32, false>(mode, a, err, st);
+  return launch_tma_fwd_t<16, false>(mode, a, err, st);
 }
 
 namespace {
@@ -1432,6 +1463,7 @@ bool tma_adj_would_run(int mode, const AdjStep& a) {
 
 cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st) {
   const bool dfield = mode == kModeDField;
+  if (a.inst.tiles && dfield) return cudaErrorNotSupported;
   CUtensorMap cur_map, prev_map, u_map, d_map;
   if (!adj_maps(mode, a, &cur_map, &prev_map, &u_map, &d_map))
     return a.inst.tiles ? cudaErrorNotSupported : launch_adj_step(mode, a, st);
@@ -1449,15 +1481,22 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
   const int hu = a.u ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfAdjoint, st, [&] {
-    if (dfield)
-      launch_step_kernel(tma_adj_kernel<kModeDField, 32>, grid, dim3(kThreads), adj_smem<kModeDField, 32>(), st,
-                         chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+    if (a.inst.tiles)  // scalar constants, 16-row tiles (checked by the planner)
+      launch_step_kernel(tma_adj_kernel<kModeScalar, 16, true>, grid, dim3(kThreads),
+                         adj_smem<kModeScalar, 16>(), st, chained, a, cur_map, prev_map, u_map, d_map, tiles_x,
+                         tiles_y, hu, err);
+    else if (dfield)
+      launch_step_kernel(tma_adj_kernel<kModeDField, 32, false>, grid, dim3(kThreads),
+                         adj_smem<kModeDField, 32>(), st, chained, a, cur_map, prev_map, u_map, d_map, tiles_x,
+                         tiles_y, hu, err);
     else if (tr == 32)
-      launch_step_kernel(tma_adj_kernel<kModeScalar, 32>, grid, dim3(kThreads), adj_smem<kModeScalar, 32>(), st,
-                         chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+      launch_step_kernel(tma_adj_kernel<kModeScalar, 32, false>, grid, dim3(kThreads),
+                         adj_smem<kModeScalar, 32>(), st, chained, a, cur_map, prev_map, u_map, d_map, tiles_x,
+                         tiles_y, hu, err);
     else
-      launch_step_kernel(tma_adj_kernel<kModeScalar, 16>, grid, dim3(kThreads), adj_smem<kModeScalar, 16>(), st,
-                         chained, a, cur_map, prev_map, u_map, d_map, tiles_x, tiles_y, hu, err);
+      launch_step_kernel(tma_adj_kernel<kModeScalar, 16, false>, grid, dim3(kThreads),
+                         adj_smem<kModeScalar, 16>(), st, chained, a, cur_map, prev_map, u_map, d_map, tiles_x,
+                         tiles_y, hu, err);
   }, cells * alg_bytes_adjoint(mode));
 }
 
