@@ -755,6 +755,13 @@ __device__ void imaging_role(const ResCommon& c, const ResImg& g, int shot, int 
 }
 
 // ---------------------------------------------------------------- kernel
+// The thread issuing a CTA's bulk state copies (and waiting for them), and
+// the first thread of the forward role's receiver gather: both in middle
+// warps, away from the first and last warps, which compute the CTA's first
+// and last rows (the chain through the neighbours) on square grids.
+constexpr int kStoreTid = kResThreads / 2;
+constexpr int kGatherTid0 = kResThreads / 4;
+
 template <bool DENSE, int RC>
 __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommon c, const ResFwd f,
                                                                    const ResLam a, const ResImg g,
@@ -890,19 +897,27 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   x.R = R;
   x.ny = ny;
   uint32_t parity_bits = 0u;  // bit l: phase parity of bar[l]
-  auto set_levels = [&](int t) {
-    x.cur = Lv(t % 3);
-    x.prev = Lv((t + 2) % 3);
-    x.nxt = Lv((t + 1) % 3);
-    x.nxt_off_b = (uint32_t)((t + 1) % 3) * (uint32_t)level_floats * 4u;
-    const uint32_t lbar = smem_u32(&bar[(t + 1) % 3]);
-    x.up_bar = has_up ? map_rank(lbar, rank - 1) : 0u;
-    x.dn_bar = has_dn ? map_rank(lbar, rank + 1) : 0u;
+  // The levels of step t: cur is ring level cl = t % 3 (kept as a counter by
+  // the step loops), prev cl - 1 and nxt cl + 1 (mod 3).  The neighbours'
+  // mbarriers of a level are at the same offsets in their shared::cluster
+  // windows as this CTA's (mapped once).
+  const uint32_t up_bar0 = has_up ? map_rank(smem_u32(&bar[0]), rank - 1) : 0u;
+  const uint32_t dn_bar0 = has_dn ? map_rank(smem_u32(&bar[0]), rank + 1) : 0u;
+  int cl = 0;
+  auto set_levels = [&]() {
+    const int nl = cl == 2 ? 0 : cl + 1, pl = cl == 0 ? 2 : cl - 1;
+    x.cur = Lv(cl);
+    x.prev = Lv(pl);
+    x.nxt = Lv(nl);
+    x.nxt_off_b = (uint32_t)nl * (uint32_t)level_floats * 4u;
+    x.up_bar = has_up ? up_bar0 + 8u * (uint32_t)nl : 0u;
+    x.dn_bar = has_dn ? dn_bar0 + 8u * (uint32_t)nl : 0u;
   };
+  auto next_level = [&]() { cl = cl == 2 ? 0 : cl + 1; };
   // this step's wait: the neighbours pushed cur's halo during their step t-1
   auto step_wait = [&](int t) -> bool { return t >= 1 && halo_bytes > 0; };
-  auto expect_next = [&](int t) {  // halo of nxt arrives during the neighbours' step t
-    if (tid == 0 && halo_bytes > 0) mbar_arrive_expect_tx(&bar[(t + 1) % 3], halo_bytes);
+  auto expect_next = [&]() {  // halo of nxt arrives during the neighbours' step t
+    if (tid == 0 && halo_bytes > 0) mbar_arrive_expect_tx(&bar[cl == 2 ? 0 : cl + 1], halo_bytes);
   };
   const uint32_t own_bytes = (uint32_t)((size_t)rows * ny * sizeof(float));
   // own rows of a level -> global state at dst (x plane, y plane at y_off)
@@ -945,60 +960,89 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     const float* sig = c.src_signal + (size_t)shot * c.nt;
     float amp_next = (f.i0 < f.i1) ? sig[f.i0] : 0.f;
     Rhs rhs{F, 0.f, c.src_comp, nullptr, nullptr, 0.f};
-    // i % stride, i / stride and the checkpoint phases of i + 1, i + 2, kept
-    // as counters (no integer division in the step loop)
+    // i % stride and i / stride, kept as counters (no integer division in
+    // the step loop)
     int st_r = f.i0 % c.stride, st_q = f.i0 / c.stride;
+    // The state copies are the store thread's alone: its next state slot
+    // and the checkpoint phases of i + 1, i + 2 as counters, the slots as
+    // pointers stepped by additions.
     const int ck_k = f.ckpt != nullptr ? f.ck_k : 1;
     int c1_r = (f.i0 + 1) % ck_k, c1_q = (f.i0 + 1) / ck_k;
     int c2_r = (f.i0 + 2) % ck_k, c2_q = (f.i0 + 2) / ck_k;
+    float* st_next = f.states ? f.states + shot_off : nullptr;
+    // (slot c - 1 of checkpoint c: c1_q, c2_q >= 1 at every step that copies)
+    float* ck_lev0 = f.ckpt ? f.ckpt + ((ptrdiff_t)(c1_q - 1) * 2 + 0) * (ptrdiff_t)f.state_stride + shot_off
+                            : nullptr;
+    float* ck_lev1 = f.ckpt ? f.ckpt + ((ptrdiff_t)(c2_q - 1) * 2 + 1) * (ptrdiff_t)f.state_stride + shot_off
+                            : nullptr;
+    const size_t ck_seg = 2 * f.state_stride;  // floats between checkpoints
+    // The receivers this thread records (entries g, g + kResThreads, ...;
+    // g counts from kGatherTid0 so the gather avoids the first warp, which
+    // also computes the CTA's first row): shared-memory offsets and output
+    // offsets at frame 0, in registers.
+    constexpr int kGath = (kResMaxRec + kResThreads - 1) / kResThreads;
+    const int g0 = (tid + kResThreads - kGatherTid0) % kResThreads;
+    int goff[kGath];
+    size_t gout[kGath];
+    int ngath = 0;
+#pragma unroll
+    for (int h = 0; h < kGath; ++h) {
+      const int e = g0 + h * kResThreads;
+      goff[h] = e < nloc ? rec_list[2 * e] : 0;
+      gout[h] = e < nloc ? (size_t)shot * c.nt_out * c.nrec + rec_list[2 * e + 1] : 0;
+      if (e < nloc) ngath = h + 1;
+    }
     // (the step as a lambda called from one loop: measured 8 % faster on
     // rot256 than the same body written inline in the loop)
     auto fwd_step = [&](int i) {
       const int t = i - f.i0;
-      set_levels(t);
-      expect_next(t);
+      set_levels();
+      expect_next();
       rhs.amp = amp_next * kappa;
       amp_next = (i + 1 < f.i1) ? sig[i + 1] : 0.f;  // in flight during this step
       const bool w = step_wait(t);
-      ring_step<false, false>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err, U);
-      if (w) parity_bits ^= 1u << (t % 3);
+      ring_step<false, false>(T, ks, x, rhs, &bar[cl], (parity_bits >> cl) & 1u, w, c.err, U);
+      if (w) parity_bits ^= 1u << cl;
       // bulk stores issued after the previous step read a level overwritten two
       // steps from now: make sure they are done reading before the barrier
-      if (tid == 0) bulk_wait_read_all();
+      if (tid == kStoreTid) bulk_wait_read_all();
       __syncthreads();
       t_last = t;
-      // u^{i+1} (own rows of nxt) to global memory through the bulk-copy engine
-      float* dst[4] = {nullptr, nullptr, nullptr, nullptr};
-      ptrdiff_t dst_y[4] = {(ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N};  // y plane offset
-      if (f.states) dst[0] = f.states + (size_t)(i - f.i0) * f.state_stride + shot_off;
-      if (f.ckpt != nullptr) {
-        if (c1_r == 0 && c1_q <= f.ck_nseg - 1)
-          dst[1] = f.ckpt + ((size_t)(c1_q - 1) * 2 + 0) * f.state_stride + shot_off;
-        if (c2_r == 0 && c2_q <= f.ck_nseg - 1)
-          dst[2] = f.ckpt + ((size_t)(c2_q - 1) * 2 + 1) * f.state_stride + shot_off;
-      }
+      next_level();
       const bool rec_step = st_r == 0;
       const int frame = st_q;
       if (++st_r == c.stride) { st_r = 0; ++st_q; }
-      if (++c1_r == ck_k) { c1_r = 0; ++c1_q; }
-      if (++c2_r == ck_k) { c2_r = 0; ++c2_q; }
-      if (DENSE && rec_step && f.hist_x) {
-        dst[3] = f.hist_x + ((size_t)shot * c.nt_out + frame) * N;
-        dst_y[3] = f.hist_y - f.hist_x;  // the y history relative to the x history
-      }
-      if (tid == 0 && (dst[0] || dst[1] || dst[2] || dst[3])) {
-        fence_proxy_async();
+      if (tid == kStoreTid) {
+        // u^{i+1} (own rows of nxt) to global memory through the bulk-copy engine
+        float* dst[4] = {st_next, nullptr, nullptr, nullptr};
+        ptrdiff_t dst_y[4] = {(ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N, (ptrdiff_t)N};  // y plane offset
+        if (st_next) st_next += f.state_stride;
+        if (f.ckpt != nullptr) {
+          if (c1_r == 0 && c1_q <= f.ck_nseg - 1) dst[1] = ck_lev0;
+          if (c2_r == 0 && c2_q <= f.ck_nseg - 1) dst[2] = ck_lev1;
+          if (++c1_r == ck_k) { c1_r = 0; ++c1_q; ck_lev0 += ck_seg; }
+          if (++c2_r == ck_k) { c2_r = 0; ++c2_q; ck_lev1 += ck_seg; }
+        }
+        if (DENSE && rec_step && f.hist_x) {
+          dst[3] = f.hist_x + ((size_t)shot * c.nt_out + frame) * N;
+          dst_y[3] = f.hist_y - f.hist_x;  // the y history relative to the x history
+        }
+        if (dst[0] || dst[1] || dst[2] || dst[3]) {
+          fence_proxy_async();
 #pragma unroll
-        for (int d = 0; d < 4; ++d)
-          if (dst[d]) store_level(x.nxt, dst[d], dst_y[d]);
-        bulk_commit();
+          for (int d = 0; d < 4; ++d)
+            if (dst[d]) store_level(x.nxt, dst[d], dst_y[d]);
+          bulk_commit();
+        }
       }
-      if (!DENSE && rec_step && f.tr_x) {
-        for (int e = tid; e < nloc; e += kResThreads) {
-          const int off = rec_list[2 * e], r = rec_list[2 * e + 1];
-          const size_t o = ((size_t)shot * c.nt_out + frame) * c.nrec + r;
-          f.tr_x[o] = T.comp(x.nxt, 0)[off];
-          f.tr_y[o] = T.comp(x.nxt, 1)[off];
+      if (!DENSE && rec_step && ngath > 0 && f.tr_x) {
+        const size_t fo = (size_t)frame * c.nrec;
+#pragma unroll
+        for (int h = 0; h < kGath; ++h) {
+          if (h < ngath) {
+            f.tr_x[gout[h] + fo] = T.comp(x.nxt, 0)[goff[h]];
+            f.tr_y[gout[h] + fo] = T.comp(x.nxt, 1)[goff[h]];
+          }
         }
       }
     };
@@ -1044,17 +1088,24 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     } else if (RC == 0 && !DENSE && next_src >= a.m_lo + 1) {
       load_g(next_src);
     }
-    // Register-resident form: the receivers of this CTA sorted by the thread
-    // that owns their cell (counting sort), so that each owner adds its
-    // cells' residuals to its own registers; entry (cell bit << 16) | e.
+    // The receivers of this CTA sorted by the thread that owns their cell
+    // (counting sort); entry (cell bit << 16) | e.  Register-resident form:
+    // each owner adds its cells' residuals to its own registers.  Generic
+    // form with one unit per thread and the launch's residuals staged in
+    // shared memory: each owner adds them to its own cells of lam^{m+2} in
+    // shared memory before its step, which only it reads this step, so no
+    // barrier is needed (the adds inside the row updates instead measured
+    // slower on rot256: 174 against 159 us per reverse launch).
+    const bool own_inj = RC == 0 && !DENSE && staged && U.items <= kResThreads;
+    const int own_rows = RC > 0 ? RCn : U.rc;  // rows of a thread's unit
     int inj_beg = 0, inj_end = 0;
-    if (RC > 0 && !DENSE && nloc > 0) {
+    if ((RC > 0 || own_inj) && !DENSE && nloc > 0) {
       const int ncq = ny / 4;
       auto owner_of = [&](int e, int& bit) {
         const int off = rec_list[2 * e];
         const int s = off / ny, jj = off - s * ny;  // halo row s = local row + 1
-        const int lr = s - 1, ch = lr / RCn;
-        bit = 4 * (lr - ch * RCn) + (jj & 3);
+        const int lr = s - 1, ch = lr / own_rows;
+        bit = 4 * (lr - ch * own_rows) + (jj & 3);
         return ch * ncq + (jj >> 2);
       };
       for (int k = tid; k < kResThreads; k += kResThreads) inj_cnt[k] = 0;
@@ -1089,10 +1140,11 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
         while (q >= inj_beg && inj[q] > v) { inj[q + 1] = inj[q]; --q; }
         inj[q + 1] = v;
       }
-      for (int p = inj_beg; p < inj_end; ++p) RU.rmask |= 1u << (inj[p] >> 16);
+      if (RC > 0)
+        for (int p = inj_beg; p < inj_end; ++p) RU.rmask |= 1u << (inj[p] >> 16);
     }
     // lam^{m_hi+1} is the imaging partner of u^{m_hi}: store it first
-    if (tid == 0 && a.lbuf && a.store_init) {
+    if (tid == kStoreTid && a.lbuf && a.store_init) {
       fence_proxy_async();
       store_level(Lv(0), a.lbuf + (size_t)(a.m_hi + 1 - a.slot_base) * a.state_stride + shot_off,
                   (ptrdiff_t)N);
@@ -1104,8 +1156,8 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
     auto lam_step = [&](int m, const float (&Cx)[RCn][4], const float (&Cy)[RCn][4], float (&Px)[RCn][4],
                         float (&Py)[RCn][4]) {
       const int t = a.m_hi - m;  // cur = lam^{m+1}, prev = lam^{m+2}, nxt = lam^m
-      set_levels(t);
-      expect_next(t);
+      set_levels();
+      expect_next();
       const bool src_step = sm_r == 0;
       const int frame = sm_q;
       if (sm_r == 0) { sm_r = c.stride - 1; --sm_q; } else { --sm_r; }
@@ -1132,6 +1184,21 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
             }
             Px[cb >> 2][cb & 3] += -gs * gxs;
             Py[cb >> 2][cb & 3] += -gs * gys;
+          }
+        }
+      } else if (own_inj) {
+        // generic form, owner adds: lam^m = (2 lam^{m+1} - lam^{m+2} + ...) + g
+        // with g subtracted from the owner's cells of lam^{m+2}, one receiver
+        // after another (as the shared-memory atomic adds below)
+        if (src_step && inj_end > inj_beg) {
+          const float* gst = F + 2 * (ptrdiff_t)(frame - f_lo) * nloc;
+          float* p0 = T.comp(const_cast<float*>(x.prev), 0);
+          float* p1 = T.comp(const_cast<float*>(x.prev), 1);
+          for (int p = inj_beg; p < inj_end; ++p) {
+            const int e = inj[p] & 0xffff;
+            const int off = rec_list[2 * e];
+            p0[off] += -gs * gst[2 * e];
+            p1[off] += -gs * gst[2 * e + 1];
           }
         }
       } else if (RC == 0 && !DENSE && src_step) {
@@ -1162,15 +1229,16 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
       const bool w = step_wait(t);
       if (RC > 0) {
         if (RU.active)
-          reg_step<true, DENSE, RCn>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err,
-                                     RU, Cx, Cy, Px, Py);
+          reg_step<true, DENSE, RCn>(T, ks, x, rhs, &bar[cl], (parity_bits >> cl) & 1u, w, c.err, RU, Cx, Cy,
+                                     Px, Py);
       } else
-        ring_step<true, DENSE>(T, ks, x, rhs, &bar[t % 3], (parity_bits >> (t % 3)) & 1u, w, c.err, U);
-      if (w) parity_bits ^= 1u << (t % 3);
-      if (tid == 0) bulk_wait_read_all();
+        ring_step<true, DENSE>(T, ks, x, rhs, &bar[cl], (parity_bits >> cl) & 1u, w, c.err, U);
+      if (w) parity_bits ^= 1u << cl;
+      if (tid == kStoreTid) bulk_wait_read_all();
       __syncthreads();
       t_last = t;
-      if (tid == 0 && a.lbuf && m - a.slot_base >= 0) {
+      next_level();
+      if (tid == kStoreTid && a.lbuf && m - a.slot_base >= 0) {
         fence_proxy_async();
         store_level(x.nxt, a.lbuf + (size_t)(m - a.slot_base) * a.state_stride + shot_off,
                     (ptrdiff_t)N);
@@ -1192,7 +1260,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_kernel(const ResCommo
   // wait for them before this CTA's shared memory goes away.
   if (t_last >= 0 && halo_bytes > 0)
     halo_wait(&bar[(t_last + 1) % 3], (parity_bits >> ((t_last + 1) % 3)) & 1u, c.err);
-  if (tid == 0) bulk_wait_all();
+  if (tid == kStoreTid) bulk_wait_all();
   __syncthreads();
   if (!is_fwd && a.m_hi >= a.m_lo + 1 && al16(a.lam_save) && al16(a.lam_save + a.save_stride)) {
     // lam^{m_lo+1} (level of step t_last + 1) and lam^{m_lo+2} -> lam_save,
