@@ -267,8 +267,10 @@ struct Rhs {
 
 // One row lr (local) of one column quad j: windows w[0..1] hold halo rows
 // lr, lr+1 on entry; loads halo row lr+2, computes, stores, pushes boundary
-// rows to the neighbours, shifts the windows.
-template <bool LAM, bool DENSE>
+// rows to the neighbours, shifts the windows.  EDGE = false: lr is neither
+// the CTA's first nor its last row (interior rows carry no push tests:
+// measured 2.5 % faster on rot256).
+template <bool LAM, bool DENSE, bool EDGE = true>
 __device__ __forceinline__ void row_step(const Tile& T, const KSr& ks, const StepCtx& x,
                                          const Rhs& rhs, int lr, int j, float wx[3][6],
                                          float wy[3][6]) {
@@ -312,12 +314,12 @@ __device__ __forceinline__ void row_step(const Tile& T, const KSr& ks, const Ste
   const float4 nvy = make_float4(v2y[0].x, v2y[0].y, v2y[1].x, v2y[1].y);
   *reinterpret_cast<float4*>(T.comp(x.nxt, 0) + T.at(s, j)) = nvx;
   *reinterpret_cast<float4*>(T.comp(x.nxt, 1) + T.at(s, j)) = nvy;
-  if (lr == 0 && x.up_base) {  // into rank-1's bottom halo row
+  if (EDGE && lr == 0 && x.up_base) {  // into rank-1's bottom halo row
     const uint32_t o = x.nxt_off_b + 4u * (uint32_t)T.at(x.R + 1, j);
     st_async16(x.up_base + o, nvx, x.up_bar);
     st_async16(x.up_base + o + 4u * (uint32_t)T.plane, nvy, x.up_bar);
   }
-  if (lr == x.rows - 1 && x.dn_base) {  // into rank+1's top halo row
+  if (EDGE && lr == x.rows - 1 && x.dn_base) {  // into rank+1's top halo row
     const uint32_t o = x.nxt_off_b + 4u * (uint32_t)T.at(0, j);
     st_async16(x.dn_base + o, nvx, x.dn_bar);
     st_async16(x.dn_base + o + 4u * (uint32_t)T.plane, nvy, x.dn_bar);
@@ -339,29 +341,29 @@ __device__ __forceinline__ void load_windows(const Tile& T, const StepCtx& x, in
 // Rows a .. a+n-1 with windows already holding local rows a-1, a; on return
 // they hold rows a+n-1, a+n.  Counts up to 4 are unrolled (window shifts
 // become register renames).
-template <bool LAM, bool DENSE>
+template <bool LAM, bool DENSE, bool EDGE = true>
 __device__ __forceinline__ void rows_from(const Tile& T, const KSr& ks, const StepCtx& x,
                                           const Rhs& rhs, int a, int n, int j, float wx[3][6],
                                           float wy[3][6]) {
   switch (n) {
     case 0: return;
     case 1:
-      row_step<LAM, DENSE>(T, ks, x, rhs, a, j, wx, wy);
+      row_step<LAM, DENSE, EDGE>(T, ks, x, rhs, a, j, wx, wy);
       return;
     case 2:
 #pragma unroll
-      for (int q = 0; q < 2; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+      for (int q = 0; q < 2; ++q) row_step<LAM, DENSE, EDGE>(T, ks, x, rhs, a + q, j, wx, wy);
       return;
     case 3:
 #pragma unroll
-      for (int q = 0; q < 3; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+      for (int q = 0; q < 3; ++q) row_step<LAM, DENSE, EDGE>(T, ks, x, rhs, a + q, j, wx, wy);
       return;
     case 4:
 #pragma unroll
-      for (int q = 0; q < 4; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+      for (int q = 0; q < 4; ++q) row_step<LAM, DENSE, EDGE>(T, ks, x, rhs, a + q, j, wx, wy);
       return;
     default:
-      for (int q = 0; q < n; ++q) row_step<LAM, DENSE>(T, ks, x, rhs, a + q, j, wx, wy);
+      for (int q = 0; q < n; ++q) row_step<LAM, DENSE, EDGE>(T, ks, x, rhs, a + q, j, wx, wy);
   }
 }
 
@@ -412,7 +414,7 @@ __device__ __forceinline__ void ring_step(const Tile& T, const KSr& ks, const St
     float wx[3][6], wy[3][6];
     if (active && ia < ib) {
       load_windows(T, x, ia, 4 * qc, wx, wy);
-      rows_from<LAM, DENSE>(T, ks, x, rhs, ia, ib - ia, 4 * qc, wx, wy);
+      rows_from<LAM, DENSE, false>(T, ks, x, rhs, ia, ib - ia, 4 * qc, wx, wy);  // no boundary row
     }
     if (wait) halo_wait(cur_bar, parity, err);
     if (active && ra < rb) {
@@ -434,7 +436,7 @@ __device__ __forceinline__ void ring_step(const Tile& T, const KSr& ks, const St
     if (ia < ib) {
       float wx[3][6], wy[3][6];
       load_windows(T, x, ia, 4 * qc, wx, wy);
-      rows_from<LAM, DENSE>(T, ks, x, rhs, ia, ib - ia, 4 * qc, wx, wy);
+      rows_from<LAM, DENSE, false>(T, ks, x, rhs, ia, ib - ia, 4 * qc, wx, wy);  // no boundary row
     }
   }
   if (wait) halo_wait(cur_bar, parity, err);
