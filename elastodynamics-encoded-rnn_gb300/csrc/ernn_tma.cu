@@ -334,21 +334,23 @@ __device__ __forceinline__ TileId grid_tile(TileId id, int nx, int ny) {
   return id;
 }
 
-// Entry t of an instance tile table (canvas plane 0).
-__device__ __forceinline__ TileId table_tile(const InstTiles& in, int t) {
-  const int4 e = in.tiles[t];
-  const int4 b = in.box[2 * e.x];
+// An entry of an instance tile table (canvas plane 0): instance, then the
+// tile's origin and its instance's region [xs, xe) x [ys, ye) as pairs of
+// 16-bit canvas coordinates (row | column << 16; canvases are below 65536
+// cells a side), so one 16-byte load gives the whole tile.
+__device__ __forceinline__ TileId decode_tile(const int4 e) {
   TileId id;
   id.shot = 0;
-  id.x0 = e.y;
-  id.y0 = e.z;
   id.inst = e.x;
-  id.xs = b.x;
-  id.ys = b.y;
-  id.xe = b.z;
-  id.ye = b.w;
+  id.x0 = (int)((unsigned)e.y & 0xffffu);
+  id.y0 = (int)((unsigned)e.y >> 16);
+  id.xs = (int)((unsigned)e.z & 0xffffu);
+  id.ys = (int)((unsigned)e.z >> 16);
+  id.xe = (int)((unsigned)e.w & 0xffffu);
+  id.ye = (int)((unsigned)e.w >> 16);
   return id;
 }
+__device__ __forceinline__ TileId table_tile(const InstTiles& in, int t) { return decode_tile(__ldg(&in.tiles[t])); }
 
 // The tiles t = first, first + stride, ... of a CTA, walked in (shot, row
 // block, column block) coordinates: the stride is split once into the same
@@ -398,17 +400,28 @@ __device__ __forceinline__ TileId step_tile(const InstTiles& in, int t, int tile
   else return tile_of<TR>(t, tiles_x, tiles_y);
 }
 
-// Tile t of a CTA's compute loop.  The grid of tiles is walked in step with
-// t (advanced here); the table needs no walk.
+// Tile t of a CTA's compute loop, whose next tile is t + step (below end).
+// The grid of tiles is walked in step with t (advanced here); table entries
+// are loaded one tile ahead (`ahead` holds tile t's on entry, the next
+// tile's on return), so a tile's entry is in registers when it starts.
 template <bool INST, int TR>
-__device__ __forceinline__ TileId walk_tile(const InstTiles& in, int t, TileWalk<TR>& walk, int nx, int ny) {
+__device__ __forceinline__ TileId walk_tile(const InstTiles& in, int t, int step, int end, int4& ahead,
+                                            TileWalk<TR>& walk, int nx, int ny) {
   if constexpr (INST) {
-    return table_tile(in, t);
+    const TileId id = decode_tile(ahead);
+    if (t + step < end) ahead = __ldg(&in.tiles[t + step]);
+    return id;
   } else {
     const TileId id = grid_tile(walk.id(), nx, ny);
     walk.next();
     return id;
   }
+}
+// The first entry of a CTA's table walk (INST), else zeros.
+template <bool INST>
+__device__ __forceinline__ int4 first_entry(const InstTiles& in, int t, int end) {
+  if constexpr (INST) return t < end ? __ldg(&in.tiles[t]) : make_int4(0, 0, 0, 0);
+  else return make_int4(0, 0, 0, 0);
 }
 
 // 2D tile load (columns, rows) into shared memory: the degradation plane.
@@ -509,10 +522,11 @@ __global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
   const Coefs ks0 = coefs(a.coef);  // every shot's, unless per-shot constants
   TileWalk<F::kTR> walk;
   walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+  int4 ahead = first_entry<INST>(a.inst, blockIdx.x, ntiles);
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = walk_tile<INST>(a.inst, t, walk, nx, ny);
+    const TileId id = walk_tile<INST>(a.inst, t, (int)gridDim.x, ntiles, ahead, walk, nx, ny);
     // per-tile scalars, loaded before the wait (coefficients per shot with
     // per-shot constants)
     const Coef* K = a.coef + (size_t)id.inst * a.coef_stride;
@@ -690,10 +704,11 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
   const Coefs ks0 = coefs(a.coef);  // every shot's, unless per-shot constants
   TileWalk<F::kTR> walk;
   walk.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+  int4 ahead = first_entry<INST>(a.inst, blockIdx.x, ntiles);
   for (int k = 0;; ++k) {
     const int t = blockIdx.x + k * gridDim.x;
     if (t >= ntiles) break;
-    const TileId id = walk_tile<INST>(a.inst, t, walk, nx, ny);
+    const TileId id = walk_tile<INST>(a.inst, t, (int)gridDim.x, ntiles, ahead, walk, nx, ny);
     const Coef* K = a.coef + (size_t)id.inst * a.coef_stride;
     const Coefs ks = a.coef_stride != 0 ? coefs(K) : ks0;
     const float* sig = a.src_signal + (size_t)id.inst * a.nt;
@@ -953,10 +968,11 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE, TR>::kCtasPerSm)
   const Coefs ks0 = coefs(a.coef);  // every shot's, unless per-shot constants
   TileWalk<L::kTR> walk;
   walk.init(t_first, t_step, tiles_x, tiles_y);
+  int4 ahead = first_entry<INST>(a.inst, t_first, t_end);
   for (int k = 0;; ++k) {
     const int t = t_first + k * t_step;
     if (t >= t_end) break;
-    const TileId id = walk_tile<INST>(a.inst, t, walk, nx, ny);
+    const TileId id = walk_tile<INST>(a.inst, t, t_step, t_end, ahead, walk, nx, ny);
     if (MODE == kModeScalar && per_shot && has_u && id.inst != acc_shot) {
       if (acc_shot >= 0) flush(acc_shot);
       acc_shot = id.inst;
@@ -1301,7 +1317,11 @@ __global__ void inst_table_kernel(const InstDesc d, int4* __restrict__ tiles, in
   const int n = inst_tiles(d.nx[b], d.ny[b]);
   for (int t = threadIdx.x; t < n; t += blockDim.x) {
     const int xt = t / tiles_y, yt = t - xt * tiles_y;
-    tiles[d.base[b] + t] = make_int4(k, d.x0[b] + kInstTileRows * xt, d.y0[b] + 64 * yt, 0);
+    // the entry: instance, tile origin, instance region (16-bit pairs)
+    const unsigned rx = (unsigned)(d.x0[b] + kInstTileRows * xt), ry = (unsigned)(d.y0[b] + 64 * yt);
+    const unsigned xs = (unsigned)d.x0[b], ys = (unsigned)d.y0[b];
+    const unsigned xe = xs + (unsigned)d.nx[b], ye = ys + (unsigned)d.ny[b];
+    tiles[d.base[b] + t] = make_int4(k, (int)(rx | (ry << 16)), (int)(xs | (ys << 16)), (int)(xe | (ye << 16)));
   }
   if (threadIdx.x == 0) {
     box[2 * k] = make_int4(d.x0[b], d.y0[b], d.x0[b] + d.nx[b], d.y0[b] + d.ny[b]);
@@ -1354,6 +1374,13 @@ int tma_adj_tile_rows(int mode, int tile_rows) {
 
 namespace {
 inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// CTAs of a persistent launch over `ntiles` tiles with room for `slots`
+// resident CTAs: every slot.  (Spreading the tiles evenly over the fewest
+// CTAs of the same number of waves measured slower, damage512 81.7 -> 88.8
+// ms and multi64 734 -> 737 ms: the memory-bound kernels lose more to the
+// fewer CTAs in flight than the last partial wave costs.)
+inline int persistent_grid(int ntiles, int slots) { return ntiles < slots ? ntiles : slots; }
 }  // namespace
 
 // Steps the tiled kernels cannot take (u^i == 0 at the first step, buffers
@@ -1383,8 +1410,7 @@ cudaError_t launch_tma_fwd2(int mode, const FwdStep& a, int* err, cudaStream_t s
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + F::kTR - 1) / F::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
-  int grid = num_sms() * F::kCtasPerSm;
-  if (grid > ntiles) grid = ntiles;
+  const int grid = persistent_grid(ntiles, num_sms() * F::kCtasPerSm);
   const int hp = a.prev ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
   return tracked_launch(kProfForward, st, [&] {
@@ -1414,8 +1440,7 @@ cudaError_t launch_tma_fwd_t(int mode, const FwdStep& a, int* err, cudaStream_t 
   if (e != cudaSuccess) return e;
   const int tiles_x = (a.nx + F::kTR - 1) / F::kTR, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = INST ? a.inst.ntiles : a.S * tiles_x * tiles_y;
-  int grid = num_sms() * F::kCtasPerSm;
-  if (grid > ntiles) grid = ntiles;
+  const int grid = persistent_grid(ntiles, num_sms() * F::kCtasPerSm);
   const double cells = INST ? (double)a.inst.ntiles * F::kTR * kTY : (double)a.S * a.nx * a.ny;
   const int hp = a.prev ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
@@ -1472,11 +1497,11 @@ cudaError_t launch_tma_adj(int mode, const AdjStep& a, int* err, cudaStream_t st
   const int tr = tma_adj_tile_rows(mode, a.inst.tiles ? 16 : a.tile_rows);
   const int tiles_x = (a.nx + tr - 1) / tr, tiles_y = (a.ny + kTY - 1) / kTY;
   const int ntiles = a.inst.tiles ? a.inst.ntiles : a.S * tiles_x * tiles_y;
-  int grid = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm
-                                 : (tr == 32 ? AdjLayout<kModeScalar, 32>::kCtasPerSm
-                                             : AdjLayout<kModeScalar, 16>::kCtasPerSm));
-  if (grid > ntiles) grid = ntiles;
-  if (grid > kTiledRowsPerShot) grid = kTiledRowsPerShot;
+  int slots = num_sms() * (dfield ? AdjLayout<kModeDField>::kCtasPerSm
+                                  : (tr == 32 ? AdjLayout<kModeScalar, 32>::kCtasPerSm
+                                              : AdjLayout<kModeScalar, 16>::kCtasPerSm));
+  if (slots > kTiledRowsPerShot) slots = kTiledRowsPerShot;  // one partial row per CTA
+  const int grid = persistent_grid(ntiles, slots);
   const double cells = a.inst.tiles ? (double)a.inst.ntiles * tr * kTY : (double)a.S * a.nx * a.ny;
   const int hu = a.u ? 1 : 0;
   const bool chained = a.chained != 0 && chain_tiled(mode);
