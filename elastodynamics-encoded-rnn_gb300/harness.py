@@ -445,14 +445,17 @@ class MultiInversion:
         return np.stack([inv.relative_errors() for inv in self.invs])
 
 
-def canvas_layout(ws, gap_rows=1, gap_cols=4):
+def canvas_layout(ws, gap_rows=1, gap_cols=4, col_align=32):
     """Shelf packing of the instances' grids on one canvas: largest first,
-    shelves of the canvas width (about square overall), regions gap_rows
-    rows and gap_cols columns apart (the cells between them stay zero: the
-    instances' ghost rings).  Returns (X, Y, x0, y0) with x0, y0 per
-    instance in the order of `ws`."""
-    area = sum((w.nx + gap_rows) * (w.ny + gap_cols) for w in ws)
-    width = max(max(w.ny for w in ws) + gap_cols, int(np.ceil(np.sqrt(area) / 64.0)) * 64)
+    shelves of the canvas width (about square overall), regions at least
+    gap_rows rows and gap_cols columns apart (the cells between them stay
+    zero: the instances' ghost rings), each region's first column a multiple
+    of col_align (32 floats: its rows start on 128-byte lines, as a grid's
+    do, so that a tile's own boxes touch no extra sector per row).  Returns
+    (X, Y, x0, y0) with x0, y0 per instance in the order of `ws`."""
+    up = lambda v: -(-v // col_align) * col_align
+    area = sum((w.nx + gap_rows) * up(w.ny + gap_cols) for w in ws)
+    width = max(up(max(w.ny for w in ws) + gap_cols), int(np.ceil(np.sqrt(area) / 64.0)) * 64)
     order = sorted(range(len(ws)), key=lambda k: (-ws[k].nx, -ws[k].ny, k))
     x0, y0 = [0] * len(ws), [0] * len(ws)
     shelf_x, shelf_h, col = 0, 0, 0
@@ -462,7 +465,7 @@ def canvas_layout(ws, gap_rows=1, gap_cols=4):
             shelf_x += shelf_h + gap_rows
             shelf_h, col = 0, 0
         x0[k], y0[k] = shelf_x, col
-        col += w.ny + gap_cols
+        col = up(col + w.ny + gap_cols)
         shelf_h = max(shelf_h, w.nx)
     X = shelf_x + shelf_h
     Y = width
