@@ -65,6 +65,9 @@ def parse(argv=None):
                     help="launch every iteration from the host instead of replaying a CUDA graph")
     ap.add_argument("--no-overlap", action="store_true",
                     help="launch consecutive step kernels without programmatic dependent launch")
+    ap.add_argument("--canvas-parts", type=int, default=2,
+                    help="multi64: split the instances over this many canvases of about equal work, "
+                         "each on its own stream (1: one canvas)")
     ap.add_argument("--grouped", action="store_true",
                     help="multi64: the instances grouped by size, one call per group on 8 streams, "
                          "instead of one canvas with a tile table")
@@ -583,12 +586,33 @@ def multi_grad_errors(inv, max_side=128, count=3):
     return out
 
 
-def canvas_grad_errors(inv, dev, count=64):
+def canvas_set_grad_errors(inv, dev, count=64):
+    """canvas_grad_errors over the canvases of a CanvasSet: the `count`
+    smallest instances of the whole set, instance numbers of the set."""
+    order = sorted(range(len(inv.ws)), key=lambda k: inv.ws[k].nx)[:count]
+    out, secs = [], 0.0
+    for part, members in zip(inv.parts, inv.members):
+        local = [members.index(k) for k in order if k in members]
+        if not local:
+            continue
+        r = canvas_grad_errors(part, dev, select=local)
+        secs += r["oracle_s"]
+        for e in r["per_instance"]:
+            out.append({**e, "instance": members[e["instance"]]})
+    worst = max(out, key=lambda r: r["grad_rel_err"])
+    return {"instances": len(out), "max_fwd_rel_err": max(r["fwd_rel_err"] for r in out),
+            "max_grad_rel_err": worst["grad_rel_err"],
+            "max_grad_rel_err_same_residual": max(r["grad_rel_err_same_residual"] for r in out),
+            "worst": worst, "oracle_s": round(secs, 1), "per_instance": out}
+
+
+def canvas_grad_errors(inv, dev, count=64, select=None):
     """Per-instance trace and gradient error of the canvas iteration against
     the FP64 C oracle (oracle/accuracy.py, the checker), every instance on
     its own grid with its own steps, at the instances' current constants, for
     the misfit of the canvas objective (S x mean over the padded traces) and
-    the same observations.  Instances are checked smallest first."""
+    the same observations.  Instances are checked smallest first (or the
+    instances `select`)."""
     from oracle import oracle as O
     from oracle.accuracy import _rel
     ws, S = inv.ws, len(inv.ws)
@@ -610,7 +634,7 @@ def canvas_grad_errors(inv, dev, count=64):
     rec = inv.geom.rec_idx.detach().cpu().numpy()
     X, Y = inv.canvas
     out, t0 = [], time.perf_counter()
-    for k in sorted(range(S), key=lambda k: ws[k].nx)[:count]:
+    for k in (select if select is not None else sorted(range(S), key=lambda k: ws[k].nx)[:count]):
         w, nt = ws[k], inv.nts[k]
         x0, y0 = inv.x0[k], inv.y0[k]
         rk = ((rec[k] // Y - x0) * w.ny + (rec[k] % Y - y0)).astype(np.int32)
@@ -691,7 +715,8 @@ def run_multi(args, dist):
     else:
         # configuration 5 as one propagation: every instance a region of one
         # canvas, one launch per time step over the running instances' tiles
-        inv = Hn.CanvasInversion(ws, dev, nt=args.nt)
+        inv = (Hn.CanvasInversion(ws, dev, nt=args.nt) if args.canvas_parts <= 1 else
+               Hn.CanvasSet(ws, dev, parts=args.canvas_parts, nt=args.nt))
     setup_s = time.perf_counter() - t0
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(max(args.warmup, 0)):
@@ -754,8 +779,10 @@ def run_multi(args, dist):
         if args.grouped:
             extra["grad_error_vs_fp64"] = multi_grad_errors(inv)
             extra["plain_autograd_loop"] = multi_plain_autograd(inv, dev)
-        else:
+        elif args.canvas_parts <= 1:
             extra["grad_error_vs_fp64"] = canvas_grad_errors(inv, dev, count=args.err_instances)
+        else:
+            extra["grad_error_vs_fp64"] = canvas_set_grad_errors(inv, dev, count=args.err_instances)
     return {
         "metric": "Gcell-steps/s fwd+adj (hand adjoint, one Adam iteration)",
         "value": round(value, 4), "unit": "Gcell-steps/s", "n_gpus": dist.world,
@@ -768,7 +795,11 @@ def run_multi(args, dist):
                                 f"per-shot constants, on 8 streams" if args.grouped else
                                 f"one {inv.canvas[0]}x{inv.canvas[1]} canvas, one launch per step over "
                                 f"a tile table of the running instances (checkpoint every "
-                                f"{inv.geom.ckpt_k})"),
+                                f"{inv.geom.ckpt_k})" if args.canvas_parts <= 1 else
+                                f"{len(inv.parts)} canvases (" + ", ".join(f"{c.canvas[0]}x{c.canvas[1]}"
+                                                                         for c in inv.parts) +
+                                "), each one launch per step over its running instances' tiles, "
+                                "on their own streams"),
                    "cell_steps_per_iter": inv.cell_steps,
                    "path_choice": "measured per group (autotune)" if tuned else args.path,
                    "l2": "flushed between timed iterations (256 MiB write)"},

@@ -486,7 +486,7 @@ class CanvasInversion(_GraphedIteration):
     residual: the sum of the instances' misfits up to a factor per instance
     that Adam's per-parameter step normalisation ignores."""
 
-    def __init__(self, ws, device, lr=1e-2, seed=0, graph=True, nt=None):
+    def __init__(self, ws, device, lr=1e-2, seed=0, graph=True, nt=None, budget_fraction=0.4):
         from .propagate import Instances, choose_ckpt_k
         self.ws = ws
         self.device = device
@@ -521,7 +521,8 @@ class CanvasInversion(_GraphedIteration):
                              src_map=smap, src_origin=torch.tensor(origins, dtype=torch.int32, device=device),
                              stride=1, src_comp=1, rec_idx=rec, instances=inst)
         from ._lib import FLAG_INSTANCES
-        self.geom.ckpt_k = choose_ckpt_k(self.geom, 0, device, flags=FLAG_INSTANCES)
+        self.geom.ckpt_k = choose_ckpt_k(self.geom, 0, device, budget_fraction=budget_fraction,
+                                         flags=FLAG_INSTANCES)
         self.rho = torch.full((S,), RHO, dtype=torch.float32, device=device)
         # observations: the same propagation at the true constants plus
         # Gaussian noise of 0.5 % of each instance's trace RMS (seeded)
@@ -568,3 +569,61 @@ class CanvasInversion(_GraphedIteration):
 
     def constants(self):
         return self.params().detach().double().cpu().numpy()
+
+
+class CanvasSet(_GraphedIteration):
+    """The instances split into `parts` canvases of about equal work
+    (cell-steps, largest first to the lightest part), each a CanvasInversion
+    advanced on its own CUDA stream, the whole iteration one graph.  Each
+    canvas is one launch per step; the canvases' launches overlap, so one
+    canvas's last partial wave of tiles runs beside the other's work."""
+
+    def __init__(self, ws, device, parts=2, lr=1e-2, seed=0, graph=True, nt=None):
+        self.device = device
+        self.ws = ws
+        work = [w.nx * w.ny * (w.nt if nt is None else min(w.nt, nt)) for w in ws]
+        load = [0] * parts
+        members = [[] for _ in range(parts)]
+        for k in sorted(range(len(ws)), key=lambda k: -work[k]):
+            p = min(range(parts), key=lambda q: load[q])
+            members[p].append(k)
+            load[p] += work[k]
+        self.members = [sorted(m) for m in members if m]
+        # each canvas's tape and scratch from its share of the memory budget
+        self.parts = [CanvasInversion([ws[k] for k in m], device, lr=lr, seed=seed, graph=False, nt=nt,
+                                      budget_fraction=0.4 / len(self.members))
+                      for m in self.members]
+        self.streams = [torch.cuda.Stream(device) for _ in self.parts]
+        self.obs = [o for c in self.parts for o in c.obs]
+        self.cell_steps = sum(c.cell_steps for c in self.parts)
+        self.opt = None
+        if graph:
+            self.capture()
+
+    def step_eager(self):
+        main = torch.cuda.current_stream(self.device)
+        losses = []
+        for c, st in zip(self.parts, self.streams):
+            st.wait_stream(main)
+            with torch.cuda.stream(st):
+                losses.append(c.step_eager())
+        for st in self.streams:
+            main.wait_stream(st)
+        return torch.stack([l.detach() for l in losses]).sum()
+
+    def step(self, obs=None):
+        if obs is not None:
+            for dst, src in zip(self.obs, obs):
+                if dst.data_ptr() != src.data_ptr():
+                    dst.copy_(src, non_blocking=True)
+        if self.graph is None:
+            return self.step_eager()
+        self.graph.replay()
+        return self._loss
+
+    def gradient(self):
+        """Gradients in the order of `ws`."""
+        g = torch.empty((len(self.ws), 6), dtype=torch.float32, device=self.device)
+        for c, m in zip(self.parts, self.members):
+            g[m] = c.theta.grad
+        return g.reshape(-1)

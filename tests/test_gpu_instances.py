@@ -157,3 +157,27 @@ def test_canvas_inversion_graph_replay_equals_eager():
     assert np.isfinite(loss_g) and abs(loss_g - loss_e) <= 1e-6 * abs(loss_e), (loss_g, loss_e)
     assert rel(grad_g, grad_e) <= 1e-6, rel(grad_g, grad_e)
     E.check_device_status()
+
+
+def test_canvas_set_parts_equal_single_canvases():
+    # two canvases of about equal work on their own streams, one graph: each
+    # part's loss and gradient equal those of a canvas of the same instances
+    # run alone (same kernels, same constants), and the set's gradient comes
+    # back in the instances' order
+    ws = Hn.multi_instances(6, sides=[128, 192, 128, 256, 192, 128])
+    cs = Hn.CanvasSet(ws, DEV, parts=2, graph=True, nt=300)
+    assert sorted(k for m in cs.members for k in m) == list(range(len(ws)))
+    theta = [p.theta.detach().clone() for p in cs.parts]
+    loss = float(cs.step())
+    grad = cs.gradient().detach().double().cpu().numpy().reshape(len(ws), 6)
+    total = 0.0
+    for members, th in zip(cs.members, theta):
+        ref = Hn.CanvasInversion([ws[k] for k in members], DEV, graph=False, nt=300,
+                                 budget_fraction=0.4 / len(cs.members))
+        with torch.no_grad():
+            ref.theta.copy_(th)
+        total += float(ref.step())
+        g = ref.gradient().detach().double().cpu().numpy().reshape(len(members), 6)
+        assert rel(grad[members], g) <= 1e-6, rel(grad[members], g)
+    assert np.isfinite(loss) and abs(loss - total) <= 1e-6 * abs(total), (loss, total)
+    E.check_device_status()
