@@ -463,17 +463,23 @@ static int forward_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPl
 
   InstTiles itab{nullptr, nullptr, 0};
   if (ip != nullptr) {
-    // instances: the tiled kernels over the tile table only; every state
-    // buffer starts at zero (cells between the regions are never written:
-    // the instances' ghost rings), trace frames past an instance's steps too
+    // instances: the tiled kernels over the tile table only.  A and B start
+    // at zero (B stands for u^0); the stored states need only the instances'
+    // ghost rings zeroed (the cells between the regions are never written,
+    // and outside the regions the kernels read only the rings); trace frames
+    // past an instance's steps are zero
     if (p->path != ERNN_PATH_AUTO && p->path != ERNN_PATH_TILED) return ERNN_ERR_UNSUPPORTED;
     if (!tma_eligible(p->mode, p->nx, p->ny, 1)) return ERNN_ERR_UNSUPPORTED;
     itab.tiles = reinterpret_cast<int4*>(at(tape, pl.t_inst));
     itab.box = reinterpret_cast<int4*>(at(tape, pl.t_inst + align_up(inst_table_bound(p->nx, p->ny, p->nshots) *
                                                                        sizeof(int4))));
     ERNN_CUDA(launch_inst_table(ip->d, const_cast<int4*>(itab.tiles), const_cast<int4*>(itab.box), st));
-    const size_t zero_to = with_tape ? pl.t_total_tape : pl.t_total_notape;
-    ERNN_CUDA(cudaMemsetAsync(at(tape, pl.t_A), 0, zero_to - pl.t_A, st));
+    ERNN_CUDA(cudaMemsetAsync(at(tape, pl.t_A), 0, 2 * pl.state_bytes, st));  // A and B are adjacent
+    if (with_tape) {
+      const int nstore = pl.store_all ? p->nt : 2 * (pl.nseg - 1);
+      ERNN_CUDA(launch_inst_ring_zero(fat(tape, pl.t_store), pl.state_bytes / sizeof(float), nstore, p->nx, p->ny,
+                                      itab.box, p->nshots, st));
+    }
     const size_t tr_bytes = (size_t)p->nshots * pl.nt_out * p->nrec * sizeof(float);
     ERNN_CUDA(cudaMemsetAsync(out_ux, 0, tr_bytes, st));
     ERNN_CUDA(cudaMemsetAsync(out_uy, 0, tr_bytes, st));
@@ -595,8 +601,8 @@ static int adjoint_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPl
   InstTiles itab{nullptr, nullptr, 0};
   if (ip != nullptr) {
     // instances: the tiled kernels over the tile table only; the zero state
-    // and the recompute segment start at zero (cells between the regions are
-    // never written: the instances' ghost rings)
+    // starts at zero, the recompute segment's states need only the
+    // instances' ghost rings zeroed (as the stored states of the forward)
     if (p->path != ERNN_PATH_AUTO && p->path != ERNN_PATH_TILED) return ERNN_ERR_UNSUPPORTED;
     if (!tma_eligible(p->mode, p->nx, p->ny, 1)) return ERNN_ERR_UNSUPPORTED;
     itab.tiles = reinterpret_cast<int4*>(at(scratch, pl.s_inst));
@@ -604,7 +610,9 @@ static int adjoint_impl(const ErnnProblem* p, const ErnnInputs* in, const InstPl
                                                                           sizeof(int4))));
     ERNN_CUDA(launch_inst_table(ip->d, const_cast<int4*>(itab.tiles), const_cast<int4*>(itab.box), st));
     ERNN_CUDA(cudaMemsetAsync(at(scratch, pl.s_zero), 0, pl.state_bytes, st));
-    if (!pl.store_all) ERNN_CUDA(cudaMemsetAsync(at(scratch, pl.s_seg), 0, (size_t)pl.k * pl.state_bytes, st));
+    if (!pl.store_all)
+      ERNN_CUDA(launch_inst_ring_zero(fat(scratch, pl.s_seg), pl.state_bytes / sizeof(float), pl.k, p->nx, p->ny,
+                                      itab.box, p->nshots, st));
   }
 
   if (ip == nullptr && (p->path == ERNN_PATH_AUTO || p->path == ERNN_PATH_RESIDENT)) {

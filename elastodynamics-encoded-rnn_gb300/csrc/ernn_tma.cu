@@ -1343,6 +1343,46 @@ __global__ void inst_tile_flags_kernel(const int32_t* __restrict__ rec_idx, int 
 }
 }  // namespace
 
+namespace {
+// Block (k, s0) zeroes instance k's ghost ring in states s0, s0 + gridDim.y,
+// ...: the rows above and below the region (corners included) and the
+// columns left and right of it, clipped to the canvas.
+__global__ void inst_ring_zero_kernel(float* __restrict__ base, size_t slot_floats, int nslots, int nx, int ny,
+                                      const int4* __restrict__ box) {
+  const int4 r = box[2 * blockIdx.x];  // region [r.x, r.z) x [r.y, r.w)
+  const int W = r.w - r.y + 2, H = r.z - r.x;
+  const size_t N = (size_t)nx * ny;
+  const int n = 2 * W + 2 * H;
+  for (int s = blockIdx.y; s < nslots; s += gridDim.y) {
+    float* p = base + (size_t)s * slot_floats;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+      int gi, gj;
+      if (e < 2 * W) {
+        gi = e < W ? r.x - 1 : r.z;
+        gj = r.y - 1 + (e < W ? e : e - W);
+      } else {
+        const int f = e - 2 * W;
+        gi = r.x + (f < H ? f : f - H);
+        gj = f < H ? r.y - 1 : r.w;
+      }
+      if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+      const size_t o = (size_t)gi * ny + gj;
+      p[o] = 0.f;
+      p[N + o] = 0.f;
+    }
+  }
+}
+}  // namespace
+
+cudaError_t launch_inst_ring_zero(float* base, size_t slot_floats, int nslots, int nx, int ny, const int4* box,
+                                  int count, cudaStream_t st) {
+  if (count < 1 || nslots < 1) return cudaSuccess;
+  const dim3 grid((unsigned)count, (unsigned)(nslots < 1024 ? nslots : 1024));
+  return tracked_launch(kProfOther, st, [&] {
+    inst_ring_zero_kernel<<<grid, 256, 0, st>>>(base, slot_floats, nslots, nx, ny, box);
+  });
+}
+
 cudaError_t launch_inst_table(const InstDesc& d, int4* tiles, int4* box, cudaStream_t st) {
   if (d.count < 1) return cudaSuccess;
   return tracked_launch(kProfOther, st, [&] { inst_table_kernel<<<d.count, 256, 0, st>>>(d, tiles, box); });

@@ -52,6 +52,14 @@ __host__ __device__ inline int inst_tiles(int nx, int ny) {
 // Writes the tile table (sum of inst_tiles entries, in the order of d) and
 // the per-instance boxes (2 x S int4) described in InstTiles.
 cudaError_t launch_inst_table(const InstDesc& d, int4* tiles, int4* box, cudaStream_t st);
+// Zeroes the one-cell ghost ring around every instance region (box[2 k]) in
+// `nslots` canvas states of slot_floats floats from `base` (both components
+// of each).  The kernels read a state outside the instance regions only
+// there: cells further out feed only cells that are never stored, and the
+// imaging masks them by selection, so a recompute segment or checkpoint
+// buffer needs its rings zeroed, not the whole canvas.
+cudaError_t launch_inst_ring_zero(float* base, size_t slot_floats, int nslots, int nx, int ny, const int4* box,
+                                  int count, cudaStream_t st);
 // Receiver table of the instance tile table: flags[t] = 1 where the tile's
 // instance has a receiver in it (ntiles bytes).
 cudaError_t launch_inst_tile_flags(const int32_t* rec_idx, int S, int nrec, int ny, const int4* box,

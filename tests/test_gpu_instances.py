@@ -181,3 +181,23 @@ def test_canvas_set_parts_equal_single_canvases():
         assert rel(grad[members], g) <= 1e-6, rel(grad[members], g)
     assert np.isfinite(loss) and abs(loss - total) <= 1e-6 * abs(total), (loss, total)
     E.check_device_status()
+
+
+def test_instances_ignore_stale_workspace():
+    # Only the instances' ghost rings of the stored and recomputed states are
+    # zeroed per call: the rest of the canvas outside the regions may hold
+    # anything.  Fill the caching allocator's free blocks with NaN so the
+    # next run's tape and scratch come from them: traces and gradients must
+    # be bitwise those of a run on fresh memory.
+    insts = _instances(SPECS, seed=7)
+    geom = _canvas(insts, ckpt_k=25)
+    wx, wy = _weights(insts, geom.nt)
+    ref = _run_canvas(insts, geom, wx, wy)
+    torch.cuda.empty_cache()
+    junk = [torch.full((n << 18,), float("nan"), device=DEV) for n in (1, 2, 4, 8, 16, 32, 64, 128) for _ in range(2)]
+    torch.cuda.synchronize()
+    del junk
+    out = _run_canvas(insts, geom, wx, wy)
+    for a, b in zip(ref, out):
+        assert np.array_equal(a, b)
+    E.check_device_status()
