@@ -652,12 +652,12 @@ def canvas_grad_errors(inv, dev, count=64, select=None):
         ry = 2.0 * S * (py32[k:k + 1, :nt] - oy[k:k + 1, :nt]) / count_all
         sC, _ = O.adjoint_ckpt(case, kk, ck, rx, ry, "f64")
         s = inv.scale[k].detach().double().cpu().numpy()
-        rec = {"instance": k, "side": w.nx, "nt": nt,
+        row = {"instance": k, "side": w.nx, "nt": nt,
                "fwd_rel_err": round(max(_rel(px32[k:k + 1, :nt], qx), _rel(py32[k:k + 1, :nt], qy)), 9),
                "residual_rel_diff": round(max(_rel(rx, gx), _rel(ry, gy)), 9),
                "grad_rel_err": round(_rel(g32[k] * s, gC * s), 9),
                "grad_rel_err_same_residual": round(_rel(g32[k] * s, sC * s), 9)}
-        if rec["grad_rel_err"] > 1e-4:
+        if row["grad_rel_err"] > 1e-4:
             # the same scheme in FP32 (the C oracle: FP32 fields and arithmetic,
             # FP64 sums): the gradient difference any FP32 evaluation carries
             # where the residual is this sensitive to the forward
@@ -665,8 +665,8 @@ def canvas_grad_errors(inv, dev, count=64, select=None):
             hx = 2.0 * S * (fx.astype(np.float64) - ox[k:k + 1, :nt]) / count_all
             hy = 2.0 * S * (fy.astype(np.float64) - oy[k:k + 1, :nt]) / count_all
             fC, _ = O.adjoint_ckpt(case, kk, ck32, hx, hy, "f32")
-            rec["oracle_fp32_grad_rel_err"] = round(_rel(fC * s, gC * s), 9)
-        out.append(rec)
+            row["oracle_fp32_grad_rel_err"] = round(_rel(fC * s, gC * s), 9)
+        out.append(row)
     worst = max(out, key=lambda r: r["grad_rel_err"]) if out else None
     return {"instances": len(out), "max_fwd_rel_err": max(r["fwd_rel_err"] for r in out),
             "max_grad_rel_err": worst["grad_rel_err"],
