@@ -666,6 +666,9 @@ def canvas_grad_errors(inv, dev, count=64, select=None):
             hy = 2.0 * S * (fy.astype(np.float64) - oy[k:k + 1, :nt]) / count_all
             fC, _ = O.adjoint_ckpt(case, kk, ck32, hx, hy, "f32")
             row["oracle_fp32_grad_rel_err"] = round(_rel(fC * s, gC * s), 9)
+            row["oracle_fp32_fwd_rel_err"] = round(max(_rel(fx.astype(np.float64), qx),
+                                                       _rel(fy.astype(np.float64), qy)), 9)
+            row["oracle_fp32_residual_rel_diff"] = round(max(_rel(hx, gx), _rel(hy, gy)), 9)
         out.append(row)
     worst = max(out, key=lambda r: r["grad_rel_err"]) if out else None
     return {"instances": len(out), "max_fwd_rel_err": max(r["fwd_rel_err"] for r in out),
