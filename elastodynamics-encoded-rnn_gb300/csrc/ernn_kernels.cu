@@ -290,15 +290,17 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
         ly *= cf[k][0];
       }
     }
-    const float px = prev ? prev[o] : 0.f;
-    const float py = prev ? prev[N + o] : 0.f;
-    float vx = (2.f * st.cx - px) + lx;
-    float vy = (2.f * st.cy - py) + ly;
+    // the load joins the operator sum before the update, as in the
+    // reference's (A u + f) / rho: one rounding of the increment into 2 c - p
     const int sa = gi - ox, sb = gj - oy;
     if (has_src && sa >= 0 && sa < a.bx && sb >= 0 && sb < a.by) {
-      const float f = amp * a.src_map[((size_t)s * a.bx + sa) * a.by + sb];
-      if (a.src_comp == 0) vx += f; else vy += f;
+      const float f = a.src_map[((size_t)s * a.bx + sa) * a.by + sb];  // L + amp f, one rounding
+      if (a.src_comp == 0) lx = fmaf(amp, f, lx); else ly = fmaf(amp, f, ly);
     }
+    const float px = prev ? prev[o] : 0.f;
+    const float py = prev ? prev[N + o] : 0.f;
+    const float vx = (2.f * st.cx - px) + lx;
+    const float vy = (2.f * st.cy - py) + ly;
     out[o] = vx;
     out[N + o] = vy;
     if (a.copy0) {

@@ -277,31 +277,34 @@ __device__ __forceinline__ void row_step(const Tile& T, const KSr& ks, const Ste
   const int ny = x.ny;
   const int s = lr + 1;
   float* cur = const_cast<float*>(x.cur);
+  float4 fl = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!LAM) fl = *reinterpret_cast<const float4*>(rhs.F + lr * ny + j);  // first: it feeds the operator sum
   load_row6(T.comp(cur, 0) + T.at(s + 1, 0), j, ny, wx[2]);
   load_row6(T.comp(cur, 1) + T.at(s + 1, 0), j, ny, wy[2]);
   Quad st;
   quad_stencils(wx, wy, st);
   const float4 pvx = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(x.prev), 0) + T.at(s, j));
   const float4 pvy = *reinterpret_cast<const float4*>(T.comp(const_cast<float*>(x.prev), 1) + T.at(s, j));
-  // v = (2 c - p) + L u (2 c is exact: one rounding either way), then the
-  // right-hand side; two cells per instruction
+  // v = (2 c - p) + (L u + f) (2 c is exact: one rounding either way); two
+  // cells per instruction.  The load joins the operator sum before the
+  // update, as in the reference's (A u + f) / rho: one rounding of the
+  // increment into 2 c - p.  (Added after the update instead, the forward's
+  // rounding near the source projects onto the gradient: ten times the FP32
+  // reference's gradient error close to convergence.)
   float2 v2x[2], v2y[2];
 #pragma unroll
   for (int p = 0; p < 2; ++p) {
     float2 lx, ly;
     lq2(ks, st, p, lx, ly);
+    if (!LAM) {  // L + amp F, one rounding
+      if (rhs.src_comp == 0) lx = __ffma2_rn(dup2(rhs.amp), pair4(fl, p), lx);
+      else ly = __ffma2_rn(dup2(rhs.amp), pair4(fl, p), ly);
+    }
     const float2 px = pair4(pvx, p), py = pair4(pvy, p);
     v2x[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cx, p), neg2(px)), lx);
     v2y[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cy, p), neg2(py)), ly);
   }
-  if (!LAM) {
-    const float4 fl = *reinterpret_cast<const float4*>(rhs.F + lr * ny + j);
-#pragma unroll
-    for (int p = 0; p < 2; ++p) {
-      const float2 fz = __fmul2_rn(dup2(rhs.amp), pair4(fl, p));
-      if (rhs.src_comp == 0) v2x[p] = __fadd2_rn(v2x[p], fz); else v2y[p] = __fadd2_rn(v2y[p], fz);
-    }
-  } else if (DENSE && rhs.gx != nullptr) {
+  if (LAM && DENSE && rhs.gx != nullptr) {
     const float4 a4 = *reinterpret_cast<const float4*>(rhs.gx + (size_t)lr * ny + j);
     const float4 b4 = *reinterpret_cast<const float4*>(rhs.gy + (size_t)lr * ny + j);
 #pragma unroll
@@ -540,24 +543,23 @@ __device__ __forceinline__ void reg_row(const Tile& T, const KSr& ks, const Step
   }
   ref_stencils(ax, bx, dx, st.xx_x, st.yy_x, st.xy_x);
   ref_stencils(ay, by, dy, st.xx_y, st.yy_y, st.xy_y);
+  // the load joins the operator sum before the update, as in row_step
+  const bool src = !LAM && src_row;
+  float4 fl = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (src) fl = *reinterpret_cast<const float4*>(rhs.F + lr * ny + j);
   float2 v2x[2], v2y[2];
 #pragma unroll
   for (int p = 0; p < 2; ++p) {
     float2 lx, ly;
     lq2(ks, st, p, lx, ly);
+    if (src) {  // L + amp F, one rounding
+      if (rhs.src_comp == 0) lx = __ffma2_rn(dup2(rhs.amp), pair4(fl, p), lx);
+      else ly = __ffma2_rn(dup2(rhs.amp), pair4(fl, p), ly);
+    }
     v2x[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cx, p), neg2(pair(px, p))), lx);
     v2y[p] = __fadd2_rn(__ffma2_rn(dup2(2.f), pair(st.cy, p), neg2(pair(py, p))), ly);
   }
-  if (!LAM) {
-    if (src_row) {
-      const float4 fl = *reinterpret_cast<const float4*>(rhs.F + lr * ny + j);
-#pragma unroll
-      for (int p = 0; p < 2; ++p) {
-        const float2 fz = __fmul2_rn(dup2(rhs.amp), pair4(fl, p));
-        if (rhs.src_comp == 0) v2x[p] = __fadd2_rn(v2x[p], fz); else v2y[p] = __fadd2_rn(v2y[p], fz);
-      }
-    }
-  } else if (DENSE && rhs.gx != nullptr) {
+  if (LAM && DENSE && rhs.gx != nullptr) {
     const float4 a4 = *reinterpret_cast<const float4*>(rhs.gx + (size_t)lr * ny + j);
     const float4 b4 = *reinterpret_cast<const float4*>(rhs.gy + (size_t)lr * ny + j);
 #pragma unroll

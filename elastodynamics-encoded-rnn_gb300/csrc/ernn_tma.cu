@@ -292,8 +292,46 @@ __device__ __forceinline__ void apply2(const Coefs& k, const Sums4& s, int p, fl
   ly = fma2(dup2(k.k26h), pair(s.xy_y, p), ly);
 }
 
-// Leapfrog update of a quad: v = (2 c - p) + w (L u), w = 1 unless WEIGHT
-// (2 c is exact, so 2 c - p is one rounding either way).
+// The forward update in two parts, so that the load joins the operator sum
+// before the update, as in the reference's (A u + f) / rho: oper4 writes the
+// operator terms w (L u) of a quad (w = 1 unless WEIGHT) into vx, vy, the
+// caller adds the load there, and update4 turns them into v = (2 c - p) +
+// (w (L u) + f), one rounding of the increment into 2 c - p.  (Added after
+// the update instead, the forward's rounding near the source projects onto
+// the gradient: ten times the FP32 reference's gradient error close to
+// convergence.)
+template <bool WEIGHT>
+__device__ __forceinline__ void oper4(const Coefs& k, const Sums4& s, const float4& w, float vx[4], float vy[4]) {
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    float2 lx, ly;
+    apply2(k, s, p, lx, ly);
+    if (WEIGHT) {
+      lx = __fmul2_rn(lx, pair4(w, p));
+      ly = __fmul2_rn(ly, pair4(w, p));
+    }
+    vx[2 * p] = lx.x;
+    vx[2 * p + 1] = lx.y;
+    vy[2 * p] = ly.x;
+    vy[2 * p + 1] = ly.y;
+  }
+}
+__device__ __forceinline__ void update4(const float cx[4], const float cy[4], const float4& pvx, const float4& pvy,
+                                        float vx[4], float vy[4]) {
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const float2 px = pair4(pvx, p), py = pair4(pvy, p);
+    const float2 ax = __fadd2_rn(fma2(dup2(2.f), pair(cx, p), neg2(px)), make_float2(vx[2 * p], vx[2 * p + 1]));
+    const float2 ay = __fadd2_rn(fma2(dup2(2.f), pair(cy, p), neg2(py)), make_float2(vy[2 * p], vy[2 * p + 1]));
+    vx[2 * p] = ax.x;
+    vx[2 * p + 1] = ax.y;
+    vy[2 * p] = ay.x;
+    vy[2 * p + 1] = ay.y;
+  }
+}
+
+// Leapfrog update of a quad without a load: v = (2 c - p) + w (L u), w = 1
+// unless WEIGHT (2 c is exact, so 2 c - p is one rounding either way).
 template <bool WEIGHT>
 __device__ __forceinline__ void leap4(const Coefs& k, const Sums4& s, const float cx[4], const float cy[4],
                                       const float4& pvx, const float4& pvy, const float4& w, float vx[4],
@@ -570,19 +608,20 @@ __global__ void __launch_bounds__(kThreads, FwdLayoutT<TR>::kCtasPerSm)
         pvy = *reinterpret_cast<const float4*>(pb + F::kTR * kTY + r * kTY + j);
       }
       float vx[4], vy[4];
-      leap4<MODE == kModeDField>(ks, st, st.cx, st.cy, pvx, pvy, MODE == kModeDField ? w4[q2] : pvx, vx, vy);
       // source box: rows and columns of this thread's 4 cells inside it
       const int sa = gi - ox;
+      oper4<MODE == kModeDField>(ks, st, MODE == kModeDField ? w4[q2] : pvx, vx, vy);
       if (has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int sb = gj + q - oy;
           if ((unsigned)sb < (unsigned)a.by) {
-            const float f = amp * a.src_map[((size_t)id.inst * a.bx + sa) * a.by + sb];
-            if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
+            const float f = a.src_map[((size_t)id.inst * a.bx + sa) * a.by + sb];  // L + amp f, one rounding
+            if (a.src_comp == 0) vx[q] = fmaf(amp, f, vx[q]); else vy[q] = fmaf(amp, f, vy[q]);
           }
         }
       }
+      update4(st.cx, st.cy, pvx, pvy, vx, vy);
       if (gi < id.xe && gj < id.ye) {
         const float4 nvx = make_float4(vx[0], vx[1], vx[2], vx[3]);
         const float4 nvy = make_float4(vy[0], vy[1], vy[2], vy[3]);
@@ -749,22 +788,23 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
       const int gi = id.x0 + m - 1, gj = id.y0 - 4 + b;  // ny % 4 == 0: a quad is in or out
       const bool inside = gi >= id.xs && gi < id.xe && gj >= id.ys && gj < id.ye;
       float vx[4], vy[4];
-      leap4<false>(ks, st, st.cx, st.cy, pvx, pvy, pvx, vx, vy);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        vx[q] = inside ? vx[q] : 0.f;
-        vy[q] = inside ? vy[q] : 0.f;
-      }
       const int sa = gi - ox;
+      oper4<false>(ks, st, pvx, vx, vy);
       if (inside && has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int sb = gj + q - oy;
           if ((unsigned)sb < (unsigned)a.by) {
-            const float f = amp1 * smap[(size_t)sa * a.by + sb];
-            if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
+            const float f = smap[(size_t)sa * a.by + sb];  // L + amp f, one rounding
+            if (a.src_comp == 0) vx[q] = fmaf(amp1, f, vx[q]); else vy[q] = fmaf(amp1, f, vy[q]);
           }
         }
+      }
+      update4(st.cx, st.cy, pvx, pvy, vx, vy);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        vx[q] = inside ? vx[q] : 0.f;
+        vy[q] = inside ? vy[q] : 0.f;
       }
       const float4 nvx = make_float4(vx[0], vx[1], vx[2], vx[3]);
       const float4 nvy = make_float4(vy[0], vy[1], vy[2], vy[3]);
@@ -794,18 +834,19 @@ __global__ void __launch_bounds__(kThreads, Fwd2Layout::kCtasPerSm)
       const float4 pvy = *reinterpret_cast<const float4*>(cb + F::kBH2 * kBW + (rg + 2) * kBW + j + 4);
       const int gi = id.x0 + rg, gj = id.y0 + j;
       float vx[4], vy[4];
-      leap4<false>(ks, st, st.cx, st.cy, pvx, pvy, pvx, vx, vy);
       const int sa = gi - ox;
+      oper4<false>(ks, st, pvx, vx, vy);
       if (has_src && (unsigned)sa < (unsigned)a.bx && gj + 3 >= oy && gj < oy + a.by) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int sb = gj + q - oy;
           if ((unsigned)sb < (unsigned)a.by) {
-            const float f = amp2 * smap[(size_t)sa * a.by + sb];
-            if (a.src_comp == 0) vx[q] += f; else vy[q] += f;
+            const float f = smap[(size_t)sa * a.by + sb];  // L + amp f, one rounding
+            if (a.src_comp == 0) vx[q] = fmaf(amp2, f, vx[q]); else vy[q] = fmaf(amp2, f, vy[q]);
           }
         }
       }
+      update4(st.cx, st.cy, pvx, pvy, vx, vy);
       if (gi < id.xe && gj < id.ye) {
         const size_t o = (size_t)gi * ny + gj;
         *reinterpret_cast<float4*>(out2 + o) = make_float4(vx[0], vx[1], vx[2], vx[3]);
@@ -968,11 +1009,18 @@ __global__ void __launch_bounds__(kThreads, AdjLayout<MODE, TR>::kCtasPerSm)
   const Coefs ks0 = coefs(a.coef);  // every shot's, unless per-shot constants
   TileWalk<L::kTR> walk;
   walk.init(t_first, t_step, tiles_x, tiles_y);
-  int4 ahead = first_entry<INST>(a.inst, t_first, t_end);
+  // (table entries loaded when a tile starts: one ahead measured the same
+  // here and needs registers this kernel does not have)
   for (int k = 0;; ++k) {
     const int t = t_first + k * t_step;
     if (t >= t_end) break;
-    const TileId id = walk_tile<INST>(a.inst, t, t_step, t_end, ahead, walk, nx, ny);
+    TileId id;
+    if constexpr (INST) {
+      id = table_tile(a.inst, t);
+    } else {
+      id = grid_tile(walk.id(), nx, ny);
+      walk.next();
+    }
     if (MODE == kModeScalar && per_shot && has_u && id.inst != acc_shot) {
       if (acc_shot >= 0) flush(acc_shot);
       acc_shot = id.inst;

@@ -57,12 +57,13 @@ def source_distance_mask(w, radius):
 
 
 def workload_errors(w, device, nt=None, ckpt_k=None, path=0, oracle_k=None, fp32_floor=False,
-                    source_radius=16):
+                    source_radius=16, C=None):
     """Errors of the CUDA path on workload `w` (scalar constants at the
     seeded initial guess, or the degradation map at D = 0) against FP64.
 
     nt: steps (default: the workload's own); ckpt_k: the library's checkpoint
     interval (default: the workload's); path: the library's kernel path.
+    C: scalar constants to evaluate at (default: the seeded initial guess).
     fp32_floor: also run the oracle in FP32 (FP32 fields and arithmetic, FP64
     sums) and report its gradient error against FP64, the error any FP32
     evaluation of this scheme can be expected to carry.  For the degradation
@@ -87,7 +88,8 @@ def workload_errors(w, device, nt=None, ckpt_k=None, path=0, oracle_k=None, fp32
         D = torch.zeros((w.nx, w.ny), device=device, requires_grad=True)
         ux, uy = E.propagate(C, rho, geom, D=D)
     else:
-        C = torch.tensor(Hn.initial_guess(w), dtype=torch.float32, device=device, requires_grad=True)
+        C0 = Hn.initial_guess(w) if C is None else np.asarray(C, np.float64)
+        C = torch.tensor(C0, dtype=torch.float32, device=device, requires_grad=True)
         D = None
         ux, uy = E.propagate(C, rho, geom)
     loss = Hn.trace_misfit(ux, uy, obs[0], obs[1])

@@ -73,3 +73,24 @@ def test_damage512_full_grid():
     assert r["fwd_rel_err"] <= FWD_TOL, r
     assert r["grad_rel_err_same_residual"] <= GRAD_TOL, r
     assert r["grad_rel_err"] <= max(GRAD_TOL, 2.0 * r["oracle_fp32_grad_rel_err"]), r
+
+
+@pytest.mark.parametrize("path", [E.PATH_RESIDENT, E.PATH_TILED])
+def test_gradient_near_convergence(path):
+    # Close to the minimum the residual is small and the gradient is most
+    # sensitive to how the FP32 forward rounds.  One of the multi-instance
+    # configuration's grids (256^2, 1331 steps) at constants 0.2 % from the
+    # truth: the load joins the operator sum before the update (as in the
+    # reference's (A u + f) / rho), which keeps the end-to-end gradient
+    # within the bound (added after the update, an FP32 emulation of the same
+    # case gave 5e-4 .. 3e-3).
+    import numpy as np
+    w = Wk.multi_instances(64)[3]
+    assert (w.nx, w.nt) == (256, 1331)
+    rng = np.random.default_rng(11)
+    C = w.C_true * (1 + 2e-3 * rng.standard_normal(6))
+    r = workload_errors(w, DEV, path=path, C=C)
+    print(w.name, r)
+    assert r["fwd_rel_err"] <= FWD_TOL, r
+    assert r["grad_rel_err_same_residual"] <= GRAD_TOL, r
+    assert r["grad_rel_err"] <= GRAD_TOL, r
