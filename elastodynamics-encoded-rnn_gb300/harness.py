@@ -571,6 +571,20 @@ class CanvasInversion(_GraphedIteration):
         return self.params().detach().double().cpu().numpy()
 
 
+def split_by_work(ws, parts, nt=None):
+    """Instances split into `parts` lists of about equal work (cell-steps):
+    largest first, each to the currently lightest part.  Returns the lists of
+    instance numbers (ascending), empty parts dropped."""
+    work = [w.nx * w.ny * (w.nt if nt is None else min(w.nt, nt)) for w in ws]
+    load = [0] * parts
+    members = [[] for _ in range(parts)]
+    for k in sorted(range(len(ws)), key=lambda k: (-work[k], k)):
+        p = min(range(parts), key=lambda q: (load[q], q))
+        members[p].append(k)
+        load[p] += work[k]
+    return [sorted(m) for m in members if m]
+
+
 class CanvasSet(_GraphedIteration):
     """The instances split into `parts` canvases of about equal work
     (cell-steps, largest first to the lightest part), each a CanvasInversion
@@ -581,14 +595,7 @@ class CanvasSet(_GraphedIteration):
     def __init__(self, ws, device, parts=2, lr=1e-2, seed=0, graph=True, nt=None):
         self.device = device
         self.ws = ws
-        work = [w.nx * w.ny * (w.nt if nt is None else min(w.nt, nt)) for w in ws]
-        load = [0] * parts
-        members = [[] for _ in range(parts)]
-        for k in sorted(range(len(ws)), key=lambda k: -work[k]):
-            p = min(range(parts), key=lambda q: load[q])
-            members[p].append(k)
-            load[p] += work[k]
-        self.members = [sorted(m) for m in members if m]
+        self.members = split_by_work(ws, parts, nt)
         # each canvas's tape and scratch from its share of the memory budget
         self.parts = [CanvasInversion([ws[k] for k in m], device, lr=lr, seed=seed, graph=False, nt=nt,
                                       budget_fraction=0.4 / len(self.members))
