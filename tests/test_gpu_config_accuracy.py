@@ -10,8 +10,8 @@ steps (the FP64 CPU run of 4000 steps of sixteen 1024^2 shots would take
 hours), still long enough for several checkpoint segments and, on the tiled
 path, the two-step recompute.
 
-Bounds (the benchmark spec): forward relative L2 <= 1e-4 against
-FP64, gradient relative error <= 1e-4.
+Bounds (the accuracy this library promises for its FP32 path): forward
+relative L2 <= 1e-4 against FP64, gradient relative error <= 1e-4.
 """
 import pytest
 import torch

@@ -1,8 +1,8 @@
 """CUDA path vs the oracle and vs the reference's golden vectors (GPU only).
 
-Tolerances (stated by the benchmark spec): forward relative L2 error
-<= 1e-4 against the FP64 run of the same scheme, gradient relative error
-<= 1e-4.  The FP32 CUDA path typically lands near 1e-6.
+Tolerances: forward relative L2 error <= 1e-4 against the FP64 run of the
+same scheme, gradient relative error <= 1e-4 (the accuracy this library
+promises for its FP32 path).  The FP32 CUDA path typically lands near 1e-6.
 """
 import ctypes
 import os
