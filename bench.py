@@ -523,7 +523,7 @@ ERR_SAMPLE_STEPS = 160
 
 def config_errors(args, dev):
     """Forward-trace and gradient error of the benchmarked workload against
-    the FP64 run of the same scheme (oracle/accuracy.py, the checker): same
+    the FP64 run of the same scheme (oracle/accuracy.py): same
     grid, shots, receivers, constants, checkpoint interval and kernel path."""
     from oracle.accuracy import workload_errors
     w = make_workload(args)
@@ -608,7 +608,7 @@ def canvas_set_grad_errors(inv, dev, count=64):
 
 def canvas_grad_errors(inv, dev, count=64, select=None):
     """Per-instance trace and gradient error of the canvas iteration against
-    the FP64 C oracle (oracle/accuracy.py, the checker), every instance on
+    the FP64 C oracle (oracle/accuracy.py), every instance on
     its own grid with its own steps, at the instances' current constants, for
     the misfit of the canvas objective (S x mean over the padded traces) and
     the same observations.  Instances are checked smallest first (or the

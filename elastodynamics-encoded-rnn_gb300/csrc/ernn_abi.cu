@@ -383,7 +383,7 @@ const char* ernn_error_string(int code) {
     case ERNN_ERR_CUDA: return "CUDA runtime call failed";
     case ERNN_ERR_UNSTABLE: return "leapfrog stability bound violated for these constants";
     case ERNN_ERR_TIMEOUT: return "bounded device-side wait timed out";
-    case ERNN_ERR_UNSUPPORTED: return "request not supported by this build";
+    case ERNN_ERR_UNSUPPORTED: return "request not supported by this library";
     default: return "unknown error code";
   }
 }

@@ -41,7 +41,7 @@ enum {
   ERNN_ERR_CUDA = 3,        /* a CUDA runtime call failed */
   ERNN_ERR_UNSTABLE = 4,    /* leapfrog stability bound violated */
   ERNN_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
-  ERNN_ERR_UNSUPPORTED = 6  /* valid request this build cannot serve */
+  ERNN_ERR_UNSUPPORTED = 6  /* valid request this library cannot serve */
 };
 
 enum {

@@ -1,5 +1,5 @@
 """Forward-trace and gradient error of a benchmark workload against the FP64
-run of the same scheme (test infrastructure: the checker, never the product).
+run of the same scheme (test infrastructure: the oracle, never the product).
 
 ORACLE: only tests/, __graft_entry__.smoke() and bench.py's CPU leg use it.
 

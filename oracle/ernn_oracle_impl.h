@@ -1,6 +1,6 @@
 /*
  * CPU restatement of the ERNN finite-difference cell and its exact discrete
- * adjoint.  TEST INFRASTRUCTURE ONLY: this file is the checker that the CUDA
+ * adjoint.  TEST INFRASTRUCTURE ONLY: this file is the oracle that the CUDA
  * path is compared against.  It is never linked into the product library.
  *
  * Included twice by ernn_oracle.c, once with REAL=float (the precision the

@@ -1,6 +1,6 @@
 """ctypes front end of the FEM generator oracle (test infrastructure only).
 
-ORACLE: the checker the CUDA FEM kernels are compared against; only tests/
+ORACLE: the oracle the CUDA FEM kernels are compared against; only tests/
 and __graft_entry__.smoke() import it.  The C restatement
 (oracle/fem_oracle.c) follows Parameter_inversion/FEM_generate_data.py:117-527;
 its parity is pinned by tests/golden/fem*.npz from the reference solver.

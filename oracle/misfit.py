@@ -1,6 +1,6 @@
 """Misfit oracle (test infrastructure only).
 
-ORACLE: the checker the fused CUDA misfit (ernn_misfit / ernn_misfit_grad)
+ORACLE: the oracle the fused CUDA misfit (ernn_misfit / ernn_misfit_grad)
 is compared against; only tests/ import it.  A numpy restatement in FP64 of
   - compute_loss of the parameter inverter
     (Parameter_inversion/Inversion_adam.py:358-391): [:, ::ts, ::ss, ::ss] of

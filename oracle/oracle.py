@@ -1,6 +1,6 @@
 """ctypes front end of the C oracle (test infrastructure only).
 
-ORACLE: this module is the checker the CUDA path is compared against.  Only
+ORACLE: this module is the oracle the CUDA path is compared against.  Only
 tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import it.
 
 It restates the reference's forward time loop

@@ -1,6 +1,6 @@
 """bench.py's multi-process plumbing on CPU: world_size 2 over gloo.
 
-Every GPU machine of this project has one GPU, so N > 1 runs are replicas of the
+Each process of this project drives one GPU, so N > 1 runs are replicas of the
 single-GPU step (one process per GPU, no collective on the data path); what
 they share is the barrier and the max-over-ranks of the timed region, tested
 here with two CPU processes.
