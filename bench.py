@@ -677,26 +677,27 @@ def canvas_grad_errors(inv, dev, count=64, select=None):
             "worst": worst, "oracle_s": round(time.perf_counter() - t0, 1), "per_instance": out}
 
 
-def multi_plain_autograd(inv, dev, nt=100, count=8):
+def multi_plain_autograd(ws, dev, nt=100, count=8):
     """The restated reference path with autograd on the GPU (FP32), looped over
-    `count` instances spread over the sizes, `nt` steps each: cell-steps per
-    second of forward + backward (the plain form config 5 compares with)."""
+    `count` of the instances `ws` spread over the sizes, `nt` steps each, at
+    their seeded initial guesses: cell-steps per second of forward + backward
+    (the plain form the multi-instance configuration compares with)."""
     import ernn_gb300.harness as Hn
     from oracle import torch_ref
-    order = sorted(range(len(inv.invs)), key=lambda k: inv.invs[k].w.nx)
+    order = sorted(range(len(ws)), key=lambda k: ws[k].nx)
     pick = [order[round(i * (len(order) - 1) / max(1, count - 1))] for i in range(count)]
     cells, secs = 0, 0.0
+    rho = torch.tensor(Hn.RHO, device=dev)
     for k in pick:
-        one = inv.invs[k]
-        g = one.geom
-        C = one.params().detach().clone().requires_grad_(True)
+        g = Hn.geometry(ws[k], dev)
+        C = torch.tensor(Hn.initial_guess(ws[k], k), dtype=torch.float32, device=dev, requires_grad=True)
         load = _dense_load(g, torch.float32, dev)
         sig = g.src_signal[:, :nt].contiguous()
         rec = g.rec_idx
         for rep in range(2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            px, py = torch_ref.propagate([C[i] for i in range(6)], one.rho, g.nx, g.ny, nt, g.h, g.dt,
+            px, py = torch_ref.propagate([C[i] for i in range(6)], rho, g.nx, g.ny, nt, g.h, g.dt,
                                          sig, load, g.stride, rec, g.src_comp)
             ((px.double() ** 2).mean() + (py.double() ** 2).mean()).backward()
             torch.cuda.synchronize()
@@ -704,8 +705,8 @@ def multi_plain_autograd(inv, dev, nt=100, count=8):
                 secs += time.perf_counter() - t0
                 cells += g.nx * g.ny * nt
     return {"value": round(cells / secs / 1e9, 5), "unit": "Gcell-steps/s",
-            "sample": f"{count} of {len(inv.invs)} instances (sides "
-                      f"{sorted(inv.invs[k].w.nx for k in pick)}), {nt} steps each, "
+            "sample": f"{count} of {len(ws)} instances (sides "
+                      f"{sorted(ws[k].nx for k in pick)}), {nt} steps each, "
                       f"PyTorch restatement of the reference path with autograd on the same GPU"}
 
 
@@ -791,11 +792,13 @@ def run_multi(args, dist):
     if dist.rank == 0 and not args.no_cpu_baseline:
         if args.grouped:
             extra["grad_error_vs_fp64"] = multi_grad_errors(inv)
-            extra["plain_autograd_loop"] = multi_plain_autograd(inv, dev)
+            extra["plain_autograd_loop"] = multi_plain_autograd(ws, dev)
         elif args.canvas_parts <= 1:
             extra["grad_error_vs_fp64"] = canvas_grad_errors(inv, dev, count=args.err_instances)
         else:
             extra["grad_error_vs_fp64"] = canvas_set_grad_errors(inv, dev, count=args.err_instances)
+        if not args.grouped:
+            extra["plain_autograd_loop"] = multi_plain_autograd(ws, dev)
     return {
         "metric": "Gcell-steps/s fwd+adj (hand adjoint, one Adam iteration)",
         "value": round(value, 4), "unit": "Gcell-steps/s", "n_gpus": dist.world,
