@@ -87,7 +87,10 @@ enum {
   /* Tiled kernels: 64 x 32 tiles for the forward steps and the scalar
    * adjoint instead of 64 x 16 (a tenth fewer halo rows per cell, one CTA
    * fewer per SM); a tile geometry the autotuner measures.  Results are the
-   * same up to FP32 rounding of the imaging sums' grouping. */
+   * same up to FP32 rounding of the imaging sums' grouping.  The D-field
+   * mode takes 64 x 32 tiles with or without the flag (its adjoint always
+   * did; its forward measured faster so: 8 x 512^2 shots, 81.3 -> 75.6 ms
+   * per inversion iteration). */
   ERNN_FLAG_TALL_TILES = 4
 };
 
