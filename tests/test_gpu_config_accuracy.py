@@ -75,7 +75,7 @@ def test_damage512_full_grid():
     assert r["grad_rel_err"] <= max(GRAD_TOL, 2.0 * r["oracle_fp32_grad_rel_err"]), r
 
 
-@pytest.mark.parametrize("path", [E.PATH_RESIDENT, E.PATH_TILED])
+@pytest.mark.parametrize("path", [E.PATH_RESIDENT, E.PATH_TILED, E.PATH_STEP])
 def test_gradient_near_convergence(path):
     # Close to the minimum the residual is small and the gradient is most
     # sensitive to how the FP32 forward rounds.  One of the multi-instance
