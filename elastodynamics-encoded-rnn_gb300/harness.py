@@ -79,7 +79,8 @@ class _GraphedIteration:
     iteration up on a side stream (allocator pools, library caches, the
     checkpoint choice), then records one iteration — the library's time
     loops, the misfit, the adjoint and the optimiser step — as one graph;
-    `step(obs)` copies new observations into the captured input tensors and
+    `step(obs)` copies new observations (host tensors, pinned for an
+    asynchronous copy, or device tensors) into the captured input tensors and
     replays it.  `step_eager()` runs the same iteration without the graph."""
 
     graph = None
