@@ -255,6 +255,18 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
   }
   grid_dep_wait();
 
+  // the own cells of u^{i-1}, issued with the staging loads (one memory
+  // round before the barrier instead of a second one after it)
+  const float* prev = a.prev ? a.prev + (size_t)s * 2 * N : nullptr;
+  float pxv[RPT_], pyv[RPT_];
+#pragma unroll
+  for (int k = 0; k < RPT_; ++k) {
+    const int gi = x0 + ty + (NTHR / TY) * k;
+    const bool in = prev != nullptr && gi < nx && gj < ny;
+    const size_t o = in ? (size_t)gi * ny + gj : 0;
+    pxv[k] = in ? prev[o] : 0.f;
+    pyv[k] = in ? prev[N + o] : 0.f;
+  }
   const float* cur = a.cur ? a.cur + (size_t)s * 2 * N : nullptr;
   stage_pair<T>(sx, sy, cur, nx, ny, N, x0, y0, tid);
 
@@ -270,7 +282,6 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
   }
   __syncthreads();
 
-  const float* prev = a.prev ? a.prev + (size_t)s * 2 * N : nullptr;
   float* out = a.out + (size_t)s * 2 * N;
 #pragma unroll
   for (int k = 0; k < RPT_; ++k) {
@@ -297,10 +308,8 @@ __global__ void __launch_bounds__(NTHR) fwd_step_kernel(const FwdStep a) {
       const float f = a.src_map[((size_t)s * a.bx + sa) * a.by + sb];  // L + amp f, one rounding
       if (a.src_comp == 0) lx = fmaf(amp, f, lx); else ly = fmaf(amp, f, ly);
     }
-    const float px = prev ? prev[o] : 0.f;
-    const float py = prev ? prev[N + o] : 0.f;
-    const float vx = (2.f * st.cx - px) + lx;
-    const float vy = (2.f * st.cy - py) + ly;
+    const float vx = (2.f * st.cx - pxv[k]) + lx;
+    const float vy = (2.f * st.cy - pyv[k]) + ly;
     out[o] = vx;
     out[N + o] = vy;
     if (a.copy0) {
@@ -358,7 +367,33 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
 #pragma unroll
     for (int it = 0; it < kIt; ++it) staged_field(tid + it * NTHR, fpre[kPre ? it : 0]);
   }
+  // The own cells' dense adjoint source (written before the step loop, so
+  // loaded before the wait) and, after it, their lam^{m+1} and lam^{m+2},
+  // issued with the staging loads: one memory round before the barrier.
+  const int gj = y0 + tx;
+  const bool dense_src = a.frame >= 0 && a.record == kRecordFields;
+  float gvx[RPT_], gvy[RPT_];
+#pragma unroll
+  for (int k = 0; k < RPT_; ++k) {
+    const int gi = x0 + ty + (NTHR / TY) * k;
+    const bool in = dense_src && gi < nx && gj < ny;
+    const size_t go = in ? ((size_t)s * a.nt_out + a.frame) * N + (size_t)gi * ny + gj : 0;
+    gvx[k] = in ? a.g_x[go] : 0.f;
+    gvy[k] = in ? a.g_y[go] : 0.f;
+  }
   grid_dep_wait();
+  const float* prev = a.prev + (size_t)s * 2 * N;
+  float l1x_[RPT_], l1y_[RPT_], pvx[RPT_], pvy[RPT_];
+#pragma unroll
+  for (int k = 0; k < RPT_; ++k) {
+    const int gi = x0 + ty + (NTHR / TY) * k;
+    const bool in = gi < nx && gj < ny;
+    const size_t o = in ? (size_t)gi * ny + gj : 0;
+    l1x_[k] = in ? cur[o] : 0.f;
+    l1y_[k] = in ? cur[N + o] : 0.f;
+    pvx[k] = in ? prev[o] : 0.f;
+    pvy[k] = in ? prev[N + o] : 0.f;
+  }
 #pragma unroll
   for (int it = 0; it < kIt; ++it) {
     const int e = tid + it * NTHR;
@@ -408,9 +443,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
   KS ks;
   if (MODE != kModeFields) ks = load_ks(K);
   const float gs = K->gscale;
-  const float* prev = a.prev + (size_t)s * 2 * N;
   float* out = a.out + (size_t)s * 2 * N;
-  const int gj = y0 + tx;
   float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // this thread's cells, one step
   float nvx[RPT_], nvy[RPT_];
 #pragma unroll
@@ -421,7 +454,7 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
     const int gi = x0 + r;
     if (gi >= nx || gj >= ny) continue;
     const size_t o = (size_t)gi * ny + gj;
-    const float l1x = cur[o], l1y = cur[N + o];
+    const float l1x = l1x_[k], l1y = l1y_[k];
     float ax, ay;
     if (MODE == kModeFields) {
       const float xx0 = (sl[0][r][tx + 1] + sl[0][r + 2][tx + 1]) - 2.f * sl[0][r + 1][tx + 1];
@@ -436,13 +469,11 @@ __global__ void __launch_bounds__(NTHR) adj_step_kernel(const AdjStep a) {
       const Sten sw = stencils(sl[0], sl[1], r, tx);
       apply_ks(ks, sw, ax, ay);
     }
-    const float px = prev[o], py = prev[N + o];
-    float vx = (2.f * l1x - px) + ax;
-    float vy = (2.f * l1y - py) + ay;
-    if (a.frame >= 0 && a.record == kRecordFields) {
-      const size_t go = ((size_t)s * a.nt_out + a.frame) * N + o;
-      vx += gs * a.g_x[go];
-      vy += gs * a.g_y[go];
+    float vx = (2.f * l1x - pvx[k]) + ax;
+    float vy = (2.f * l1y - pvy[k]) + ay;
+    if (dense_src) {
+      vx += gs * gvx[k];
+      vy += gs * gvy[k];
     }
     nvx[k] = vx;
     nvy[k] = vy;
