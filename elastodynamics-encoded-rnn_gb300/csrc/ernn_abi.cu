@@ -126,6 +126,14 @@ int validate(const ErnnProblem* p) {
     return ERNN_ERR_INVALID;
   if (!(p->h > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->h) || !std::isfinite(p->dt))
     return ERNN_ERR_INVALID;
+  // Sizes that the plan forms in 64-bit (states of the tape and scratch: at
+  // most nt + 2 ckpt_k + 2 resident segments + a few) and in 32-bit (blocks
+  // of one plain step launch) must not wrap: such a problem is refused
+  // instead of being given a workspace size that is too small.
+  const double state_bytes =
+      (double)((p->flags & ERNN_FLAG_INSTANCES) ? 1 : p->nshots) * 2.0 * (double)p->nx * p->ny * 4.0;
+  if (state_bytes * (3.0 * (double)p->nt + 16.0) >= 4.0e18) return ERNN_ERR_INVALID;
+  if ((double)p->nshots * ((p->nx + 7) / 8) * ((p->ny + 31) / 32) >= 2.0e9) return ERNN_ERR_INVALID;
   return ERNN_OK;
 }
 

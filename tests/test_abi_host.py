@@ -66,6 +66,24 @@ def test_validation_rejects_bad_problems():
     assert lib.ernn_validate(None) == 1
 
 
+def test_sizes_that_would_wrap_are_refused():
+    """A problem whose tape or scratch size would not fit in 64 bits, or whose
+    plain step launch would have more blocks than an int counts, is invalid
+    and its size queries return 0 (never a wrapped, too small size)."""
+    lib = E.load_library()
+    huge_tape = dict(nshots=65535, nx=46340, ny=46340, nt=2 ** 30, ckpt_k=2 ** 30)
+    many_blocks = dict(nshots=65535, nx=46340, ny=46340, nt=1, ckpt_k=1)
+    for kw in (huge_tape, many_blocks):
+        p = _problem(**kw)
+        assert lib.ernn_validate(ctypes.byref(p)) == 1, kw
+        assert lib.ernn_tape_bytes(ctypes.byref(p), 1) == 0
+        assert lib.ernn_adjoint_scratch_bytes(ctypes.byref(p)) == 0
+    # a large problem within the bounds still gets its exact size
+    ok = _problem(nshots=16, nx=1024, ny=1024, nt=4000, ckpt_k=4000)
+    assert lib.ernn_validate(ctypes.byref(ok)) == 0
+    assert lib.ernn_tape_bytes(ctypes.byref(ok), 1) >= 4000 * 16 * 2 * 1024 * 1024 * 4
+
+
 def test_instance_workspace_holds_one_canvas_plane():
     # with instances the state is one canvas plane, not one per shot, and the
     # tape and scratch hold the tile table (and the scratch a zero state)
