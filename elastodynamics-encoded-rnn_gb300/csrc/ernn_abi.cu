@@ -340,8 +340,8 @@ int plan_instances(const ErnnProblem& p, const ErnnInstances* in, InstPlan* ip) 
   const int S = in->count;
   for (int k = 0; k < S; ++k) {
     const int x0 = in->x0[k], y0 = in->y0[k], nx = in->nx[k], ny = in->ny[k], nt = in->nt[k];
-    if (x0 < 0 || y0 < 0 || nx < 1 || ny < 4 || y0 % 4 != 0 || ny % 4 != 0 || x0 + nx > p.nx ||
-        y0 + ny > p.ny || nt < 1 || nt > p.nt)
+    if (x0 < 0 || y0 < 0 || nx < 1 || ny < 4 || y0 % 4 != 0 || ny % 4 != 0 || (int64_t)x0 + nx > p.nx ||
+        (int64_t)y0 + ny > p.ny || nt < 1 || nt > p.nt)  // (64-bit sums: no wrap past the canvas)
       return ERNN_ERR_INVALID;
   }
   // regions at least one cell apart: those cells stay zero, the instances'

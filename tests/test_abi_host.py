@@ -84,6 +84,33 @@ def test_sizes_that_would_wrap_are_refused():
     assert lib.ernn_tape_bytes(ctypes.byref(ok), 1) >= 4000 * 16 * 2 * 1024 * 1024 * 4
 
 
+def test_instance_regions_are_checked_before_any_device_work():
+    """Regions past the canvas (also where x0 + nx overflows 32 bits),
+    overlapping or touching regions, and step counts above nt are refused
+    on the host.  The inputs are placeholders that are never dereferenced and
+    the tape is given as 0 bytes, so valid regions stop at the workspace
+    check (ERNN_ERR_WORKSPACE) and bad ones at the region check
+    (ERNN_ERR_INVALID), both before any CUDA call."""
+    lib = E.load_library()
+    p = _problem(flags=2, nshots=2, nx=256, ny=256, nt=100)
+    dummy = ctypes.c_void_p(16)  # non-null placeholder, never dereferenced on these paths
+    ins = E._lib.ErnnInputs(dummy, None, dummy, dummy, dummy, dummy, dummy)
+
+    def call(x0, y0, nx, ny, nt):
+        arr = lambda v: (ctypes.c_int32 * 2)(*v)
+        inst = E._lib.ErnnInstances(2, arr(x0), arr(y0), arr(nx), arr(ny), arr(nt))
+        return lib.ernn_forward_instances(ctypes.byref(p), ctypes.byref(ins), ctypes.byref(inst), dummy, dummy,
+                                          dummy, 0, 1, None)
+    assert call((0, 20), (0, 0), (10, 10), (16, 16), (100, 60)) == 2  # valid: only the tape is short
+    bad = [((0, 2 ** 31 - 8), (0, 0), (10, 16), (16, 16), (100, 100)),   # x0 + nx wraps
+           ((0, 0), (0, 2 ** 31 - 4), (10, 10), (16, 8), (100, 100)),    # y0 + ny wraps
+           ((0, 250), (0, 0), (10, 10), (16, 16), (100, 100)),           # past the canvas
+           ((0, 10), (0, 0), (10, 10), (16, 16), (100, 100)),            # no ghost row between
+           ((0, 20), (0, 0), (10, 10), (16, 16), (100, 101))]            # more steps than nt
+    for args in bad:
+        assert call(*args) == 1, args
+
+
 def test_instance_workspace_holds_one_canvas_plane():
     # with instances the state is one canvas plane, not one per shot, and the
     # tape and scratch hold the tile table (and the scratch a zero state)
