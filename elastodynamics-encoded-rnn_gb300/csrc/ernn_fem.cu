@@ -202,8 +202,9 @@ extern "C" size_t ernn_fem_workspace_bytes(const ErnnFemProblem* p) {
 extern "C" int ernn_fem_forward(const ErnnFemProblem* p, const float* load, const float* signal,
                                 const float* C_fields, float* frames_x, float* frames_y,
                                 void* workspace, size_t workspace_bytes, void* stream) {
+  // (the per-level launch takes 8 node rows per block along grid y: at most 65535 blocks)
   if (p == nullptr || p->nx < 2 || p->ny < 2 || p->nt < 1 || p->stride < 1 ||
-      (int64_t)p->nx * p->ny >= ((int64_t)1 << 31))
+      (int64_t)p->nx * p->ny >= ((int64_t)1 << 31) || (p->nx + 7) / 8 > 65535)
     return ERNN_ERR_INVALID;
   if (!(p->dx > 0.0) || !(p->dy > 0.0) || !(p->dt > 0.0) || !(p->rho > 0.0) ||
       !std::isfinite(p->dx) || !std::isfinite(p->dy) || !std::isfinite(p->dt) ||

@@ -202,6 +202,8 @@ int validate_series(const ErnnSeries* s) {
       s->frame_stride < 1 || s->space_stride < 1)
     return ERNN_ERR_INVALID;
   if (!(s->wx >= 0.0) || !(s->wy >= 0.0)) return ERNN_ERR_INVALID;  // also rejects NaN
+  // element counts are formed in 64-bit: refuse series that would wrap them
+  if ((double)s->series * (double)s->frames * (double)s->nx * (double)s->ny >= 4.0e18) return ERNN_ERR_INVALID;
   return ERNN_OK;
 }
 

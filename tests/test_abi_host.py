@@ -279,6 +279,25 @@ def test_series_misfit_validates_on_the_host():
         series_misfit(torch.zeros(3), torch.zeros(3), torch.zeros(3), torch.zeros(3))
 
 
+def test_abi_refuses_series_and_fem_grids_beyond_its_bounds():
+    """Host-side refusals made before any CUDA call: a misfit series whose
+    element count would wrap 64 bits, a FEM grid whose per-level launch
+    would exceed the 65535 blocks of grid y."""
+    lib = E.load_library()
+    dummy = ctypes.c_void_p(16)  # non-null placeholder, never dereferenced on these paths
+    huge = E._lib.ErnnSeries(2 ** 40, 2 ** 30, 2 ** 20, 2 ** 20, 1, 1, 1.0, 1.0)
+    assert lib.ernn_misfit(ctypes.byref(huge), dummy, dummy, dummy, dummy, dummy, dummy,
+                           lib.ernn_misfit_workspace_bytes(), None) == 1
+    assert lib.ernn_misfit_grad(ctypes.byref(huge), dummy, dummy, dummy, dummy, None, dummy, dummy, None) == 1
+    ok = E._lib.ErnnSeries(2, 10, 1, 64, 1, 1, 1.0, 1.0)
+    assert lib.ernn_misfit(ctypes.byref(ok), dummy, dummy, dummy, dummy, dummy, dummy, 0, None) == 2
+    C6 = (ctypes.c_double * 6)(1e9, 1e9, 1e9, 0.0, 0.0, 1e9)
+    tall = E._lib.ErnnFemProblem(524289, 3, 10, 1, 1e-3, 1e-3, 1e-8, 1.0, C6, 0.7)
+    assert lib.ernn_fem_forward(ctypes.byref(tall), dummy, dummy, None, dummy, dummy, dummy, 2 ** 40, None) == 1
+    fits = E._lib.ErnnFemProblem(524280, 3, 10, 1, 1e-3, 1e-3, 1e-8, 1.0, C6, 0.7)
+    assert lib.ernn_fem_forward(ctypes.byref(fits), dummy, dummy, None, dummy, dummy, dummy, 0, None) == 2
+
+
 def test_fused_adam_rejects_bad_hyper_parameters():
     from ernn_gb300.optim import FusedAdam
     p = torch.zeros(3, requires_grad=True)
