@@ -303,9 +303,13 @@ class ErnnPropagate(torch.autograd.Function):
                                       int(want_grad), _stream())
                 _lib.check("ernn_forward", rc)
             _STATUS.enqueue("ernn_forward", prob, tape, 0)
-        ctx.geom = geom
         ctx.mode = mode
-        ctx.flags = flags
+        # the problem as the tape was laid out: a later change of the geometry
+        # (its checkpoint interval, say) must not change how backward reads it
+        ctx.prob = _lib.ErnnProblem.from_buffer_copy(prob)
+        ctx.out_shape = geom.out_shape()
+        ctx.srcs = (geom.src_signal, geom.src_map, geom.src_origin, geom.rec_idx)
+        ctx.inst = inst
         ctx.tape = tape if want_grad else None
         ctx.save_for_backward(C, D, rho)
         return out_ux, out_uy
@@ -313,29 +317,30 @@ class ErnnPropagate(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g_ux, g_uy):
         C, D, rho = ctx.saved_tensors
-        geom, mode = ctx.geom, ctx.mode
+        mode = ctx.mode
         if ctx.tape is None:
             return None, None, None, None, None
         dev = C.device
-        shape = geom.out_shape()
+        shape = ctx.out_shape
         g_ux = torch.zeros(shape, device=dev) if g_ux is None else g_ux.to(torch.float32).contiguous()
         g_uy = torch.zeros(shape, device=dev) if g_uy is None else g_uy.to(torch.float32).contiguous()
         lib = _lib.load()
-        prob = geom.problem(mode, ctx.flags)
+        prob = ctx.prob
         scratch_bytes = lib.ernn_adjoint_scratch_bytes(ctypes.byref(prob))
         with torch.cuda.device(dev):
             scratch = torch.empty(scratch_bytes, dtype=torch.uint8, device=dev)
             grad_C64 = torch.empty(tuple(C.shape), dtype=torch.float64, device=dev) \
                 if mode == MODE_SCALAR else None
             if mode == MODE_FIELDS:
-                grad_field = torch.empty((6, geom.nx, geom.ny), dtype=torch.float32, device=dev)
+                grad_field = torch.empty((6, prob.nx, prob.ny), dtype=torch.float32, device=dev)
             elif mode == MODE_DFIELD:
-                grad_field = torch.empty((geom.nx, geom.ny), dtype=torch.float32, device=dev)
+                grad_field = torch.empty((prob.nx, prob.ny), dtype=torch.float32, device=dev)
             else:
                 grad_field = None
-            ins = _inputs(geom, C, D, rho)
-            if geom.instances is not None:
-                ist = geom.instances.c_struct()
+            sig, smap, sorg, rec = ctx.srcs
+            ins = _lib.ErnnInputs(_ptr(C), _ptr(D), _ptr(rho), _ptr(sig), _ptr(smap), _ptr(sorg), _ptr(rec))
+            if ctx.inst is not None:
+                ist = ctx.inst.c_struct()
                 rc = lib.ernn_adjoint_instances(ctypes.byref(prob), ctypes.byref(ins), ctypes.byref(ist),
                                                 _ptr(g_ux), _ptr(g_uy), _ptr(ctx.tape),
                                                 ctypes.c_size_t(ctx.tape.numel()), _ptr(scratch),
