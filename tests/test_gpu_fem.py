@@ -93,10 +93,9 @@ def test_damaged_plate_matches_reference_solver(tmp_path):
         assert int(z["damage_info/total_damaged_points"]) == int(g["damage_mask"].sum())
 
 
-def _plate(nx, ny, nt, fields=False, seed=0):
+def _plate(nx, ny, nt):
     """Arguments of fem_frames for a Gaussian load near the centre of an
-    nx x ny plate, and (fields) per-node constants between 0.5 and 1 times
-    the uniform ones."""
+    nx x ny plate with the constants of the larger-grid test."""
     dx = dy = 1e-3
     x = np.linspace(-(nx - 1) * dx / 2, (nx - 1) * dx / 2, nx)
     y = np.linspace(-(ny - 1) * dy / 2, (ny - 1) * dy / 2, ny)
@@ -104,18 +103,13 @@ def _plate(nx, ny, nt, fields=False, seed=0):
     load = EF.gaussian_point_load(X, Y, 0.004, -0.003, 5e5).astype(np.float32)
     sig = EF.ricker_wavelet(np.arange(nt) * 5e-8, 500e3, 2e-6, 1e10).astype(np.float32)
     C = (130.74e9, 11.5e9, 10.49e9, 30.67e9, 3.75e9, 14.77e9)
-    cf = None
-    if fields:
-        rng = np.random.default_rng(seed)
-        cf = (np.asarray(C, dtype=np.float64)[:, None, None] *
-              rng.uniform(0.5, 1.0, size=(6, nx, ny))).astype(np.float32)
-    return (nx, ny, nt, dx, dy, 5e-8, 1610.0, C, load, sig), cf
+    return nx, ny, nt, dx, dy, 5e-8, 1610.0, C, load, sig
 
 
 def test_fem_frames_match_fp64_oracle_generator_grid():
     """The generator's 301^2 grid, 300 levels, against the FP64 restatement
     of the generator loop."""
-    args, _ = _plate(301, 301, 300)
+    args = _plate(301, 301, 300)
     fx, fy = EF.fem_frames(*args, stride=5)
     ox, oy = OF.fem_forward(*args, stride=5)
     ex, ey = rel(fx.cpu().numpy(), ox), rel(fy.cpu().numpy(), oy)
