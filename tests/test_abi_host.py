@@ -30,6 +30,25 @@ def test_library_exports_every_declared_symbol():
     assert set(names) <= set(E._lib.SIGNATURES)
 
 
+def test_c_program_uses_the_abi_without_python(tmp_path):
+    """tests/abi_c/ernn_abi_host.c, compiled as strict C99 against
+    include/ernn.h and linked to the library, runs the host-side entry points
+    (validation, size queries, stability check, error strings) from C."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc absent")
+    E.load_library()  # builds the library when it is missing
+    libdir = os.path.dirname(E._lib.library_path())
+    exe = str(tmp_path / "ernn_abi_host")
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                    "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "abi_c", "ernn_abi_host.c"),
+                    "-L", libdir, "-lernn_gb300", f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
+
+
 def test_struct_layout_matches_header():
     # ErnnProblem: 14 int32 then 2 doubles = 72 bytes; ErnnInputs: 7 pointers
     assert ctypes.sizeof(E._lib.ErnnProblem) == 72
