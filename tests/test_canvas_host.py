@@ -50,3 +50,27 @@ def test_split_by_work_balances_and_covers():
     assert Hn.split_by_work(ws, 2) == Hn.split_by_work(ws, 2)  # deterministic
     # fewer instances than parts: empty parts are dropped
     assert len(Hn.split_by_work(ws[:2], 4)) == 2
+
+
+def test_canvas_layout_random_instance_sets():
+    """Seeded random sets of 1-40 instances (heights 4-300, widths multiples
+    of 4 up to 300): every placement satisfies what the library checks for
+    ERNN_FLAG_INSTANCES (inside the canvas, canvas width and first columns
+    multiples of 4, any two regions at least one row or one column apart)
+    plus the layout's own alignment and gap."""
+    from types import SimpleNamespace
+    rng = np.random.default_rng(7)
+    for _ in range(200):
+        n = int(rng.integers(1, 41))
+        ws = [SimpleNamespace(nx=int(rng.integers(4, 301)), ny=4 * int(rng.integers(1, 76))) for _ in range(n)]
+        for align in (32, 4):
+            X, Y, x0, y0 = Hn.canvas_layout(ws, col_align=align)
+            # the canvas width: a multiple of the alignment (so of 4, as the
+            # tiled kernels need), below the 16-bit limit of the tile table
+            assert Y % align == 0 and Y % 4 == 0 and X <= 65535 and Y <= 65535
+            r = _rects(ws, x0, y0)
+            for k, (a0, b0, a1, b1) in enumerate(r):
+                assert 0 <= a0 and a1 <= X and 0 <= b0 and b1 <= Y
+                assert b0 % align == 0
+                for (c0, d0, c1, d1) in r[k + 1:]:
+                    assert a1 + 1 <= c0 or c1 + 1 <= a0 or b1 + 4 <= d0 or d1 + 4 <= b0
